@@ -1,0 +1,385 @@
+// Table builders, detection post-processing and the legacy-input beamformer.
+//
+//  * tables: geometric phase (geometry.c:40-101), inverse Jones
+//    (jones.c:97-157) and their product, the per-(tile, channel) weight
+//    W = phi J^-1 the beam kernels apply. FP64 on the device, W rounded to FP32.
+//  * renormalise: per-channel min/max scale-and-offset to 8 bits
+//    (form_beam.cpp:408-449), writing the spliced multi-channel layout
+//    directly when asked.
+//  * incoherent beam of 4+4-bit legacy voltages (form_beam.cpp:60-87).
+//  * beamformer for fine-channel voltages already in legacy layout
+//    (v_IDX [s][c][i], 4+4-bit or complex FP64): vmApplyJ_kernel followed by
+//    vmBeamform_kernel (form_beam.cpp:122-371) in one pass.
+#include "vgb_internal.cuh"
+
+namespace vgb {
+
+// ---------------------------------------------------------------------------
+// FP64 complex helpers with cuCmul's operation order.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 zmul(double2 a, double2 b)
+{
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 zadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 zsub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+
+// geometry.c:40-101 for one (pointing, tile, channel): phase terms use the
+// reference's order of operations, 2*pi*dt*f.
+__global__ void phase_kernel(const double *unit, const double *east, const double *north, const double *height,
+                             const double *cable, const double *freqs, int npointing, int nant, int nchan,
+                             double href, double2 *phi)
+{
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long n = (long long)npointing * nant * nchan;
+    if (idx >= n) return;
+    const int c = idx % nchan;
+    const int a = (idx / nchan) % nant;
+    const int p = idx / ((long long)nchan * nant);
+    const double L = cable[a] - 0.0;
+    const double w = (east[a] - 0.0) * unit[3 * p + 0] + (north[a] - 0.0) * unit[3 * p + 1] +
+                     (height[a] - href) * unit[3 * p + 2];
+    const double dt = (w - L) / 299792458.0;
+    const double f = (double)(uint32_t)freqs[c];
+    const double phase = 2.0 * 3.14159265358979323846 * dt * f;
+    double s, co;
+    sincos(phase, &s, &co);
+    phi[idx] = make_double2(co, s);
+}
+
+// jones.c:97-157: J = inv2x2S(D[a][c] B[p][a] / ||D B||_F), zero if the norm is 0.
+__global__ void jones_kernel(const double2 *D, const double2 *B, int npointing, int nant, int nchan, double2 *J)
+{
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long n = (long long)npointing * nant * nchan;
+    if (idx >= n) return;
+    const int c = idx % nchan;
+    const int a = (idx / nchan) % nant;
+    const int p = idx / ((long long)nchan * nant);
+    const double2 *d = D + 4 * ((long long)a * nchan + c);
+    const double2 *b = B + 4 * ((long long)p * nant + a);
+    double2 m[4];
+    m[0] = zadd(zmul(d[0], b[0]), zmul(d[1], b[2]));
+    m[1] = zadd(zmul(d[0], b[1]), zmul(d[1], b[3]));
+    m[2] = zadd(zmul(d[2], b[0]), zmul(d[3], b[2]));
+    m[3] = zadd(zmul(d[2], b[1]), zmul(d[3], b[3]));
+    double F = 0.0;
+    for (int i = 0; i < 4; i++) F += zmul(m[i], make_double2(m[i].x, -m[i].y)).x;
+    F = sqrt(F);
+    double2 *o = J + 4 * idx;
+    if (F == 0.0) {
+        for (int i = 0; i < 4; i++) o[i] = make_double2(0.0, 0.0);
+        return;
+    }
+    for (int i = 0; i < 4; i++) m[i] = make_double2(m[i].x / F, m[i].y / F);
+    const double2 det = zsub(zmul(m[0], m[3]), zmul(m[1], m[2]));
+    const double scale = 1.0 / (det.x * det.x + det.y * det.y);
+    const double2 inv = make_double2(scale * det.x, -scale * det.y);
+    const double2 ninv = make_double2(-inv.x, -inv.y);
+    o[0] = zmul(inv, m[3]);
+    o[1] = zmul(ninv, m[1]);
+    o[2] = zmul(ninv, m[2]);
+    o[3] = zmul(inv, m[0]);
+}
+
+// W[p][a][c] = phi[p][a][c] * J[p][a][c] in FP64, rounded to FP32 and stored
+// as two float4: (w00, w01), (w10, w11).
+__global__ void weights_kernel(const double2 *J, const double2 *phi, long long n, float4 *W)
+{
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= n) return;
+    const double2 ph = phi[idx];
+    const double2 *j = J + 4 * idx;
+    double2 w[4];
+    for (int i = 0; i < 4; i++) w[i] = zmul(ph, j[i]);
+    W[2 * idx] = make_float4((float)w[0].x, (float)w[0].y, (float)w[1].x, (float)w[1].y);
+    W[2 * idx + 1] = make_float4((float)w[2].x, (float)w[2].y, (float)w[3].x, (float)w[3].y);
+}
+
+int launch_phase(const double *unit, const double *east, const double *north, const double *height,
+                 const double *cable, const double *freqs, int npointing, int nant, int nchan, double href,
+                 double2 *phi, cudaStream_t st)
+{
+    const long long n = (long long)npointing * nant * nchan;
+    if (n == 0) return VGB_SUCCESS;
+    phase_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(unit, east, north, height, cable, freqs, npointing,
+                                                               nant, nchan, href, phi);
+    return check_launch("phase_kernel");
+}
+
+int launch_jones(const double2 *D, const double2 *B, int npointing, int nant, int nchan, double2 *J,
+                 cudaStream_t st)
+{
+    const long long n = (long long)npointing * nant * nchan;
+    if (n == 0) return VGB_SUCCESS;
+    jones_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(D, B, npointing, nant, nchan, J);
+    return check_launch("jones_kernel");
+}
+
+int launch_weights(const double2 *J, const double2 *phi, long long n, float4 *W, cudaStream_t st)
+{
+    if (n == 0) return VGB_SUCCESS;
+    weights_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(J, phi, n, W);
+    return check_launch("weights_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// renormalise_channels (form_beam.cpp:408-449)
+// ---------------------------------------------------------------------------
+struct RenormArgs {
+    const float *S;        // [cc][p][nstep][nstokes][nchan]
+    long long S_cc;
+    int npointing, nstep, nstokes, nchan;
+    uint8_t *out;          // out + cc*out_cc + p*out_p + s*out_s + st*out_st + c
+    long long out_cc, out_p, out_s, out_st;
+    float *offsets, *scales; // + cc*stat_cc + (p*nstokes + st)*nchan + c
+    long long stat_cc;
+};
+
+// The float -> uint8 conversion of form_beam.cpp:443, (uint8_t)(val + 0.5)
+// with val + 0.5 in FP64, as the reference's GPU build performs it: truncate
+// to an integer and keep the low 8 bits, so a channel's maximum sample
+// (256.5) becomes 0; NaN becomes 0. val is never negative here.
+__device__ __forceinline__ uint8_t sat_u8(double t)
+{
+    if (t != t || t <= 0.0) return 0;
+    return (uint8_t)((unsigned)t & 0xFFu);
+}
+
+// One warp lane per channel; the 8 warps of a block split the samples.
+__global__ void __launch_bounds__(256) renorm_kernel(const RenormArgs a)
+{
+    __shared__ float smin[8][32], smax[8][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int c = blockIdx.x * 32 + lane;
+    const int st = blockIdx.y % a.nstokes, p = blockIdx.y / a.nstokes;
+    const int cc = blockIdx.z;
+    const bool live = c < a.nchan;
+    const long long sstride = (long long)a.nstokes * a.nchan;
+    const float *S = a.S + cc * a.S_cc + ((long long)p * a.nstep * a.nstokes + st) * a.nchan + (live ? c : 0);
+
+    // Sequential-scan semantics of the reference: every partial starts from
+    // sample 0 and uses the same comparisons, so the result is the same.
+    const float s0 = S[0];
+    float mn = s0, mx = s0;
+    for (int s = wid; s < a.nstep; s += 8) {
+        const float v = S[s * sstride];
+        mn = (v < mn ? v : mn);
+        mx = (v > mx ? v : mx);
+    }
+    smin[wid][lane] = mn;
+    smax[wid][lane] = mx;
+    __syncthreads();
+    mn = smin[0][lane];
+    mx = smax[0][lane];
+    for (int w = 1; w < 8; w++) {
+        const float v0 = smin[w][lane], v1 = smax[w][lane];
+        mn = (v0 < mn ? v0 : mn);
+        mx = (v1 > mx ? v1 : mx);
+    }
+    const float scale = (float)((double)(mx - mn) / 256.0);
+    const float offset = mn;
+    if (live) {
+        uint8_t *o = a.out + cc * a.out_cc + p * a.out_p + st * a.out_st + c;
+        for (int s = wid; s < a.nstep; s += 8) {
+            const float v = (S[s * sstride] - offset) / scale;
+            o[s * a.out_s] = sat_u8((double)v + 0.5);
+        }
+        if (wid == 0) {
+            const long long si = cc * a.stat_cc + ((long long)p * a.nstokes + st) * a.nchan + c;
+            a.scales[si] = scale;
+            a.offsets[si] = offset;
+        }
+    }
+}
+
+int launch_renorm(const RenormArgs &a, int ncc, cudaStream_t st)
+{
+    if (a.nstep <= 0 || ncc <= 0) return VGB_SUCCESS;
+    dim3 grid((a.nchan + 31) / 32, a.npointing * a.nstokes, ncc);
+    renorm_kernel<<<grid, 256, 0, st>>>(a);
+    return check_launch("renorm_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// Incoherent beam of 4+4-bit voltages (form_beam.cpp:60-87): exact integer
+// sums of |v|^2 over all inputs. Eight lanes per (s, c) row of ninput bytes.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int nib(uint32_t x) { return ((int)(x << 28)) >> 28; }
+
+__device__ __forceinline__ int power4(uint32_t w)
+{
+    int acc = 0;
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+        const uint32_t byte = (w >> (8 * b)) & 0xFFu;
+        const int re = nib(byte >> 4), im = nib(byte);
+        acc += re * re + im * im;
+    }
+    return acc;
+}
+
+__global__ void incoh_kernel(const uint8_t *data, long long nrows, int ninput, float *incoh)
+{
+    const long long row = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 3;
+    const int sub = threadIdx.x & 7;
+    int acc = 0;
+    if (row < nrows) {
+        const uint8_t *r = data + row * ninput;
+        if ((ninput & 31) == 0) {
+            for (int off = sub * 4; off < ninput; off += 32)
+                acc += power4(*reinterpret_cast<const uint32_t *>(r + off));
+        } else {
+            for (int off = sub; off < ninput; off += 8) acc += power4(r[off]);
+        }
+    }
+    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 4);
+    if (row < nrows && sub == 0) incoh[row] = (float)acc;
+}
+
+int launch_incoh(const uint8_t *data, long long nrows, int ninput, float *incoh, cudaStream_t st)
+{
+    if (nrows <= 0) return VGB_SUCCESS;
+    const long long threads = nrows * 8;
+    incoh_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(data, nrows, ninput, incoh);
+    return check_launch("incoh_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// Beamformer for legacy-layout fine voltages v[s][c][i].
+// A block covers 16 channels x 16 samples; the voltage rows are staged in
+// shared memory with a 4-byte pad so the per-antenna byte gathers of 32
+// threads fall in 32 different banks.
+// ---------------------------------------------------------------------------
+struct LegacyArgs {
+    const void *v;           // [s][c][ni] uint8 (int4) or double2
+    int datatype;            // VGB_INT4 or VGB_DBL
+    int nsamples, nchan, nant;
+    const uint32_t *polQ, *polP;
+    const float4 *W;         // [p][nant][nchan][2]
+    int npointing;
+    float invw;
+    int nstokes;
+    float *S;                // [p][s][nstokes][nchan]
+    float4 *e;               // [p][s][nchan] nullable
+    float *incoh;            // [s][nchan] nullable (int4 only)
+};
+
+constexpr int kLS = 16, kLC = 16; // samples, channels per block
+
+template <bool kInt4>
+__global__ void __launch_bounds__(256) legacy_beam_kernel(const LegacyArgs a)
+{
+    extern __shared__ __align__(16) unsigned char lsm[];
+    const int ni = 2 * a.nant;
+    const int tid = threadIdx.x;
+    const int cl = tid & (kLC - 1), sl = tid >> 4;
+    const int c0 = blockIdx.x * kLC, s0 = blockIdx.y * kLS;
+    const int c = c0 + cl, s = s0 + sl;
+    const bool live = c < a.nchan && s < a.nsamples;
+
+    // Stage the 4+4-bit rows (s, c) of this block, row stride ni/4 + 1 words.
+    // Complex FP64 voltages are read straight from global memory.
+    if (kInt4) {
+        const int wpr = ni / 4 + 1;
+        uint32_t *rows = reinterpret_cast<uint32_t *>(lsm);
+        const int nw = ni / 4;
+        for (int idx = tid; idx < kLS * kLC * nw; idx += 256) {
+            const int r = idx / nw, wdx = idx % nw;
+            const int rs = s0 + r / kLC, rc = c0 + r % kLC;
+            uint32_t val = 0;
+            if (rs < a.nsamples && rc < a.nchan)
+                val = __ldg(reinterpret_cast<const uint32_t *>(static_cast<const uint8_t *>(a.v) +
+                                                                ((long long)rs * a.nchan + rc) * ni) +
+                            wdx);
+            rows[r * wpr + wdx] = val;
+        }
+    }
+    __syncthreads();
+    if (!live) return;
+    const int r = sl * kLC + cl;
+
+    for (int p = 0; p < a.npointing; p++) {
+        float acc[9];
+#pragma unroll
+        for (int q = 0; q < 9; q++) acc[q] = 0.f;
+        const float4 *Wp = a.W + ((long long)p * a.nant * a.nchan + c) * 2;
+        for (int ant = 0; ant < a.nant; ant++) {
+            const uint32_t iq = __ldg(a.polQ + ant), ip = __ldg(a.polP + ant);
+            float2 vq, vp;
+            if (kInt4) {
+                const uint8_t *row = lsm + 4 * (r * (ni / 4 + 1));
+                const uint32_t bq = row[iq], bp = row[ip];
+                vq = make_float2((float)nib(bq >> 4), (float)nib(bq));
+                vp = make_float2((float)nib(bp >> 4), (float)nib(bp));
+            } else {
+                const double2 *row = static_cast<const double2 *>(a.v) + ((long long)s * a.nchan + c) * ni;
+                const double2 dq = __ldg(row + iq), dp = __ldg(row + ip);
+                vq = make_float2((float)dq.x, (float)dq.y);
+                vp = make_float2((float)dp.x, (float)dp.y);
+            }
+            const float4 wa = __ldg(Wp + (long long)ant * a.nchan * 2);
+            const float4 wb = __ldg(Wp + (long long)ant * a.nchan * 2 + 1);
+            const float exr = wa.x * vq.x - wa.y * vq.y + wa.z * vp.x - wa.w * vp.y;
+            const float exi = wa.x * vq.y + wa.y * vq.x + wa.z * vp.y + wa.w * vp.x;
+            const float eyr = wb.x * vq.x - wb.y * vq.y + wb.z * vp.x - wb.w * vp.y;
+            const float eyi = wb.x * vq.y + wb.y * vq.x + wb.z * vp.y + wb.w * vp.x;
+            acc[0] += exr;
+            acc[1] += exi;
+            acc[2] += eyr;
+            acc[3] += eyi;
+            acc[4] = fmaf(exr, exr, fmaf(exi, exi, acc[4]));
+            acc[5] = fmaf(eyr, eyr, fmaf(eyi, eyi, acc[5]));
+            acc[6] = fmaf(exr, eyr, fmaf(exi, eyi, acc[6]));
+            acc[7] = fmaf(exi, eyr, fmaf(-exr, eyi, acc[7]));
+        }
+        const float bnXX = acc[0] * acc[0] + acc[1] * acc[1] - acc[4];
+        const float bnYY = acc[2] * acc[2] + acc[3] * acc[3] - acc[5];
+        const float bxr = acc[0] * acc[2] + acc[1] * acc[3] - acc[6];
+        const float bxi = acc[1] * acc[2] - acc[0] * acc[3] - acc[7];
+        float *S = a.S + (((long long)p * a.nsamples + s) * a.nstokes) * a.nchan + c;
+        S[0] = a.invw * (bnXX + bnYY);
+        if (a.nstokes == 4) {
+            S[a.nchan] = a.invw * (bnXX - bnYY);
+            S[2 * a.nchan] = 2.0f * a.invw * bxr;
+            S[3 * a.nchan] = -2.0f * a.invw * bxi;
+        }
+        if (a.e) a.e[((long long)p * a.nsamples + s) * a.nchan + c] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+    }
+    if (kInt4 && a.incoh) {
+        const uint32_t *row = reinterpret_cast<const uint32_t *>(lsm) + r * (ni / 4 + 1);
+        int accp = 0;
+        for (int wdx = 0; wdx < ni / 4; wdx++) accp += power4(row[wdx]);
+        a.incoh[(long long)s * a.nchan + c] = (float)accp;
+    }
+}
+
+int launch_legacy_beam(const LegacyArgs &a, cudaStream_t st)
+{
+    if (a.nsamples <= 0) return VGB_SUCCESS;
+    const int ni = 2 * a.nant;
+    const bool int4 = a.datatype == VGB_INT4;
+    if (int4 && (ni % 4) != 0) return set_error(VGB_ERR_INVALID, "legacy beamformer: 2*nant must be a multiple of 4");
+    const size_t smem = int4 ? (size_t)kLS * kLC * (ni / 4 + 1) * 4 : 16;
+    if (smem > 227 * 1024)
+        return set_error(VGB_ERR_INVALID, "legacy beamformer: %d inputs do not fit the shared-memory tile", ni);
+    dim3 grid((a.nchan + kLC - 1) / kLC, (a.nsamples + kLS - 1) / kLS);
+    if (int4) {
+        int rc = check_cuda(cudaFuncSetAttribute(legacy_beam_kernel<true>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                            "cudaFuncSetAttribute(legacy)");
+        if (rc) return rc;
+        legacy_beam_kernel<true><<<grid, 256, smem, st>>>(a);
+    } else {
+        int rc = check_cuda(cudaFuncSetAttribute(legacy_beam_kernel<false>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                            "cudaFuncSetAttribute(legacy)");
+        if (rc) return rc;
+        legacy_beam_kernel<false><<<grid, 256, smem, st>>>(a);
+    }
+    return check_launch("legacy_beam_kernel");
+}
+
+} // namespace vgb

@@ -1,0 +1,263 @@
+// Shared device/host definitions for the GB300 voltage hot path.
+//
+// Layout vocabulary follows VCSBeam (include/vcsbeam.h.in:234-268):
+//   MWAX voltages   [block][input][sample-in-block] char2, 64000 samples/block
+//   fine voltages   v_IDX  [sample][chan][input]
+//   Stokes          C_IDX  [pointing][sample][stokes][chan]
+//   beam voltages   B_IDX  [pointing][sample][chan][pol]
+// A "frame" is the 128 consecutive samples one fine spectrum consumes.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "../../include/vcsbeam_gb300.h"
+
+namespace vgb {
+
+constexpr int kVSPVB = 64000;               // samples per MWAX voltage block
+constexpr int kK = 128;                     // fine channels (FFT length)
+constexpr int kP = 12;                      // taps
+constexpr int kFramesPerBlock = kVSPVB / kK; // 500
+constexpr int kHistFrames = kP;             // frames of the previous second a second needs
+
+// Error flag bits a kernel may raise in the device status word.
+constexpr unsigned kErrWaitTimeout = 1u;    // a bounded mbarrier wait gave up
+constexpr unsigned kErrBadFrame = 2u;       // a frame index fell outside the described buffers
+
+// ---------------------------------------------------------------------------
+// Where the frames of one coarse channel's second live.
+//
+// Window frame w (w = 0 .. nspectra+P-2) is the w-th 128-sample frame of the
+// time axis that starts P frames before the second: w < P are the previous
+// second's last P frames ("history"), w >= P is frame (w-P) of the second.
+// This covers both the reference's single buffer with a one-block margin in
+// front (pfb.cpp:149-153) and a compact history array.
+// ---------------------------------------------------------------------------
+struct VoltView {
+    const char2 *hist;     // history frame 0 of input 0
+    long long hist_input;  // char2 stride between inputs in the history
+    const char2 *cur;      // block 0, input 0, sample 0 of the second
+    long long cur_block;   // char2 stride between voltage blocks
+    long long cc_hist;     // char2 stride between coarse channels (history)
+    long long cc_cur;      // char2 stride between coarse channels (second)
+    int ninputs;
+    int nblocks;           // voltage blocks in the second
+};
+
+// ---------------------------------------------------------------------------
+// Host-side status helpers (defined in vgb_api.cu).
+// ---------------------------------------------------------------------------
+int set_error(int code, const char *fmt, ...);
+int check_cuda(cudaError_t e, const char *what);
+int check_launch(const char *what);
+
+// ---------------------------------------------------------------------------
+// PTX helpers: shared-memory addresses, mbarriers, 1-D bulk (TMA) copies.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// Bounded wait on an mbarrier phase. Returns false if the phase did not
+// complete within `max_polls` polls (the caller records an error and skips
+// the work instead of spinning forever).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t phase, uint32_t max_polls)
+{
+    uint32_t addr = smem_u32(bar);
+    for (uint32_t i = 0; i < max_polls; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n"
+            " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// 1-D bulk copy global -> shared through the TMA unit. dst, src and bytes
+// must be multiples of 16 (callers copy whole 256-byte frames).
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// 128-point DFT building blocks (8 threads per transform).
+//
+// n = 8q + j (j = thread in group, q = 0..15); k = k1 + 16 k2.
+//   pass 1: thread j: Y_j[k1] = sum_q x[8q+j] W16^{q k1}, then * W128^{j k1}
+//   pass 2: thread t: for k1 in {2t, 2t+1}: X[k1+16k2] = sum_j Y_j[k1] W8^{j k2}
+// The sign of the exponent is a template parameter: -1 forward (cuFFT's
+// CUFFT_FORWARD convention), +1 inverse (unnormalised).
+// ---------------------------------------------------------------------------
+template <int SIGN> __device__ __forceinline__ float2 cmul_tw(float2 a, float c, float s)
+{
+    // a * (c + i*SIGN*s) where (c, s) = (cos, |sin|) of the positive angle
+    const float ss = SIGN * s;
+    return make_float2(a.x * c - a.y * ss, a.x * ss + a.y * c);
+}
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// multiply by SIGN*i  (e^{SIGN i pi/2})
+template <int SIGN> __device__ __forceinline__ float2 mul_i(float2 a)
+{
+    return SIGN > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+// In-register radix-2 DFT of length 4 with exponent sign SIGN.
+template <int SIGN> __device__ __forceinline__ void dft4(float2 &a0, float2 &a1, float2 &a2, float2 &a3)
+{
+    float2 t0 = cadd(a0, a2), t1 = csub(a0, a2);
+    float2 t2 = cadd(a1, a3), t3 = mul_i<SIGN>(csub(a1, a3));
+    a0 = cadd(t0, t2);
+    a2 = csub(t0, t2);
+    a1 = cadd(t1, t3);
+    a3 = csub(t1, t3);
+}
+
+// Length-8 DFT in registers, natural order in and out.
+template <int SIGN> __device__ __forceinline__ void dft8(float2 *x)
+{
+    const float r = 0.70710678118654752440f;
+    // stage 1: 4 butterflies of distance 4
+    float2 a[8];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        a[i] = cadd(x[i], x[i + 4]);
+        a[i + 4] = csub(x[i], x[i + 4]);
+    }
+    // twiddles W8^{SIGN*i} on the odd half: i = 1, 2, 3
+    a[5] = make_float2(r * (a[5].x - SIGN * a[5].y), r * (a[5].y + SIGN * a[5].x));
+    a[6] = mul_i<SIGN>(a[6]);
+    a[7] = make_float2(r * (-a[7].x - SIGN * a[7].y), r * (-a[7].y + SIGN * a[7].x));
+    // two length-4 DFTs: evens -> X[0,2,4,6], odds -> X[1,3,5,7]
+    dft4<SIGN>(a[0], a[1], a[2], a[3]);
+    dft4<SIGN>(a[4], a[5], a[6], a[7]);
+    x[0] = a[0];
+    x[2] = a[1];
+    x[4] = a[2];
+    x[6] = a[3];
+    x[1] = a[4];
+    x[3] = a[5];
+    x[5] = a[6];
+    x[7] = a[7];
+}
+
+// Length-16 DFT in registers (4 x 4 decomposition), natural order.
+template <int SIGN> __device__ __forceinline__ void dft16(float2 *x)
+{
+    // n = 4 n1 + n2, k = k1 + 4 k2
+    float2 y[16];
+#pragma unroll
+    for (int n2 = 0; n2 < 4; n2++) {
+        float2 a0 = x[n2], a1 = x[n2 + 4], a2 = x[n2 + 8], a3 = x[n2 + 12];
+        dft4<SIGN>(a0, a1, a2, a3); // over n1 -> k1
+        y[n2 * 4 + 0] = a0;
+        y[n2 * 4 + 1] = a1;
+        y[n2 * 4 + 2] = a2;
+        y[n2 * 4 + 3] = a3;
+    }
+    // twiddle W16^{n2 k1}
+    const float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f;
+    const float r = 0.70710678118654752440f;
+#pragma unroll
+    for (int n2 = 1; n2 < 4; n2++) {
+#pragma unroll
+        for (int k1 = 1; k1 < 4; k1++) {
+            const int e = n2 * k1; // 1..9
+            float c, s;
+            switch (e) {
+            case 1: c = c1; s = s1; break;
+            case 2: c = r; s = r; break;
+            case 3: c = s1; s = c1; break;
+            case 4: c = 0.f; s = 1.f; break;
+            case 6: c = -r; s = r; break;
+            case 9: c = -c1; s = -s1; break;
+            default: c = 1.f; s = 0.f; break;
+            }
+            y[n2 * 4 + k1] = cmul_tw<SIGN>(y[n2 * 4 + k1], c, s);
+        }
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) {
+        float2 a0 = y[k1], a1 = y[4 + k1], a2 = y[8 + k1], a3 = y[12 + k1];
+        dft4<SIGN>(a0, a1, a2, a3); // over n2 -> k2
+        x[k1] = a0;
+        x[k1 + 4] = a1;
+        x[k1 + 8] = a2;
+        x[k1 + 12] = a3;
+    }
+}
+
+// Shared-memory row geometry of one 128-point transform (float2 units).
+// Pass-1 output Y_j[k1] is stored at k1*9 + j (9 = 8 + 1 pad, conflict-free
+// for both passes). Rows are padded so that 4 transforms in one warp land on
+// alternating bank halves.
+constexpr int kFftRow = 152;
+
+// Pass 1: the 8 threads of one group read x[8q + j] (row `row`), transform
+// over q, twiddle by W128^{j k1} from `tw` (laid out [k1][j], cos/sin pairs of
+// the positive angle 2*pi*j*k1/128) and write back in place as Y_j[k1].
+template <int SIGN>
+__device__ __forceinline__ void fft128_pass1(float2 *row, const float2 *tw, int j)
+{
+    float2 x[16];
+#pragma unroll
+    for (int q = 0; q < 16; q++) x[q] = row[8 * q + j];
+    __syncwarp();
+    dft16<SIGN>(x);
+#pragma unroll
+    for (int k1 = 1; k1 < 16; k1++) {
+        float2 w = tw[k1 * 8 + j];
+        x[k1] = cmul_tw<SIGN>(x[k1], w.x, w.y);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < 16; k1++) row[k1 * 9 + j] = x[k1];
+}
+
+// Pass 2: thread t of the group produces X[k1 + 16 k2] for k1 = 2t, 2t+1 and
+// all k2, into `out[2][8]` (out[h][k2] for k1 = 2t + h).
+template <int SIGN>
+__device__ __forceinline__ void fft128_pass2(const float2 *row, int t, float2 (&out)[2][8])
+{
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int k1 = 2 * t + h;
+#pragma unroll
+        for (int j = 0; j < 8; j++) out[h][j] = row[k1 * 9 + j];
+        dft8<SIGN>(out[h]);
+    }
+}
+
+} // namespace vgb
