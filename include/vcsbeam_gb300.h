@@ -1,0 +1,249 @@
+/*
+ * vcsbeam_gb300.h -- plain C ABI of the GB300 voltage hot path.
+ *
+ * Every entry point takes device pointers, sizes and a CUDA stream (as
+ * void *, NULL = the legacy default stream), returns VGB_SUCCESS or an error
+ * code, and never exits the process. vgb_last_error() describes the last
+ * failure on the calling thread. Launches are asynchronous on the given
+ * stream; vgb_check_device_status() reports errors kernels raised (a bounded
+ * wait that expired, a frame outside the described buffers).
+ *
+ * The VCSBeam library API (include/vcsbeam.h in this project, mirroring the
+ * reference's include/vcsbeam.h.in) is implemented on top of these calls.
+ * Each entry point below names the reference routine(s) it replaces;
+ * file:line references are to the VCSBeam source tree.
+ *
+ * Layouts use the reference's index macros (include/vcsbeam.h.in:234-268):
+ *   MWAX voltages  [block][input][sample] char2, 64000 samples per block,
+ *                  input = 2*antenna + pol (pol 0 = X = "Q", 1 = Y = "P")
+ *   legacy/fine    v_IDX [sample][chan][input]
+ *   Stokes         C_IDX [pointing][sample][stokes][chan]
+ *   beam voltages  B_IDX [pointing][sample][chan][pol] complex float
+ * Batched calls add a leading coarse-channel dimension ("cc").
+ */
+#ifndef VCSBEAM_GB300_H
+#define VCSBEAM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define VGB_SUCCESS 0
+#define VGB_ERR_INVALID 1     /* an argument is out of range or misaligned */
+#define VGB_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define VGB_ERR_DEVICE 3      /* a kernel raised its device status word */
+#define VGB_ERR_UNSUPPORTED 4 /* a shape the kernels are not built for */
+#define VGB_ERR_ALLOC 5       /* device or pinned host allocation failed */
+#define VGB_ERR_STATE 6       /* call out of order (e.g. buffer locked) */
+
+/* ---- pfb_flags bits (include/vcsbeam.h.in:459-480) ---- */
+#define VGB_PFB_COMPLEX_INT4 0x10
+#define VGB_PFB_COMPLEX_FLOAT64 0x20
+#define VGB_PFB_IMAG_PART_FIRST 0x100
+#define VGB_PFB_EMULATE_FPGA 0x200
+
+/* Not a reference bit: accumulate the weighted overlap-add in FP32 instead of
+ * int32. Exact (identical results) only when every partial sum of the filter
+ * times int8 voltages stays below 2^24; vgb_filter_fp32_exact() checks that. */
+#define VGB_WOLA_FP32 0x10000
+
+/* ---- vcsbeam_datatype (include/vcsbeam.h.in:346-350) ---- */
+#define VGB_INT4 0
+#define VGB_DBL 1
+
+/* Fine-PFB geometry the kernels are built for: 128 channels, 12 taps,
+ * 64000-sample MWAX blocks (pfb.cpp:153 hard-codes the 500 frames/block). */
+#define VGB_NCHAN 128
+#define VGB_NTAPS 12
+#define VGB_SAMPLES_PER_BLOCK 64000
+
+const char *vgb_last_error(void);
+int vgb_version(void);
+/* 1 if FP32 accumulation of the weighted overlap-add is exact for this
+ * host-side filter (K*P taps) and int8 voltages, else 0. */
+int vgb_filter_fp32_exact(const int32_t *filter, int ntaps, int nchan);
+/* Copies and clears the device status word of the current device (after
+ * synchronising `stream`). Returns VGB_ERR_DEVICE if any bit was set. */
+int vgb_check_device_status(void *stream, unsigned *flags_out);
+
+/*
+ * Where one second of MWAX voltages lives, per coarse channel. Window frame
+ * w (128 samples) of the second is history frame w for w < 12 (the last 12
+ * frames of the previous second) and frame w-12 of the second otherwise.
+ * The reference's read buffer (one margin block, then the second,
+ * buffer.c:52-77, metadata.c:448-454) is hist = buffer + 488*256 bytes,
+ * hist_input_stride = 128000, cur = buffer + block_bytes,
+ * cur_block_stride = block_bytes. All pointers and strides in bytes and
+ * multiples of 16 (the frames are copied by the TMA unit).
+ */
+typedef struct vgb_voltages {
+    const void *hist;
+    long long hist_input_stride;
+    long long hist_cc_stride;
+    const void *cur;
+    long long cur_block_stride;
+    long long cur_cc_stride;
+    int ninputs;
+    int nblocks;
+} vgb_voltages;
+
+/*
+ * Fused forward fine PFB + tied-array beam + incoherent sum + Stokes
+ * detection for `ncc` coarse channels of MWAX voltages. Replaces, per second:
+ * vmUploadForwardPFBChunk..vmPackChunk (pfb.cpp:544-673) followed by
+ * vmApplyJChunk and vmBeamformChunk (form_beam.cpp:510-582), i.e.
+ * vmBeamformSecond (form_beam.cpp:587-627) for one pointing.
+ *   filter      K*P int32 analysis taps (pfb.cpp:459-460 cast)
+ *   pfb_flags   VGB_PFB_EMULATE_FPGA and/or VGB_PFB_COMPLEX_INT4 select the
+ *               rounding (pfb.cpp:602-616) and the 4-bit demotion the
+ *               reference's beamformer input carries (pfb.cpp:325-332)
+ *   W           [ncc][nant][128][2][2] complex float: phi * J^-1
+ *               (vgb_weights)
+ *   invw        1 / number of unflagged RF inputs (metadata.c:1554-1561)
+ *   S           [ncc][nspectra][nstokes][128] float (nstokes 1 or 4)
+ *   e           [ncc][nspectra][128][2] complex float, or NULL
+ *   incoh       [ncc][nspectra][128] float, or NULL
+ */
+int vgb_beamform_mwax(const vgb_voltages *v, int ncc, int nspectra, const int32_t *filter, int ntaps,
+                      int nchan, unsigned pfb_flags, const void *W, int nant, float invw, int nstokes,
+                      float *S, void *e, float *incoh, void *stream);
+
+/*
+ * Forward fine PFB only, packed to the legacy recombined layout (the output
+ * of vmExecuteForwardPFB, pfb.cpp:730-773): out [ncc][nspectra][128][ninputs]
+ * uint8 (4+4-bit, VGB_PFB_COMPLEX_INT4) or complex double, input i written at
+ * column i_idx[i] (the VCS order, pfb.cpp:410-419).
+ */
+int vgb_fpfb(const vgb_voltages *v, int ncc, int nspectra, const int32_t *filter, int ntaps, int nchan,
+             const int32_t *i_idx, unsigned pfb_flags, void *out, void *stream);
+
+/* The reference's four forward-PFB stages, one call each (pfb.cpp:569-673):
+ * vgb_wola: b[m][i][n] int32 pairs (vmWOLAChunk, without memset/atomics);
+ * vgb_round: in place int32 -> float, FPGA rounding or 2^-14 (vmFPGARoundingChunk);
+ * vgb_fft128: in-place forward 128-point FFTs of nrows float2 rows (vmFFTChunk);
+ * vgb_pack: rows [m][i][k] -> legacy layout (vmPackChunk). */
+int vgb_wola(const vgb_voltages *v, int nspectra, const int32_t *filter, int ntaps, int nchan, int32_t *b,
+             void *stream);
+int vgb_round(int32_t *b, long long nvalues, int emulate_fpga, void *stream);
+int vgb_fft128(void *rows, long long nrows, void *stream);
+int vgb_pack(const void *ffted, int nspectra, int ninputs, const int32_t *i_idx, unsigned pfb_flags,
+             void *out, void *stream);
+
+/*
+ * Table builders on the device in FP64 (replacing the host loops
+ * vmCalcPhi geometry.c:111-135 and vmCalcJ jones.c:97-157, and the pushes
+ * vmPushPhi geometry.c:192-198 / vmPushJ metadata.c:1000-1014):
+ *   vgb_phase:   phi[p][a][c] complex double from tile E/N/H/cable (m),
+ *                pointing unit vectors unit[p][3] = (E, N, H) and channel
+ *                frequencies (Hz); href = array reference height (m)
+ *   vgb_jones:   J[p][a][c][2][2] = inv(norm_F(D[a][c] B[p][a]))
+ *   vgb_weights: W[n][2][2] complex float = phi[n] * J[n] (n = p*nant*nchan + ...)
+ */
+int vgb_phase(const double *unit, const double *east, const double *north, const double *height,
+              const double *cable, const double *chan_freqs_hz, int npointing, int nant, int nchan,
+              double href, void *phi, void *stream);
+int vgb_jones(const void *D, const void *B, int npointing, int nant, int nchan, void *J, void *stream);
+int vgb_weights(const void *J, const void *phi, long long n, void *W, void *stream);
+
+/*
+ * Beamformer for fine voltages already in the legacy layout v_IDX
+ * [nsamples][nchan][2*nant], 4+4-bit (VGB_INT4) or complex double (VGB_DBL)
+ * (vmApplyJChunk + vmBeamformChunk, form_beam.cpp:510-582, for legacy
+ * recombined input, form_beam.cpp:593-596). polQ/polP: vcs_order of each
+ * antenna's X/Y input (jones.c:40-64). W [npointing][nant][nchan][2][2].
+ * S [npointing][nsamples][nstokes][nchan]; e (nullable) [npointing][nsamples][nchan][2]
+ * complex float; incoh (nullable, VGB_INT4 only) [nsamples][nchan].
+ */
+int vgb_beamform_legacy(const void *v, int datatype, int nsamples, int nchan, int nant, const uint32_t *polQ,
+                        const uint32_t *polP, const void *W, int npointing, float invw, int nstokes, float *S,
+                        void *e, float *incoh, void *stream);
+
+/* Incoherent beam of 4+4-bit voltages [nrows][ninput] -> [nrows] float
+ * (incoh_beam, form_beam.cpp:60-87, nrows = nsample*nchan). */
+int vgb_incoh_beam(const uint8_t *data, long long nrows, int ninput, float *incoh, void *stream);
+
+/*
+ * Per-channel 8-bit scale-and-offset (renormalise_channels_kernel,
+ * form_beam.cpp:408-449, launched by vmSendSToFits form_beam.cpp:653-663 and
+ * cu_form_incoh_beam form_beam.cpp:495-497) for ncc coarse channels.
+ * S [ncc][npointing][nstep][nstokes][nchan] float. The 8-bit output element
+ * (cc, p, s, st, c) goes to out[cc*out_cc + p*out_p + s*out_s + st*out_st + c]
+ * (the per-channel layout, or a spliced multi-channel PSRFITS row layout
+ * with no MPI gather, beam_psrfits.c:608-628). offsets/scales:
+ * [ncc][npointing][nstokes][nchan].
+ */
+int vgb_renormalise(const float *S, int ncc, int npointing, int nstep, int nstokes, int nchan, uint8_t *out,
+                    long long out_cc, long long out_p, long long out_s, long long out_st, float *offsets,
+                    float *scales, void *stream);
+
+/*
+ * Inverse PFB to 1.28 MHz complex samples and/or VDIF frames for njobs
+ * (coarse channel, pointing) pairs (ipfb_kernel + cu_invert_pfb,
+ * pfb.cpp:842-1003, and the quantisation of vdif_write_second,
+ * beam_vdif.c:29-92).
+ *   e       [job][nsamples][128][2] complex float (B_IDX, one pointing)
+ *   hist    [job][12][128][2] complex float: the previous second's last 12
+ *           samples, or NULL for the first second (zeros, pfb.cpp:972-976)
+ *   coeffs  12*128 float synthesis taps, already scaled (vmScaleFilterCoeffs)
+ *   out_f   [job][nsamples*128][2][2] float (data_buffer_vdif layout), or NULL
+ *   vdif    [job][nsamples][544] bytes: 32-byte header + 512 payload, or NULL
+ *   hdr     [job][8] uint32 header of the second's first frame (words other
+ *           than the frame number are copied), or NULL for zeros
+ */
+int vgb_ipfb(const void *e, long long e_job_stride, const void *hist, long long hist_job_stride,
+             const float *coeffs, int ntaps, int nchan, int nsamples, int njobs, float *out_f, uint8_t *vdif,
+             const uint32_t *hdr, int frame_offset, void *stream);
+
+/* ---- streaming pipeline: one second of all coarse channels per step ---- */
+typedef struct vgb_pipeline vgb_pipeline;
+
+typedef struct vgb_pipeline_config {
+    int ncc;                 /* coarse channels processed together */
+    int nant;                /* tiles; ninputs = 2*nant */
+    int nblocks;             /* MWAX voltage blocks per second (20) */
+    int nstokes;             /* 1 or 4 */
+    unsigned pfb_flags;      /* rounding / demotion of the beamformer input */
+    int do_ipfb;             /* inverse PFB + VDIF */
+    float invw;              /* 1 / unflagged RF inputs */
+} vgb_pipeline_config;
+
+int vgb_pipeline_create(const vgb_pipeline_config *cfg, vgb_pipeline **out);
+int vgb_pipeline_destroy(vgb_pipeline *p);
+/* Analysis taps (K*P int32) and, when do_ipfb, synthesis taps (K*P float). */
+int vgb_pipeline_set_filters(vgb_pipeline *p, const int32_t *analysis, const float *synthesis);
+/* W [ncc][nant][128][2][2] complex float on the host or device. */
+int vgb_pipeline_set_weights(vgb_pipeline *p, const void *W, int on_device);
+/* VDIF header template of frame 0, [ncc][8] uint32 on the host (optional). */
+int vgb_pipeline_set_vdif_header(vgb_pipeline *p, const uint32_t *hdr);
+/* Process one second whose voltages are already on the device, laid out
+ * [cc][block][input][sample] char2 (cc stride cur_cc_stride bytes). The
+ * previous second's last 12 frames are carried inside the pipeline. */
+int vgb_pipeline_run_device(vgb_pipeline *p, const void *d_voltages, long long cur_cc_stride);
+/* The same from host memory (pinned is fastest): copies the second to the
+ * device on a copy stream, double-buffered so the next second's copy can
+ * overlap this second's compute. */
+int vgb_pipeline_run_host(vgb_pipeline *p, const void *h_voltages, long long cur_cc_stride);
+/* Copy the last completed second's products to host buffers (each nullable):
+ * psrfits [nspectra][nstokes][ncc*128] bytes (channel-spliced rows),
+ * offsets/scales [ncc][nstokes][128], vdif [ncc][nspectra][544]. */
+int vgb_pipeline_fetch(vgb_pipeline *p, uint8_t *psrfits, float *offsets, float *scales, uint8_t *vdif);
+/* Copy the last second's unquantised products to host buffers (each
+ * nullable), as vmPullS / vmPullE do (form_beam.cpp:632-644):
+ * S [ncc][nspectra][nstokes][128] float, e [ncc][nspectra][128][2] complex
+ * float, incoh [ncc][nspectra][128] float. */
+int vgb_pipeline_fetch_raw(vgb_pipeline *p, float *S, void *e, float *incoh);
+/* Device pointers to the last second's products, for chaining further
+ * device work (valid until the next vgb_pipeline_run_*). */
+int vgb_pipeline_device_products(vgb_pipeline *p, const float **S, const void **e, const float **incoh,
+                                 const uint8_t **psrfits, const uint8_t **vdif);
+/* Kernel launches the last vgb_pipeline_run_* issued. */
+int vgb_pipeline_launch_count(vgb_pipeline *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

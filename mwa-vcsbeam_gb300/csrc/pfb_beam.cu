@@ -19,7 +19,7 @@
 //      (form_beam.cpp:298-315) and the incoherent sum; or the PFB-only back
 //      end, which writes the packed legacy-order output (pfb.cpp:316-340).
 // The fine-channel voltages never reach HBM on the beamformer path.
-#include "vgb_internal.cuh"
+#include "vgb_launch.cuh"
 
 namespace vgb {
 
@@ -268,23 +268,6 @@ __device__ __forceinline__ void drain(FrontSmem &sm, int it, int nsteps)
 // ---------------------------------------------------------------------------
 // Beamformer kernel.
 // ---------------------------------------------------------------------------
-struct BeamArgs {
-    VoltView vv;
-    const int *filter;      // K*P taps, reference order
-    const float4 *W;        // [cc][nant][K][2]: (w00, w01), (w10, w11)
-    long long W_cc;         // float4 stride between coarse channels
-    int nspectra;
-    int nant;
-    float invw;
-    int nstokes;            // 1 or 4
-    float *S;               // [cc][s][nstokes][K]
-    long long S_cc;
-    float4 *e;              // [cc][s][K] (ex, ey), nullable
-    long long e_cc;
-    float *incoh;           // [cc][s][K], nullable
-    long long inc_cc;
-    unsigned *status;
-};
 
 template <bool kInt32, bool kFpga, bool kDemote>
 __global__ void __launch_bounds__(kThreads, 1) beam_kernel(const BeamArgs a)
@@ -376,16 +359,6 @@ __global__ void __launch_bounds__(kThreads, 1) beam_kernel(const BeamArgs a)
 // ---------------------------------------------------------------------------
 // PFB-only kernel: packed legacy-order output (pfb.cpp:297-343).
 // ---------------------------------------------------------------------------
-struct PackArgs {
-    VoltView vv;
-    const int *filter;
-    const int *i_idx;       // MWAX input -> legacy input (pfb.cpp:410-419)
-    int nspectra;
-    unsigned flags;         // PFB_COMPLEX_INT4 / PFB_IMAG_PART_FIRST
-    void *out;              // [cc][s][K][I] uint8 or double2
-    long long out_cc;       // elements between coarse channels
-    unsigned *status;
-};
 
 template <bool kInt32, bool kFpga, bool kDemote>
 __global__ void __launch_bounds__(kThreads, 1) pack_kernel(const PackArgs a)
@@ -505,6 +478,36 @@ int launch_pack(const PackArgs &a, int ncc, bool int32_wola, bool fpga, bool dem
     if (a.nspectra <= 0 || ncc <= 0) return VGB_SUCCESS;
     dim3 grid((a.nspectra + kT - 1) / kT, ncc);
     return dispatch<PackSel>(a, grid, int32_wola, fpga, demote, st);
+}
+
+} // namespace vgb
+
+namespace vgb {
+
+// Gather the last P frames of a second into the compact history layout
+// [cc][input][P][K] char2 that the next second reads (the reference keeps a
+// whole voltage block for this, buffer.c:106-124; only 12 frames are used).
+__global__ void hist_gather_kernel(const char2 *cur, long long cur_block, long long cc_cur, int ninputs,
+                                   int nblocks, char2 *hist, long long cc_hist)
+{
+    const int cc = blockIdx.z, i = blockIdx.y;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x; // 16-byte word within the 3072 bytes
+    if (idx >= kHistFrames * kK / 8) return;
+    const long long last_frame = (long long)nblocks * kFramesPerBlock - kHistFrames;
+    const int b = (int)(last_frame / kFramesPerBlock), f = (int)(last_frame % kFramesPerBlock);
+    const uint4 *src = reinterpret_cast<const uint4 *>(cur + cc * cc_cur + b * cur_block + (long long)i * kVSPVB +
+                                                       (long long)f * kK);
+    uint4 *dst = reinterpret_cast<uint4 *>(hist + cc * cc_hist + (long long)i * kHistFrames * kK);
+    dst[idx] = src[idx];
+}
+
+int launch_hist_gather(const char2 *cur, long long cur_block, long long cc_cur, int ninputs, int nblocks, int ncc,
+                       char2 *hist, long long cc_hist, cudaStream_t st)
+{
+    dim3 grid(1, ninputs, ncc);
+    hist_gather_kernel<<<grid, kHistFrames * kK / 8, 0, st>>>(cur, cur_block, cc_cur, ninputs, nblocks, hist,
+                                                              cc_hist);
+    return check_launch("hist_gather_kernel");
 }
 
 } // namespace vgb

@@ -10,7 +10,7 @@
 //  * beamformer for fine-channel voltages already in legacy layout
 //    (v_IDX [s][c][i], 4+4-bit or complex FP64): vmApplyJ_kernel followed by
 //    vmBeamform_kernel (form_beam.cpp:122-371) in one pass.
-#include "vgb_internal.cuh"
+#include "vgb_launch.cuh"
 
 namespace vgb {
 
@@ -126,15 +126,6 @@ int launch_weights(const double2 *J, const double2 *phi, long long n, float4 *W,
 // ---------------------------------------------------------------------------
 // renormalise_channels (form_beam.cpp:408-449)
 // ---------------------------------------------------------------------------
-struct RenormArgs {
-    const float *S;        // [cc][p][nstep][nstokes][nchan]
-    long long S_cc;
-    int npointing, nstep, nstokes, nchan;
-    uint8_t *out;          // out + cc*out_cc + p*out_p + s*out_s + st*out_st + c
-    long long out_cc, out_p, out_s, out_st;
-    float *offsets, *scales; // + cc*stat_cc + (p*nstokes + st)*nchan + c
-    long long stat_cc;
-};
 
 // The float -> uint8 conversion of form_beam.cpp:443, (uint8_t)(val + 0.5)
 // with val + 0.5 in FP64, as the reference's GPU build performs it: truncate
@@ -253,19 +244,6 @@ int launch_incoh(const uint8_t *data, long long nrows, int ninput, float *incoh,
 // shared memory with a 4-byte pad so the per-antenna byte gathers of 32
 // threads fall in 32 different banks.
 // ---------------------------------------------------------------------------
-struct LegacyArgs {
-    const void *v;           // [s][c][ni] uint8 (int4) or double2
-    int datatype;            // VGB_INT4 or VGB_DBL
-    int nsamples, nchan, nant;
-    const uint32_t *polQ, *polP;
-    const float4 *W;         // [p][nant][nchan][2]
-    int npointing;
-    float invw;
-    int nstokes;
-    float *S;                // [p][s][nstokes][nchan]
-    float4 *e;               // [p][s][nchan] nullable
-    float *incoh;            // [s][nchan] nullable (int4 only)
-};
 
 constexpr int kLS = 16, kLC = 16; // samples, channels per block
 

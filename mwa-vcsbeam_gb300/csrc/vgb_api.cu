@@ -1,0 +1,626 @@
+// The plain C ABI (include/vcsbeam_gb300.h): argument checks, status
+// reporting and the one-second streaming pipeline.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "vgb_launch.cuh"
+
+namespace vgb {
+
+static thread_local char t_err[512] = "";
+
+int set_error(int code, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(t_err, sizeof(t_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int check_cuda(cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return VGB_SUCCESS;
+    return set_error(VGB_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int check_launch(const char *what) { return check_cuda(cudaGetLastError(), what); }
+
+// One status word per device, raised by kernels with atomicOr.
+__device__ unsigned g_status;
+
+static unsigned *status_ptr()
+{
+    static unsigned *ptrs[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    if (!ptrs[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_status) != cudaSuccess) return nullptr;
+        ptrs[dev] = static_cast<unsigned *>(p);
+    }
+    return ptrs[dev];
+}
+
+static bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+static int to_view(const vgb_voltages *v, int ncc, int nspectra, VoltView &vv)
+{
+    if (!v) return set_error(VGB_ERR_INVALID, "voltages descriptor is NULL");
+    if (v->ninputs <= 0 || v->nblocks <= 0)
+        return set_error(VGB_ERR_INVALID, "ninputs (%d) and nblocks (%d) must be positive", v->ninputs, v->nblocks);
+    if (!v->cur || !v->hist) return set_error(VGB_ERR_INVALID, "voltage pointers must not be NULL");
+    if (!aligned16(v->cur) || !aligned16(v->hist))
+        return set_error(VGB_ERR_INVALID, "voltage pointers must be 16-byte aligned");
+    if ((v->hist_input_stride | v->cur_block_stride) & 15 || (ncc > 1 && ((v->hist_cc_stride | v->cur_cc_stride) & 15)))
+        return set_error(VGB_ERR_INVALID, "voltage strides must be multiples of 16 bytes");
+    if (v->cur_block_stride < (long long)v->ninputs * kVSPVB * 2)
+        return set_error(VGB_ERR_INVALID, "cur_block_stride smaller than one voltage block");
+    if (v->hist_input_stride < kHistFrames * kK * 2)
+        return set_error(VGB_ERR_INVALID, "hist_input_stride smaller than 12 frames");
+    if (nspectra < 0 || nspectra > v->nblocks * kFramesPerBlock)
+        return set_error(VGB_ERR_INVALID, "nspectra %d exceeds the %d frames in %d blocks", nspectra,
+                         v->nblocks * kFramesPerBlock, v->nblocks);
+    vv.hist = static_cast<const char2 *>(v->hist);
+    vv.hist_input = v->hist_input_stride / 2;
+    vv.cc_hist = v->hist_cc_stride / 2;
+    vv.cur = static_cast<const char2 *>(v->cur);
+    vv.cur_block = v->cur_block_stride / 2;
+    vv.cc_cur = v->cur_cc_stride / 2;
+    vv.ninputs = v->ninputs;
+    vv.nblocks = v->nblocks;
+    return VGB_SUCCESS;
+}
+
+static int check_geometry(int ntaps, int nchan)
+{
+    if (ntaps != kP || nchan != kK)
+        return set_error(VGB_ERR_UNSUPPORTED, "kernels are built for %d taps x %d channels (got %d x %d)", kP, kK,
+                         ntaps, nchan);
+    return VGB_SUCCESS;
+}
+
+static cudaStream_t S(void *s) { return static_cast<cudaStream_t>(s); }
+
+} // namespace vgb
+
+using namespace vgb;
+
+extern "C" {
+
+const char *vgb_last_error(void) { return t_err; }
+
+int vgb_version(void) { return 1; }
+
+int vgb_filter_fp32_exact(const int32_t *filter, int ntaps, int nchan)
+{
+    if (!filter || ntaps <= 0 || nchan <= 0) return 0;
+    long long worst = 0;
+    for (int n = 0; n < nchan; n++) {
+        long long s = 0;
+        for (int p = 0; p < ntaps; p++) {
+            long long h = filter[p * nchan + n];
+            s += h < 0 ? -h : h;
+        }
+        if (s > worst) worst = s;
+    }
+    return worst * 127 < (1LL << 24) ? 1 : 0;
+}
+
+int vgb_check_device_status(void *stream, unsigned *flags_out)
+{
+    unsigned *p = status_ptr();
+    if (!p) return set_error(VGB_ERR_CUDA, "device status word unavailable");
+    int rc = check_cuda(cudaStreamSynchronize(S(stream)), "cudaStreamSynchronize");
+    if (rc) return rc;
+    unsigned h = 0;
+    rc = check_cuda(cudaMemcpy(&h, p, sizeof(h), cudaMemcpyDeviceToHost), "read device status");
+    if (rc) return rc;
+    if (h) {
+        unsigned z = 0;
+        rc = check_cuda(cudaMemcpy(p, &z, sizeof(z), cudaMemcpyHostToDevice), "clear device status");
+        if (rc) return rc;
+    }
+    if (flags_out) *flags_out = h;
+    if (h)
+        return set_error(VGB_ERR_DEVICE, "kernel status 0x%x%s%s", h,
+                         (h & kErrWaitTimeout) ? " (bounded wait expired)" : "",
+                         (h & kErrBadFrame) ? " (frame outside the voltage buffers)" : "");
+    return VGB_SUCCESS;
+}
+
+int vgb_beamform_mwax(const vgb_voltages *v, int ncc, int nspectra, const int32_t *filter, int ntaps, int nchan,
+                      unsigned pfb_flags, const void *W, int nant, float invw, int nstokes, float *S_, void *e,
+                      float *incoh, void *stream)
+{
+    int rc = check_geometry(ntaps, nchan);
+    if (rc) return rc;
+    BeamArgs a{};
+    if ((rc = to_view(v, ncc, nspectra, a.vv))) return rc;
+    if (ncc <= 0) return set_error(VGB_ERR_INVALID, "ncc must be positive");
+    if (nant <= 0 || v->ninputs != 2 * nant)
+        return set_error(VGB_ERR_INVALID, "ninputs (%d) must equal 2*nant (nant=%d)", v->ninputs, nant);
+    if (nstokes != 1 && nstokes != 4) return set_error(VGB_ERR_INVALID, "nstokes must be 1 or 4");
+    if (!filter || !W || !S_) return set_error(VGB_ERR_INVALID, "filter, W and S must not be NULL");
+    if (!aligned16(W) || (e && !aligned16(e))) return set_error(VGB_ERR_INVALID, "W and e must be 16-byte aligned");
+    a.filter = filter;
+    a.W = static_cast<const float4 *>(W);
+    a.W_cc = (long long)nant * kK * 2;
+    a.nspectra = nspectra;
+    a.nant = nant;
+    a.invw = invw;
+    a.nstokes = nstokes;
+    a.S = S_;
+    a.S_cc = (long long)nspectra * nstokes * kK;
+    a.e = static_cast<float4 *>(e);
+    a.e_cc = (long long)nspectra * kK;
+    a.incoh = incoh;
+    a.inc_cc = (long long)nspectra * kK;
+    a.status = status_ptr();
+    if (!a.status) return set_error(VGB_ERR_CUDA, "device status word unavailable");
+    return launch_beam(a, ncc, !(pfb_flags & VGB_WOLA_FP32), (pfb_flags & VGB_PFB_EMULATE_FPGA) != 0,
+                       (pfb_flags & VGB_PFB_COMPLEX_INT4) != 0, S(stream));
+}
+
+int vgb_fpfb(const vgb_voltages *v, int ncc, int nspectra, const int32_t *filter, int ntaps, int nchan,
+             const int32_t *i_idx, unsigned pfb_flags, void *out, void *stream)
+{
+    int rc = check_geometry(ntaps, nchan);
+    if (rc) return rc;
+    PackArgs a{};
+    if ((rc = to_view(v, ncc, nspectra, a.vv))) return rc;
+    if (ncc <= 0) return set_error(VGB_ERR_INVALID, "ncc must be positive");
+    if (!filter || !i_idx || !out) return set_error(VGB_ERR_INVALID, "filter, i_idx and out must not be NULL");
+    a.filter = filter;
+    a.i_idx = i_idx;
+    a.nspectra = nspectra;
+    a.flags = pfb_flags;
+    a.out = out;
+    a.out_cc = (long long)nspectra * kK * v->ninputs;
+    a.status = status_ptr();
+    if (!a.status) return set_error(VGB_ERR_CUDA, "device status word unavailable");
+    return launch_pack(a, ncc, !(pfb_flags & VGB_WOLA_FP32), (pfb_flags & VGB_PFB_EMULATE_FPGA) != 0,
+                       (pfb_flags & VGB_PFB_COMPLEX_INT4) != 0, S(stream));
+}
+
+int vgb_wola(const vgb_voltages *v, int nspectra, const int32_t *filter, int ntaps, int nchan, int32_t *b,
+             void *stream)
+{
+    int rc = check_geometry(ntaps, nchan);
+    if (rc) return rc;
+    VoltView vv{};
+    if ((rc = to_view(v, 1, nspectra, vv))) return rc;
+    if (!filter || !b) return set_error(VGB_ERR_INVALID, "filter and b must not be NULL");
+    return launch_wola_staged(vv, filter, nspectra, reinterpret_cast<int2 *>(b), S(stream));
+}
+
+int vgb_round(int32_t *b, long long nvalues, int emulate_fpga, void *stream)
+{
+    if (!b || nvalues < 0) return set_error(VGB_ERR_INVALID, "bad buffer");
+    return launch_round_staged(b, nvalues, emulate_fpga, S(stream));
+}
+
+int vgb_fft128(void *rows, long long nrows, void *stream)
+{
+    if (!rows || nrows < 0) return set_error(VGB_ERR_INVALID, "bad buffer");
+    return launch_fft_staged(static_cast<float2 *>(rows), nrows, S(stream));
+}
+
+int vgb_pack(const void *ffted, int nspectra, int ninputs, const int32_t *i_idx, unsigned pfb_flags, void *out,
+             void *stream)
+{
+    if (!ffted || !i_idx || !out || ninputs <= 0) return set_error(VGB_ERR_INVALID, "bad arguments");
+    return launch_pack_staged(static_cast<const float2 *>(ffted), nspectra, ninputs, i_idx, pfb_flags, out,
+                              S(stream));
+}
+
+int vgb_phase(const double *unit, const double *east, const double *north, const double *height,
+              const double *cable, const double *chan_freqs_hz, int npointing, int nant, int nchan, double href,
+              void *phi, void *stream)
+{
+    if (!unit || !east || !north || !height || !cable || !chan_freqs_hz || !phi)
+        return set_error(VGB_ERR_INVALID, "NULL table pointer");
+    return launch_phase(unit, east, north, height, cable, chan_freqs_hz, npointing, nant, nchan, href,
+                        static_cast<double2 *>(phi), S(stream));
+}
+
+int vgb_jones(const void *D, const void *B, int npointing, int nant, int nchan, void *J, void *stream)
+{
+    if (!D || !B || !J) return set_error(VGB_ERR_INVALID, "NULL table pointer");
+    return launch_jones(static_cast<const double2 *>(D), static_cast<const double2 *>(B), npointing, nant, nchan,
+                        static_cast<double2 *>(J), S(stream));
+}
+
+int vgb_weights(const void *J, const void *phi, long long n, void *W, void *stream)
+{
+    if (!J || !phi || !W) return set_error(VGB_ERR_INVALID, "NULL table pointer");
+    return launch_weights(static_cast<const double2 *>(J), static_cast<const double2 *>(phi), n,
+                          static_cast<float4 *>(W), S(stream));
+}
+
+int vgb_beamform_legacy(const void *v, int datatype, int nsamples, int nchan, int nant, const uint32_t *polQ,
+                        const uint32_t *polP, const void *W, int npointing, float invw, int nstokes, float *S_,
+                        void *e, float *incoh, void *stream)
+{
+    if (!v || !polQ || !polP || !W || !S_) return set_error(VGB_ERR_INVALID, "NULL pointer");
+    if (datatype != VGB_INT4 && datatype != VGB_DBL) return set_error(VGB_ERR_INVALID, "bad datatype");
+    if (nstokes != 1 && nstokes != 4) return set_error(VGB_ERR_INVALID, "nstokes must be 1 or 4");
+    if (nant <= 0 || nchan <= 0 || npointing <= 0 || nsamples < 0) return set_error(VGB_ERR_INVALID, "bad sizes");
+    if (datatype == VGB_INT4 && !aligned16(v)) return set_error(VGB_ERR_INVALID, "v must be 16-byte aligned");
+    LegacyArgs a{};
+    a.v = v;
+    a.datatype = datatype;
+    a.nsamples = nsamples;
+    a.nchan = nchan;
+    a.nant = nant;
+    a.polQ = polQ;
+    a.polP = polP;
+    a.W = static_cast<const float4 *>(W);
+    a.npointing = npointing;
+    a.invw = invw;
+    a.nstokes = nstokes;
+    a.S = S_;
+    a.e = static_cast<float4 *>(e);
+    a.incoh = datatype == VGB_INT4 ? incoh : nullptr;
+    return launch_legacy_beam(a, S(stream));
+}
+
+int vgb_incoh_beam(const uint8_t *data, long long nrows, int ninput, float *incoh, void *stream)
+{
+    if (!data || !incoh || ninput <= 0 || nrows < 0) return set_error(VGB_ERR_INVALID, "bad arguments");
+    if ((ninput & 31) == 0 && !aligned16(data)) return set_error(VGB_ERR_INVALID, "data must be 16-byte aligned");
+    return launch_incoh(data, nrows, ninput, incoh, S(stream));
+}
+
+int vgb_renormalise(const float *S_, int ncc, int npointing, int nstep, int nstokes, int nchan, uint8_t *out,
+                    long long out_cc, long long out_p, long long out_s, long long out_st, float *offsets,
+                    float *scales, void *stream)
+{
+    if (!S_ || !out || !offsets || !scales) return set_error(VGB_ERR_INVALID, "NULL pointer");
+    if (ncc <= 0 || npointing <= 0 || nstokes <= 0 || nchan <= 0 || nstep < 0)
+        return set_error(VGB_ERR_INVALID, "bad sizes");
+    RenormArgs a{};
+    a.S = S_;
+    a.S_cc = (long long)npointing * nstep * nstokes * nchan;
+    a.npointing = npointing;
+    a.nstep = nstep;
+    a.nstokes = nstokes;
+    a.nchan = nchan;
+    a.out = out;
+    a.out_cc = out_cc;
+    a.out_p = out_p;
+    a.out_s = out_s;
+    a.out_st = out_st;
+    a.offsets = offsets;
+    a.scales = scales;
+    a.stat_cc = (long long)npointing * nstokes * nchan;
+    return launch_renorm(a, ncc, S(stream));
+}
+
+int vgb_ipfb(const void *e, long long e_job_stride, const void *hist, long long hist_job_stride, const float *coeffs,
+             int ntaps, int nchan, int nsamples, int njobs, float *out_f, uint8_t *vdif, const uint32_t *hdr,
+             int frame_offset, void *stream)
+{
+    int rc = check_geometry(ntaps, nchan);
+    if (rc) return rc;
+    if (!e || !coeffs || (!out_f && !vdif)) return set_error(VGB_ERR_INVALID, "NULL pointer");
+    if (!aligned16(e) || (hist && !aligned16(hist)) || (e_job_stride & 15) || (hist_job_stride & 15))
+        return set_error(VGB_ERR_INVALID, "e/hist must be 16-byte aligned with 16-byte job strides");
+    IpfbArgs a{};
+    a.e = static_cast<const float4 *>(e);
+    a.e_job = e_job_stride / 16;
+    a.hist = static_cast<const float4 *>(hist);
+    a.hist_job = hist_job_stride / 16;
+    a.coeffs = coeffs;
+    a.nsamples = nsamples;
+    a.out_f = out_f;
+    a.outf_job = (long long)nsamples * kK * 4;
+    a.vdif = vdif;
+    a.vdif_job = (long long)nsamples * 544;
+    a.hdr = hdr;
+    a.frame_offset = frame_offset;
+    return launch_ipfb(a, njobs, S(stream));
+}
+
+} // extern "C"
+
+// ===========================================================================
+// Streaming pipeline
+// ===========================================================================
+struct vgb_pipeline {
+    vgb_pipeline_config cfg{};
+    int ninputs = 0, nspectra = 0;
+    long long second_bytes = 0;      // one coarse channel's second, bytes
+    bool fp32_wola = false;
+    cudaStream_t s_comp = nullptr, s_copy = nullptr;
+    cudaEvent_t ev_copied[2] = {}, ev_consumed[2] = {};
+    int32_t *d_filter = nullptr;
+    float *d_coeffs = nullptr;
+    float4 *d_W = nullptr;
+    char2 *d_volt[2] = {};           // host-mode staging, [cc][block][input][sample]
+    char2 *d_hist[2] = {};           // [cc][input][12][128]
+    float *d_S = nullptr;
+    float4 *d_e = nullptr;
+    float *d_incoh = nullptr;
+    float4 *d_ehist[2] = {};         // [cc][12][128]
+    uint8_t *d_psrfits = nullptr;    // [ns][nstokes][ncc*128]
+    float *d_off = nullptr, *d_scl = nullptr;
+    uint8_t *d_vdif = nullptr;       // [cc][ns][544]
+    uint32_t *d_hdr = nullptr;
+    long long second = 0;            // seconds completed
+    int launches = 0;
+    int host_buf = 0;
+};
+
+namespace {
+
+template <class T> int dalloc(T **p, size_t bytes)
+{
+    if (cudaMalloc(reinterpret_cast<void **>(p), bytes) != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return set_error(VGB_ERR_ALLOC, "cudaMalloc of %zu bytes failed", bytes);
+    }
+    return VGB_SUCCESS;
+}
+
+// One second of compute on s_comp with the voltages at `volt`.
+int pipeline_second(vgb_pipeline *p, const char2 *volt, long long cc_stride_bytes)
+{
+    const vgb_pipeline_config &c = p->cfg;
+    const int cur = (int)(p->second & 1), nxt = cur ^ 1;
+    int rc;
+    p->launches = 0;
+    vgb_voltages v{};
+    v.hist = p->d_hist[cur];
+    v.hist_input_stride = (long long)kHistFrames * kK * 2;
+    v.hist_cc_stride = (long long)p->ninputs * kHistFrames * kK * 2;
+    v.cur = volt;
+    v.cur_block_stride = (long long)p->ninputs * kVSPVB * 2;
+    v.cur_cc_stride = cc_stride_bytes;
+    v.ninputs = p->ninputs;
+    v.nblocks = c.nblocks;
+    const unsigned flags = c.pfb_flags | (p->fp32_wola ? VGB_WOLA_FP32 : 0u);
+    rc = vgb_beamform_mwax(&v, c.ncc, p->nspectra, p->d_filter, kP, kK, flags, p->d_W, c.nant, c.invw, c.nstokes,
+                           p->d_S, p->d_e, p->d_incoh, p->s_comp);
+    if (rc) return rc;
+    p->launches++;
+    // spliced PSRFITS rows: [s][st][cc*128 + c]
+    const long long row = (long long)c.nstokes * c.ncc * kK;
+    rc = vgb_renormalise(p->d_S, c.ncc, 1, p->nspectra, c.nstokes, kK, p->d_psrfits, kK, 0, row,
+                         (long long)c.ncc * kK, p->d_off, p->d_scl, p->s_comp);
+    if (rc) return rc;
+    p->launches++;
+    if (c.do_ipfb) {
+        const long long ejob = (long long)p->nspectra * kK * 16;
+        rc = vgb_ipfb(p->d_e, ejob, p->second > 0 ? p->d_ehist[cur] : nullptr, (long long)kHistFrames * kK * 16,
+                      p->d_coeffs, kP, kK, p->nspectra, c.ncc, nullptr, p->d_vdif, p->d_hdr, 0, p->s_comp);
+        if (rc) return rc;
+        p->launches++;
+        // carry the last 12 beam samples of each coarse channel
+        rc = check_cuda(cudaMemcpy2DAsync(p->d_ehist[nxt], (size_t)kHistFrames * kK * 16,
+                                          p->d_e + (long long)(p->nspectra - kHistFrames) * kK, (size_t)ejob,
+                                          (size_t)kHistFrames * kK * 16, c.ncc, cudaMemcpyDeviceToDevice,
+                                          p->s_comp),
+                        "carry beam history");
+        if (rc) return rc;
+    }
+    // carry the last 12 voltage frames of each input
+    rc = launch_hist_gather(volt, (long long)p->ninputs * kVSPVB, cc_stride_bytes / 2, p->ninputs, c.nblocks, c.ncc,
+                            p->d_hist[nxt], (long long)p->ninputs * kHistFrames * kK, p->s_comp);
+    if (rc) return rc;
+    p->launches++;
+    p->second++;
+    return VGB_SUCCESS;
+}
+
+} // namespace
+
+extern "C" {
+
+int vgb_pipeline_create(const vgb_pipeline_config *cfg, vgb_pipeline **out)
+{
+    if (!cfg || !out) return set_error(VGB_ERR_INVALID, "NULL argument");
+    if (cfg->ncc <= 0 || cfg->nant <= 0 || cfg->nblocks <= 0 || (cfg->nstokes != 1 && cfg->nstokes != 4))
+        return set_error(VGB_ERR_INVALID, "bad pipeline configuration");
+    vgb_pipeline *p = new vgb_pipeline();
+    p->cfg = *cfg;
+    p->ninputs = 2 * cfg->nant;
+    p->nspectra = cfg->nblocks * kFramesPerBlock;
+    p->second_bytes = (long long)cfg->nblocks * p->ninputs * kVSPVB * 2;
+    const long long ncc = cfg->ncc, ns = p->nspectra;
+    int rc = VGB_SUCCESS;
+    rc = rc ? rc : check_cuda(cudaStreamCreateWithFlags(&p->s_comp, cudaStreamNonBlocking), "stream");
+    rc = rc ? rc : check_cuda(cudaStreamCreateWithFlags(&p->s_copy, cudaStreamNonBlocking), "stream");
+    for (int b = 0; b < 2 && !rc; b++) {
+        rc = check_cuda(cudaEventCreateWithFlags(&p->ev_copied[b], cudaEventDisableTiming), "event");
+        rc = rc ? rc : check_cuda(cudaEventCreateWithFlags(&p->ev_consumed[b], cudaEventDisableTiming), "event");
+    }
+    rc = rc ? rc : dalloc(&p->d_filter, sizeof(int32_t) * kK * kP);
+    rc = rc ? rc : dalloc(&p->d_coeffs, sizeof(float) * kK * kP);
+    rc = rc ? rc : dalloc(&p->d_W, sizeof(float4) * 2 * ncc * cfg->nant * kK);
+    for (int b = 0; b < 2 && !rc; b++) {
+        rc = dalloc(&p->d_hist[b], (size_t)ncc * p->ninputs * kHistFrames * kK * 2);
+        rc = rc ? rc : dalloc(&p->d_ehist[b], sizeof(float4) * ncc * kHistFrames * kK);
+    }
+    rc = rc ? rc : dalloc(&p->d_S, sizeof(float) * ncc * ns * cfg->nstokes * kK);
+    rc = rc ? rc : dalloc(&p->d_e, sizeof(float4) * ncc * ns * kK);
+    rc = rc ? rc : dalloc(&p->d_incoh, sizeof(float) * ncc * ns * kK);
+    rc = rc ? rc : dalloc(&p->d_psrfits, (size_t)ns * cfg->nstokes * ncc * kK);
+    rc = rc ? rc : dalloc(&p->d_off, sizeof(float) * ncc * cfg->nstokes * kK);
+    rc = rc ? rc : dalloc(&p->d_scl, sizeof(float) * ncc * cfg->nstokes * kK);
+    if (cfg->do_ipfb) rc = rc ? rc : dalloc(&p->d_vdif, (size_t)ncc * ns * 544);
+    rc = rc ? rc : dalloc(&p->d_hdr, sizeof(uint32_t) * 8 * ncc);
+    if (!rc) {
+        for (int b = 0; b < 2 && !rc; b++)
+            rc = check_cuda(cudaMemsetAsync(p->d_hist[b], 0, (size_t)ncc * p->ninputs * kHistFrames * kK * 2,
+                                            p->s_comp),
+                            "memset history");
+        rc = rc ? rc : check_cuda(cudaMemsetAsync(p->d_hdr, 0, sizeof(uint32_t) * 8 * ncc, p->s_comp), "memset hdr");
+        rc = rc ? rc : check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
+    }
+    if (rc) {
+        vgb_pipeline_destroy(p);
+        return rc;
+    }
+    *out = p;
+    return VGB_SUCCESS;
+}
+
+int vgb_pipeline_destroy(vgb_pipeline *p)
+{
+    if (!p) return VGB_SUCCESS;
+    if (p->s_comp) cudaStreamSynchronize(p->s_comp);
+    if (p->s_copy) cudaStreamSynchronize(p->s_copy);
+    void *bufs[] = {p->d_filter, p->d_coeffs, p->d_W, p->d_volt[0], p->d_volt[1], p->d_hist[0], p->d_hist[1],
+                    p->d_S, p->d_e, p->d_incoh, p->d_ehist[0], p->d_ehist[1], p->d_psrfits, p->d_off, p->d_scl,
+                    p->d_vdif, p->d_hdr};
+    for (void *b : bufs)
+        if (b) cudaFree(b);
+    for (int b = 0; b < 2; b++) {
+        if (p->ev_copied[b]) cudaEventDestroy(p->ev_copied[b]);
+        if (p->ev_consumed[b]) cudaEventDestroy(p->ev_consumed[b]);
+    }
+    if (p->s_comp) cudaStreamDestroy(p->s_comp);
+    if (p->s_copy) cudaStreamDestroy(p->s_copy);
+    delete p;
+    return VGB_SUCCESS;
+}
+
+int vgb_pipeline_set_filters(vgb_pipeline *p, const int32_t *analysis, const float *synthesis)
+{
+    if (!p || !analysis) return set_error(VGB_ERR_INVALID, "NULL argument");
+    if (p->cfg.do_ipfb && !synthesis) return set_error(VGB_ERR_INVALID, "synthesis filter required for the IPFB");
+    p->fp32_wola = vgb_filter_fp32_exact(analysis, kP, kK) != 0;
+    int rc = check_cuda(cudaMemcpyAsync(p->d_filter, analysis, sizeof(int32_t) * kK * kP, cudaMemcpyHostToDevice,
+                                        p->s_comp),
+                        "upload analysis filter");
+    if (!rc && synthesis)
+        rc = check_cuda(cudaMemcpyAsync(p->d_coeffs, synthesis, sizeof(float) * kK * kP, cudaMemcpyHostToDevice,
+                                        p->s_comp),
+                        "upload synthesis filter");
+    return rc ? rc : check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
+}
+
+int vgb_pipeline_set_weights(vgb_pipeline *p, const void *W, int on_device)
+{
+    if (!p || !W) return set_error(VGB_ERR_INVALID, "NULL argument");
+    const size_t bytes = sizeof(float4) * 2 * p->cfg.ncc * p->cfg.nant * kK;
+    return check_cuda(cudaMemcpyAsync(p->d_W, W, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                      p->s_comp),
+                      "upload weights");
+}
+
+int vgb_pipeline_set_vdif_header(vgb_pipeline *p, const uint32_t *hdr)
+{
+    if (!p || !hdr) return set_error(VGB_ERR_INVALID, "NULL argument");
+    int rc = check_cuda(cudaMemcpyAsync(p->d_hdr, hdr, sizeof(uint32_t) * 8 * p->cfg.ncc, cudaMemcpyHostToDevice,
+                                        p->s_comp),
+                        "upload VDIF header");
+    return rc ? rc : check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
+}
+
+int vgb_pipeline_run_device(vgb_pipeline *p, const void *d_voltages, long long cur_cc_stride)
+{
+    if (!p || !d_voltages) return set_error(VGB_ERR_INVALID, "NULL argument");
+    if (cur_cc_stride < p->second_bytes && p->cfg.ncc > 1)
+        return set_error(VGB_ERR_INVALID, "coarse-channel stride smaller than one second");
+    return pipeline_second(p, static_cast<const char2 *>(d_voltages), cur_cc_stride);
+}
+
+int vgb_pipeline_run_host(vgb_pipeline *p, const void *h_voltages, long long cur_cc_stride)
+{
+    if (!p || !h_voltages) return set_error(VGB_ERR_INVALID, "NULL argument");
+    if (cur_cc_stride < p->second_bytes && p->cfg.ncc > 1)
+        return set_error(VGB_ERR_INVALID, "coarse-channel stride smaller than one second");
+    const size_t total = (size_t)p->second_bytes * p->cfg.ncc;
+    const int b = p->host_buf;
+    int rc;
+    if (!p->d_volt[b] && (rc = dalloc(&p->d_volt[b], total))) return rc;
+    // the buffer is free once the compute that last read it has finished
+    rc = check_cuda(cudaStreamWaitEvent(p->s_copy, p->ev_consumed[b], 0), "wait consumed");
+    if (rc) return rc;
+    if (cur_cc_stride == p->second_bytes || p->cfg.ncc == 1) {
+        rc = check_cuda(cudaMemcpyAsync(p->d_volt[b], h_voltages, total, cudaMemcpyHostToDevice, p->s_copy), "H2D");
+    } else {
+        rc = check_cuda(cudaMemcpy2DAsync(p->d_volt[b], (size_t)p->second_bytes, h_voltages, (size_t)cur_cc_stride,
+                                          (size_t)p->second_bytes, p->cfg.ncc, cudaMemcpyHostToDevice, p->s_copy),
+                        "H2D");
+    }
+    if (rc) return rc;
+    rc = check_cuda(cudaEventRecord(p->ev_copied[b], p->s_copy), "record copied");
+    rc = rc ? rc : check_cuda(cudaStreamWaitEvent(p->s_comp, p->ev_copied[b], 0), "wait copied");
+    if (rc) return rc;
+    rc = pipeline_second(p, p->d_volt[b], p->second_bytes);
+    if (rc) return rc;
+    rc = check_cuda(cudaEventRecord(p->ev_consumed[b], p->s_comp), "record consumed");
+    p->host_buf ^= 1;
+    return rc;
+}
+
+int vgb_pipeline_fetch(vgb_pipeline *p, uint8_t *psrfits, float *offsets, float *scales, uint8_t *vdif)
+{
+    if (!p) return set_error(VGB_ERR_INVALID, "NULL pipeline");
+    const vgb_pipeline_config &c = p->cfg;
+    const size_t ns = p->nspectra;
+    int rc = VGB_SUCCESS;
+    if (psrfits)
+        rc = check_cuda(cudaMemcpyAsync(psrfits, p->d_psrfits, ns * c.nstokes * c.ncc * kK, cudaMemcpyDeviceToHost,
+                                        p->s_comp),
+                        "D2H psrfits");
+    if (!rc && offsets)
+        rc = check_cuda(cudaMemcpyAsync(offsets, p->d_off, sizeof(float) * c.ncc * c.nstokes * kK,
+                                        cudaMemcpyDeviceToHost, p->s_comp),
+                        "D2H offsets");
+    if (!rc && scales)
+        rc = check_cuda(cudaMemcpyAsync(scales, p->d_scl, sizeof(float) * c.ncc * c.nstokes * kK,
+                                        cudaMemcpyDeviceToHost, p->s_comp),
+                        "D2H scales");
+    if (!rc && vdif) {
+        if (!c.do_ipfb) return set_error(VGB_ERR_STATE, "pipeline was created without the IPFB");
+        rc = check_cuda(cudaMemcpyAsync(vdif, p->d_vdif, (size_t)c.ncc * ns * 544, cudaMemcpyDeviceToHost, p->s_comp),
+                        "D2H vdif");
+    }
+    if (rc) return rc;
+    rc = check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
+    if (rc) return rc;
+    return vgb_check_device_status(p->s_comp, nullptr);
+}
+
+int vgb_pipeline_fetch_raw(vgb_pipeline *p, float *S_, void *e, float *incoh)
+{
+    if (!p) return set_error(VGB_ERR_INVALID, "NULL pipeline");
+    const size_t n = (size_t)p->cfg.ncc * p->nspectra * kK;
+    int rc = VGB_SUCCESS;
+    if (S_)
+        rc = check_cuda(cudaMemcpyAsync(S_, p->d_S, sizeof(float) * n * p->cfg.nstokes, cudaMemcpyDeviceToHost,
+                                        p->s_comp),
+                        "D2H S");
+    if (!rc && e)
+        rc = check_cuda(cudaMemcpyAsync(e, p->d_e, sizeof(float4) * n, cudaMemcpyDeviceToHost, p->s_comp), "D2H e");
+    if (!rc && incoh)
+        rc = check_cuda(cudaMemcpyAsync(incoh, p->d_incoh, sizeof(float) * n, cudaMemcpyDeviceToHost, p->s_comp),
+                        "D2H incoh");
+    if (rc) return rc;
+    return check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
+}
+
+int vgb_pipeline_device_products(vgb_pipeline *p, const float **S_, const void **e, const float **incoh,
+                                 const uint8_t **psrfits, const uint8_t **vdif)
+{
+    if (!p) return set_error(VGB_ERR_INVALID, "NULL pipeline");
+    int rc = check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
+    if (rc) return rc;
+    if (S_) *S_ = p->d_S;
+    if (e) *e = p->d_e;
+    if (incoh) *incoh = p->d_incoh;
+    if (psrfits) *psrfits = p->d_psrfits;
+    if (vdif) *vdif = p->d_vdif;
+    return VGB_SUCCESS;
+}
+
+int vgb_pipeline_launch_count(vgb_pipeline *p) { return p ? p->launches : 0; }
+
+} // extern "C"

@@ -1,0 +1,97 @@
+// Kernel argument blocks and launchers shared by the kernel files and the
+// C-ABI layer (vgb_api.cu). Every launcher returns a VGB_* status.
+#pragma once
+
+#include "vgb_internal.cuh"
+
+namespace vgb {
+
+struct BeamArgs {
+    VoltView vv;
+    const int *filter;      // K*P taps, reference order
+    const float4 *W;        // [cc][nant][K][2]: (w00, w01), (w10, w11)
+    long long W_cc;         // float4 stride between coarse channels
+    int nspectra;
+    int nant;
+    float invw;
+    int nstokes;            // 1 or 4
+    float *S;               // [cc][s][nstokes][K]
+    long long S_cc;
+    float4 *e;              // [cc][s][K] (ex, ey), nullable
+    long long e_cc;
+    float *incoh;           // [cc][s][K], nullable
+    long long inc_cc;
+    unsigned *status;
+};
+
+struct PackArgs {
+    VoltView vv;
+    const int *filter;
+    const int *i_idx;       // MWAX input -> legacy input (pfb.cpp:410-419)
+    int nspectra;
+    unsigned flags;         // PFB_COMPLEX_INT4 / PFB_IMAG_PART_FIRST
+    void *out;              // [cc][s][K][I] uint8 or double2
+    long long out_cc;       // elements between coarse channels
+    unsigned *status;
+};
+
+struct RenormArgs {
+    const float *S;        // [cc][p][nstep][nstokes][nchan]
+    long long S_cc;
+    int npointing, nstep, nstokes, nchan;
+    uint8_t *out;          // out + cc*out_cc + p*out_p + s*out_s + st*out_st + c
+    long long out_cc, out_p, out_s, out_st;
+    float *offsets, *scales; // + cc*stat_cc + (p*nstokes + st)*nchan + c
+    long long stat_cc;
+};
+
+struct LegacyArgs {
+    const void *v;           // [s][c][ni] uint8 (int4) or double2
+    int datatype;            // VGB_INT4 or VGB_DBL
+    int nsamples, nchan, nant;
+    const uint32_t *polQ, *polP;
+    const float4 *W;         // [p][nant][nchan][2]
+    int npointing;
+    float invw;
+    int nstokes;
+    float *S;                // [p][s][nstokes][nchan]
+    float4 *e;               // [p][s][nchan] nullable
+    float *incoh;            // [s][nchan] nullable (int4 only)
+};
+
+struct IpfbArgs {
+    const float4 *e;        // [job][ns][K] (ex, ey) beamformed voltages
+    long long e_job;
+    const float4 *hist;     // [job][P][K] previous second's last P samples; null = zeros
+    long long hist_job;
+    const float *coeffs;    // [P*K] synthesis filter (scaled)
+    int nsamples;           // fine samples in the second
+    float *out_f;           // [job][ns*K][2][2] nullable (cu_invert_pfb output)
+    long long outf_job;
+    uint8_t *vdif;          // [job][ns][544] nullable
+    long long vdif_job;
+    const uint32_t *hdr;    // [job][8] header of frame 0; nullable = zero header
+    int frame_offset;
+};
+
+int launch_beam(const BeamArgs &a, int ncc, bool int32_wola, bool fpga, bool demote, cudaStream_t st);
+int launch_pack(const PackArgs &a, int ncc, bool int32_wola, bool fpga, bool demote, cudaStream_t st);
+int launch_phase(const double *unit, const double *east, const double *north, const double *height,
+                 const double *cable, const double *freqs, int npointing, int nant, int nchan, double href,
+                 double2 *phi, cudaStream_t st);
+int launch_jones(const double2 *D, const double2 *B, int npointing, int nant, int nchan, double2 *J,
+                 cudaStream_t st);
+int launch_weights(const double2 *J, const double2 *phi, long long n, float4 *W, cudaStream_t st);
+int launch_renorm(const RenormArgs &a, int ncc, cudaStream_t st);
+int launch_incoh(const uint8_t *data, long long nrows, int ninput, float *incoh, cudaStream_t st);
+int launch_legacy_beam(const LegacyArgs &a, cudaStream_t st);
+int launch_ipfb(const IpfbArgs &a, int njobs, cudaStream_t st);
+int launch_wola_staged(const VoltView &vv, const int *filter, int nspectra, int2 *b, cudaStream_t st);
+int launch_round_staged(int *data, long long n, int fpga, cudaStream_t st);
+int launch_fft_staged(float2 *rows, long long nrows, cudaStream_t st);
+int launch_hist_gather(const char2 *cur, long long cur_block, long long cc_cur, int ninputs, int nblocks, int ncc,
+                       char2 *hist, long long cc_hist, cudaStream_t st);
+int launch_pack_staged(const float2 *ffted, int nspectra, int ninputs, const int *i_idx, unsigned flags,
+                       void *out, cudaStream_t st);
+
+} // namespace vgb

@@ -1,0 +1,299 @@
+"""ctypes binding of the GB300 library's C ABI (include/vcsbeam_gb300.h).
+
+The compute lives in ``lib/libvcsbeam_gb300.so`` (CUDA, sm_103a); this module
+only marshals arguments. Device buffers are torch tensors (or raw integer
+addresses); torch supplies allocation and the current stream, nothing else.
+There is no fallback: if the library is missing, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libvcsbeam_gb300.so")
+
+NCHAN = 128
+NTAPS = 12
+VSPVB = 64000
+FRAMES_PER_BLOCK = VSPVB // NCHAN
+HIST_FRAMES = NTAPS
+
+PFB_COMPLEX_INT4 = 0x10
+PFB_COMPLEX_FLOAT64 = 0x20
+PFB_IMAG_PART_FIRST = 0x100
+PFB_EMULATE_FPGA = 0x200
+PFB_SMART = 0x21D
+PFB_FULL_PRECISION = 0x2D
+WOLA_FP32 = 0x10000
+INT4 = 0
+DBL = 1
+
+
+class VGBError(RuntimeError):
+    pass
+
+
+class Voltages(ctypes.Structure):
+    _fields_ = [
+        ("hist", ctypes.c_void_p),
+        ("hist_input_stride", ctypes.c_longlong),
+        ("hist_cc_stride", ctypes.c_longlong),
+        ("cur", ctypes.c_void_p),
+        ("cur_block_stride", ctypes.c_longlong),
+        ("cur_cc_stride", ctypes.c_longlong),
+        ("ninputs", ctypes.c_int),
+        ("nblocks", ctypes.c_int),
+    ]
+
+
+class PipelineConfig(ctypes.Structure):
+    _fields_ = [
+        ("ncc", ctypes.c_int),
+        ("nant", ctypes.c_int),
+        ("nblocks", ctypes.c_int),
+        ("nstokes", ctypes.c_int),
+        ("pfb_flags", ctypes.c_uint),
+        ("do_ipfb", ctypes.c_int),
+        ("invw", ctypes.c_float),
+    ]
+
+
+_lib = None
+V = ctypes.c_void_p
+I = ctypes.c_int
+LL = ctypes.c_longlong
+U = ctypes.c_uint
+Fl = ctypes.c_float
+Db = ctypes.c_double
+
+_SIGS = {
+    "vgb_last_error": (ctypes.c_char_p, []),
+    "vgb_version": (I, []),
+    "vgb_filter_fp32_exact": (I, [V, I, I]),
+    "vgb_check_device_status": (I, [V, ctypes.POINTER(U)]),
+    "vgb_beamform_mwax": (I, [ctypes.POINTER(Voltages), I, I, V, I, I, U, V, I, Fl, I, V, V, V, V]),
+    "vgb_fpfb": (I, [ctypes.POINTER(Voltages), I, I, V, I, I, V, U, V, V]),
+    "vgb_wola": (I, [ctypes.POINTER(Voltages), I, V, I, I, V, V]),
+    "vgb_round": (I, [V, LL, I, V]),
+    "vgb_fft128": (I, [V, LL, V]),
+    "vgb_pack": (I, [V, I, I, V, U, V, V]),
+    "vgb_phase": (I, [V, V, V, V, V, V, I, I, I, Db, V, V]),
+    "vgb_jones": (I, [V, V, I, I, I, V, V]),
+    "vgb_weights": (I, [V, V, LL, V, V]),
+    "vgb_beamform_legacy": (I, [V, I, I, I, I, V, V, V, I, Fl, I, V, V, V, V]),
+    "vgb_incoh_beam": (I, [V, LL, I, V, V]),
+    "vgb_renormalise": (I, [V, I, I, I, I, I, V, LL, LL, LL, LL, V, V, V]),
+    "vgb_ipfb": (I, [V, LL, V, LL, V, I, I, I, I, V, V, V, I, V]),
+    "vgb_pipeline_create": (I, [ctypes.POINTER(PipelineConfig), ctypes.POINTER(V)]),
+    "vgb_pipeline_destroy": (I, [V]),
+    "vgb_pipeline_set_filters": (I, [V, V, V]),
+    "vgb_pipeline_set_weights": (I, [V, V, I]),
+    "vgb_pipeline_set_vdif_header": (I, [V, V]),
+    "vgb_pipeline_run_device": (I, [V, V, LL]),
+    "vgb_pipeline_run_host": (I, [V, V, LL]),
+    "vgb_pipeline_fetch": (I, [V, V, V, V, V]),
+    "vgb_pipeline_fetch_raw": (I, [V, V, V, V]),
+    "vgb_pipeline_device_products": (I, [V, ctypes.POINTER(V), ctypes.POINTER(V), ctypes.POINTER(V),
+                                         ctypes.POINTER(V), ctypes.POINTER(V)]),
+    "vgb_pipeline_launch_count": (I, [V]),
+}
+
+
+def exported_symbols():
+    """Names the C ABI exports (the header's declarations)."""
+    return list(_SIGS)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise VGBError(f"{LIB_PATH} is not built; run __graft_entry__.build()")
+        l = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(l, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+def check(rc: int):
+    if rc != 0:
+        raise VGBError(f"vgb error {rc}: {lib().vgb_last_error().decode()}")
+
+
+def ptr(x):
+    """Device (or host) address of a torch tensor / numpy array / int / None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    return x.data_ptr()
+
+
+def stream_ptr(stream=None):
+    import torch
+
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+# --------------------------------------------------------------------------
+# voltage descriptors
+# --------------------------------------------------------------------------
+
+def reference_buffer_voltages(buf, ninputs: int, nblocks: int, ncc: int = 1, cc_stride: int = 0) -> Voltages:
+    """The reference's read buffer: one margin block then `nblocks` blocks
+    (buffer.c:52-77). `buf` is a device tensor or address."""
+    base = ptr(buf)
+    block = ninputs * VSPVB * 2
+    return Voltages(hist=base + (FRAMES_PER_BLOCK - HIST_FRAMES) * NCHAN * 2, hist_input_stride=VSPVB * 2,
+                    hist_cc_stride=cc_stride, cur=base + block, cur_block_stride=block, cur_cc_stride=cc_stride,
+                    ninputs=ninputs, nblocks=nblocks)
+
+
+# --------------------------------------------------------------------------
+# thin wrappers (all asynchronous on the given / current stream)
+# --------------------------------------------------------------------------
+
+def beamform_mwax(v: Voltages, ncc, nspectra, filt, flags, W, nant, invw, nstokes, S, e=None, incoh=None,
+                  stream=None):
+    check(lib().vgb_beamform_mwax(ctypes.byref(v), ncc, nspectra, ptr(filt), NTAPS, NCHAN, flags, ptr(W), nant,
+                                  float(invw), nstokes, ptr(S), ptr(e), ptr(incoh), stream_ptr(stream)))
+
+
+def fpfb(v: Voltages, ncc, nspectra, filt, i_idx, flags, out, stream=None):
+    check(lib().vgb_fpfb(ctypes.byref(v), ncc, nspectra, ptr(filt), NTAPS, NCHAN, ptr(i_idx), flags, ptr(out),
+                         stream_ptr(stream)))
+
+
+def wola(v: Voltages, nspectra, filt, b, stream=None):
+    check(lib().vgb_wola(ctypes.byref(v), nspectra, ptr(filt), NTAPS, NCHAN, ptr(b), stream_ptr(stream)))
+
+
+def round_(b, nvalues, emulate_fpga, stream=None):
+    check(lib().vgb_round(ptr(b), nvalues, int(emulate_fpga), stream_ptr(stream)))
+
+
+def fft128(rows, nrows, stream=None):
+    check(lib().vgb_fft128(ptr(rows), nrows, stream_ptr(stream)))
+
+
+def pack(ffted, nspectra, ninputs, i_idx, flags, out, stream=None):
+    check(lib().vgb_pack(ptr(ffted), nspectra, ninputs, ptr(i_idx), flags, ptr(out), stream_ptr(stream)))
+
+
+def phase(unit, east, north, height, cable, freqs, npointing, nant, nchan, href, phi, stream=None):
+    check(lib().vgb_phase(ptr(unit), ptr(east), ptr(north), ptr(height), ptr(cable), ptr(freqs), npointing, nant,
+                          nchan, float(href), ptr(phi), stream_ptr(stream)))
+
+
+def jones(D, B, npointing, nant, nchan, J, stream=None):
+    check(lib().vgb_jones(ptr(D), ptr(B), npointing, nant, nchan, ptr(J), stream_ptr(stream)))
+
+
+def weights(J, phi, n, W, stream=None):
+    check(lib().vgb_weights(ptr(J), ptr(phi), n, ptr(W), stream_ptr(stream)))
+
+
+def beamform_legacy(v, datatype, nsamples, nchan, nant, polQ, polP, W, npointing, invw, nstokes, S, e=None,
+                    incoh=None, stream=None):
+    check(lib().vgb_beamform_legacy(ptr(v), datatype, nsamples, nchan, nant, ptr(polQ), ptr(polP), ptr(W),
+                                    npointing, float(invw), nstokes, ptr(S), ptr(e), ptr(incoh),
+                                    stream_ptr(stream)))
+
+
+def incoh_beam(data, nrows, ninput, out, stream=None):
+    check(lib().vgb_incoh_beam(ptr(data), nrows, ninput, ptr(out), stream_ptr(stream)))
+
+
+def renormalise(S, ncc, npointing, nstep, nstokes, nchan, out, out_cc, out_p, out_s, out_st, offsets, scales,
+                stream=None):
+    check(lib().vgb_renormalise(ptr(S), ncc, npointing, nstep, nstokes, nchan, ptr(out), out_cc, out_p, out_s,
+                                out_st, ptr(offsets), ptr(scales), stream_ptr(stream)))
+
+
+def ipfb(e, e_job_stride, hist, hist_job_stride, coeffs, nsamples, njobs, out_f=None, vdif=None, hdr=None,
+         frame_offset=0, stream=None):
+    check(lib().vgb_ipfb(ptr(e), e_job_stride, ptr(hist), hist_job_stride, ptr(coeffs), NTAPS, NCHAN, nsamples,
+                         njobs, ptr(out_f), ptr(vdif), ptr(hdr), frame_offset, stream_ptr(stream)))
+
+
+def check_device_status(stream=None) -> int:
+    flags = U(0)
+    rc = lib().vgb_check_device_status(stream_ptr(stream), ctypes.byref(flags))
+    check(rc)
+    return flags.value
+
+
+def filter_fp32_exact(h: np.ndarray) -> bool:
+    h = np.ascontiguousarray(h, dtype=np.int32)
+    return bool(lib().vgb_filter_fp32_exact(h.ctypes.data, NTAPS, NCHAN))
+
+
+# --------------------------------------------------------------------------
+# pipeline
+# --------------------------------------------------------------------------
+
+class Pipeline:
+    """One second of all coarse channels per step (vgb_pipeline_*)."""
+
+    def __init__(self, ncc, nant, nblocks=20, nstokes=4, pfb_flags=0, do_ipfb=True, invw=None):
+        cfg = PipelineConfig(ncc=ncc, nant=nant, nblocks=nblocks, nstokes=nstokes, pfb_flags=pfb_flags,
+                             do_ipfb=int(do_ipfb), invw=float(invw if invw is not None else 1.0 / (2 * nant)))
+        h = V()
+        check(lib().vgb_pipeline_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+        self.cfg = cfg
+        self.nspectra = nblocks * FRAMES_PER_BLOCK
+        self.second_bytes = nblocks * 2 * nant * VSPVB * 2
+
+    def close(self):
+        if self.h:
+            lib().vgb_pipeline_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_filters(self, analysis: np.ndarray, synthesis: np.ndarray | None):
+        a = np.ascontiguousarray(analysis, dtype=np.int32)
+        s = None if synthesis is None else np.ascontiguousarray(synthesis, dtype=np.float32)
+        check(lib().vgb_pipeline_set_filters(self.h, a.ctypes.data, None if s is None else s.ctypes.data))
+
+    def set_weights(self, W, on_device: bool):
+        check(lib().vgb_pipeline_set_weights(self.h, ptr(W), int(on_device)))
+
+    def set_vdif_header(self, hdr: np.ndarray):
+        hdr = np.ascontiguousarray(hdr, dtype=np.uint32)
+        check(lib().vgb_pipeline_set_vdif_header(self.h, hdr.ctypes.data))
+
+    def run_device(self, d_volt, cc_stride=None):
+        check(lib().vgb_pipeline_run_device(self.h, ptr(d_volt), cc_stride or self.second_bytes))
+
+    def run_host(self, h_volt, cc_stride=None):
+        check(lib().vgb_pipeline_run_host(self.h, ptr(h_volt), cc_stride or self.second_bytes))
+
+    def fetch(self, psrfits=None, offsets=None, scales=None, vdif=None):
+        check(lib().vgb_pipeline_fetch(self.h, ptr(psrfits), ptr(offsets), ptr(scales), ptr(vdif)))
+
+    def fetch_raw(self, S=None, e=None, incoh=None):
+        check(lib().vgb_pipeline_fetch_raw(self.h, ptr(S), ptr(e), ptr(incoh)))
+
+    def device_products(self):
+        S, e, inc, ps, vd = V(), V(), V(), V(), V()
+        check(lib().vgb_pipeline_device_products(self.h, ctypes.byref(S), ctypes.byref(e), ctypes.byref(inc),
+                                                 ctypes.byref(ps), ctypes.byref(vd)))
+        return S.value, e.value, inc.value, ps.value, vd.value
+
+    def launch_count(self) -> int:
+        return int(lib().vgb_pipeline_launch_count(self.h))

@@ -1,0 +1,129 @@
+"""The one-second streaming pipeline (vgb_pipeline_*) over two seconds and two
+coarse channels, against the oracle chain on the same timeline: the voltage
+and beam histories carried across the second boundary, spliced PSRFITS
+bytes, and VDIF.
+
+Tolerances as in the per-kernel tests: Stokes within 1e-5 of the largest
+magnitude; 8-bit bytes within one LSB on <= 1e-4 of samples (the reference
+maps each channel's maximum to 0; both sides do, at the same sample).
+"""
+import numpy as np
+import pytest
+
+import synthetic as SY
+from helpers import dev, host, pol_lists, rel_err, tables, torch_cuda
+
+pytestmark = pytest.mark.gpu
+
+K, P = 128, 12
+NANT, NCC, NBLK = 16, 2, 2
+NI = 2 * NANT
+NS = NBLK * 500
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return torch_cuda()
+
+
+@pytest.fixture(scope="module")
+def vgb_mod(torch):
+    import vgb
+
+    vgb.lib()
+    return vgb
+
+
+@pytest.fixture(scope="module")
+def setup(oracle_mod):
+    # voltages [second][cc][block][input][sample][2]
+    volt = oracle_mod.gen_int8(77, 2 * NCC * NBLK * NI * 64000 * 2, 16).reshape(2, NCC, NBLK, NI, 64000, 2)
+    filt = SY.analysis_filter_int16()
+    syn = SY.synthesis_filter(scale=SY.synthesis_scale(filt))
+    tabs = [tables(NANT, cc=cc, seed=cc + 1) for cc in range(NCC)]
+    return volt, filt, syn, tabs
+
+
+def oracle_second(O, volt, t, cc, filt, J, phi, invw):
+    margin = np.zeros((1, NI, 64000, 2), np.int8) if t == 0 else volt[t - 1, cc, NBLK - 1:]
+    buf = np.ascontiguousarray(np.concatenate([margin, volt[t, cc]], axis=0))
+    i_idx = np.arange(NI, dtype=np.int32)  # identity VCS order
+    v = O.fpfb(buf, NI, NS, filt, K, P, i_idx, 0)
+    polQ, polP = pol_lists(i_idx)
+    return O.beamform(v, J, phi, polQ, polP, invw)
+
+
+def make_pipeline(vgb, torch, filt, syn, tabs, invw):
+    from helpers import weights_on_device
+
+    p = vgb.Pipeline(NCC, NANT, NBLK, nstokes=4, pfb_flags=0, do_ipfb=True, invw=invw)
+    p.set_filters(filt, syn)
+    W = torch.cat([weights_on_device(J, phi) for J, phi in tabs])
+    p.set_weights(W, on_device=True)
+    hdr = np.zeros((NCC, 8), np.uint32)
+    hdr[:, 0] = [100, 200]
+    p.set_vdif_header(hdr)
+    return p
+
+
+def test_pipeline_two_seconds(vgb_mod, torch, oracle_mod, setup):
+    volt, filt, syn, tabs = setup
+    invw = 1.0 / NI
+    p = make_pipeline(vgb_mod, torch, filt, syn, tabs, invw)
+    e_prev = [None] * NCC
+    for t in range(2):
+        d = dev(volt[t].reshape(-1).view(np.uint8))
+        p.run_device(d)
+        assert p.launch_count() >= 4
+        ps = np.empty((NS, 4, NCC * K), np.uint8)
+        off = np.empty((NCC, 4, K), np.float32)
+        sc = np.empty((NCC, 4, K), np.float32)
+        vd = np.empty((NCC, NS, 544), np.uint8)
+        p.fetch(ps, off, sc, vd)
+        S = np.empty((NCC, NS, 4, K), np.float32)
+        e = np.empty((NCC, NS, K, 2), np.complex64)
+        p.fetch_raw(S, e)
+        for cc in range(NCC):
+            J, phi = tabs[cc]
+            Sref, eref = oracle_second(oracle_mod, volt, t, cc, filt, J, phi, invw)
+            assert rel_err(S[cc], Sref[0]) < 1e-5
+            assert rel_err(e[cc], eref[0]) < 1e-5
+            o, s, u = oracle_mod.renormalise(S[cc][None])
+            assert np.array_equal(ps[:, :, cc * K:(cc + 1) * K], u[0])
+            _, _, uref = oracle_mod.renormalise(Sref)
+            d8 = np.abs(ps[:, :, cc * K:(cc + 1) * K].astype(np.int16) - uref[0].astype(np.int16))
+            assert ((d8 > 1).mean() <= 1e-4) and ((d8 > 0).mean() <= 1e-3)
+            # VDIF against the oracle IPFB of the oracle's beam voltages
+            hist = np.zeros((P, K, 2)) if t == 0 else e_prev[cc][NS - P:]
+            x = np.concatenate([hist, eref[0]], axis=0)
+            truth = oracle_mod.ipfb(x, syn, P)
+            flt = np.stack([truth.real, truth.imag], axis=-1).astype(np.float32).reshape(NS, 512)
+            q = oracle_mod.vdif_quantise(flt)
+            dq = np.abs(vd[cc, :, 32:].astype(np.int16) - q.astype(np.int16))
+            assert dq.max() <= 1 and (dq > 0).mean() <= 1e-4
+            assert np.all(vd[cc, :, :4].copy().view(np.uint32)[:, 0] == (100, 200)[cc])
+            e_prev[cc] = eref[0]
+    p.close()
+
+
+def test_pipeline_host_equals_device(vgb_mod, torch, setup):
+    volt, filt, syn, tabs = setup
+    invw = 1.0 / NI
+    outs = []
+    for mode in ("device", "host"):
+        p = make_pipeline(vgb_mod, torch, filt, syn, tabs, invw)
+        res = []
+        for t in range(2):
+            if mode == "device":
+                p.run_device(dev(volt[t].reshape(-1).view(np.uint8)))
+            else:
+                hb = torch.from_numpy(volt[t].reshape(-1).view(np.uint8).copy()).pin_memory()
+                p.run_host(hb)
+            ps = np.empty((NS, 4, NCC * K), np.uint8)
+            vd = np.empty((NCC, NS, 544), np.uint8)
+            p.fetch(ps, None, None, vd)
+            res.append((ps, vd))
+        p.close()
+        outs.append(res)
+    for (a, b), (c, d) in zip(outs[0], outs[1]):
+        assert np.array_equal(a, c) and np.array_equal(b, d)
