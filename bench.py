@@ -1,0 +1,359 @@
+"""Benchmark: real-time factor (data-seconds per wall-second) of the VCSBeam
+voltage hot path on GB300.
+
+Workload (one step = one data-second of the full band): 24 coarse channels x
+128 tiles x 2 pols of 8-bit MWAX voltages (Gaussian sigma 16, clipped to
++-127, synthetic and seeded), forward fine PFB 12 taps x 128 channels, one
+tied-array beam + the incoherent beam, full Stokes at 100 us into channel-
+spliced 8-bit PSRFITS rows, and the inverse PFB back to 1.28 MHz 8-bit VDIF,
+FP32 throughout. Each step reads 15.7 GB of voltages (> the 129 MB L2, so no
+flush is needed); two distinct seconds stay resident and alternate.
+
+  value  device-resident input: voltages already in HBM when timing starts
+  e2e    the same through the pipeline's host API: every step copies its
+         second of voltages from pinned host memory to the device and its
+         PSRFITS + VDIF products back
+  --impl reference  the reference's CPU path timed on the host cores: the
+         reference has no CPU implementation of its kernels, so this is the
+         oracle's OpenMP FP32 transcription of them (oracle/oracle.c).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "mwa-vcsbeam_gb300"))
+
+METRIC = "real-time factor (data-s/wall-s) on 1 GB300, 1→1024 beams, vs plain FP32 at ≤1e-3"
+UNIT = "data-s/wall-s"
+NCC, NANT, NBLK, K, P = 24, 128, 20, 128, 12
+NI = 2 * NANT
+NSPEC = NBLK * 500
+SECOND_BYTES = NBLK * NI * 64000 * 2           # one coarse channel, one second
+PSRFITS_BYTES = NSPEC * 4 * NCC * K
+VDIF_BYTES = NCC * NSPEC * 544
+STAT_BYTES = 2 * NCC * 4 * K * 4
+WORKLOAD = ("full band: 24 coarse channels x 128 tiles x 2 pols, 8-bit MWAX voltages (sigma 16), "
+            "fine PFB 12x128 -> 1 tied-array beam + incoherent, full Stokes 100 us -> 8-bit PSRFITS; "
+            "inverse PFB -> 8-bit VDIF; FP32")
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+# --------------------------------------------------------------------------
+# clocks
+# --------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(gpu_index)], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# synthetic workload on the device
+# --------------------------------------------------------------------------
+def make_voltages(torch, nsec: int, seed: int):
+    """[nsec][cc][block][input][sample][2] int8, Gaussian sigma 16 clipped."""
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    out = torch.empty((nsec, NCC, SECOND_BYTES), dtype=torch.int8, device="cuda")
+    for s in range(nsec):
+        for cc in range(NCC):
+            x = torch.randn(SECOND_BYTES, generator=g, device="cuda", dtype=torch.float32)
+            out[s, cc] = x.mul_(16.0).round_().clamp_(-127, 127).to(torch.int8)
+            del x
+    return out
+
+
+def make_weights(torch, vgb, SY):
+    """W [cc][tile][128][2][2] complex float = phi * J^-1 built on the device
+    in FP64 (vgb_jones, vgb_phase, vgb_weights)."""
+    D = SY.calibration_jones(NANT, K, seed=11)
+    B = SY.identity_beam(1, NANT)
+    east, north, height, cable = SY.tile_layout(NANT, seed=7)
+    unit = SY.unit_vectors(45.0, 20.0)
+
+    def d(a):
+        a = np.ascontiguousarray(a)
+        if np.iscomplexobj(a):
+            a = a.view(np.float64)
+        return torch.from_numpy(a.copy()).cuda()
+
+    J = torch.empty(NANT * K * 8, dtype=torch.float64, device="cuda")
+    vgb.jones(d(D), d(B), 1, NANT, K, J)
+    W = torch.empty((NCC, NANT * K, 8), dtype=torch.float32, device="cuda")
+    phi = torch.empty(NANT * K * 2, dtype=torch.float64, device="cuda")
+    geo = [d(x) for x in (unit, east, north, height, cable)]
+    for cc in range(NCC):
+        freqs = d(SY.fine_chan_freqs_hz(SY.coarse_chan_start_hz(cc)))
+        vgb.phase(*geo, freqs, 1, NANT, K, SY.MWA_ALTITUDE_METRES, phi)
+        vgb.weights(J, phi, NANT * K, W[cc])
+    torch.cuda.synchronize()
+    return W
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: the oracle's OpenMP FP32 transcription of the reference kernels
+# --------------------------------------------------------------------------
+def cpu_sample(nspec: int):
+    """Time one bounded sample: `nspec` fine spectra of one coarse channel
+    through the PFB + beamformer, the renormalise of those spectra and the
+    reference-algorithm inverse PFB + VDIF of the same time span."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    import synthetic as SY
+
+    nblk = (nspec + 11) // 500 + 2
+    htr = O.mwax_buffer(5, nblk, NI)
+    h = SY.analysis_filter_int16()
+    D = SY.calibration_jones(NANT, K, seed=11)
+    J = O.calc_j(D, SY.identity_beam(1, NANT))
+    e_, n_, h_, c_ = SY.tile_layout(NANT, seed=7)
+    phi = O.calc_phi(SY.unit_vectors(45.0, 20.0), e_, n_, h_, c_, SY.fine_chan_freqs_hz(SY.coarse_chan_start_hz(0)))
+    W = (phi[0][:, :, None, None] * J[0]).astype(np.complex64)
+    coeffs = SY.synthesis_filter(scale=SY.synthesis_scale(h))
+    ftr, fti = O.ipfb_table(coeffs, K)
+    t0 = time.perf_counter()
+    S, e, inc, nt = O.pfb_beam32(htr, NI, 0, nspec, h, K, P, False, W, 1.0 / NI)
+    _, _, _, nt2 = O.renormalise32(S)
+    x = np.concatenate([np.zeros((P, K, 2), np.complex64), e], axis=0)
+    _, nt3 = O.ipfb_vdif32(x, ftr, fti, P, 0, nspec * K)
+    dt = time.perf_counter() - t0
+    return dt, max(nt, nt2, nt3)
+
+
+def cpu_baseline_line(target_s: float = 12.0):
+    dt, nt = cpu_sample(20)                      # calibrate
+    nspec = int(min(NSPEC, max(20, 20 * target_s / max(dt, 1e-3))))
+    dt, nt = cpu_sample(nspec)
+    data_s = nspec / NSPEC / NCC                 # data-seconds of the full band
+    return {"value": data_s / dt, "unit": UNIT, "cores": nt, "kind": "port",
+            "sample": f"{nspec} fine spectra of 1 of 24 coarse channels ({nspec / NSPEC * 1e3:.0f} ms of one channel): "
+                      f"PFB + beam + renormalise + inverse PFB/VDIF, {dt:.1f} s on {nt} threads"}
+
+
+# --------------------------------------------------------------------------
+# arms
+# --------------------------------------------------------------------------
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    for _ in range(args.warmup):
+        cpu_sample(args.ref_spectra)
+    vals, total_dt, nt = [], 0.0, 1
+    for _ in range(args.steps):
+        dt, nt = cpu_sample(args.ref_spectra)
+        total_dt += dt
+        vals.append(dt)
+    data_s = args.steps * args.ref_spectra / NSPEC / NCC
+    value = data_s / total_dt
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total_dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "step": f"{args.ref_spectra} fine spectra of one coarse channel"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port",
+                             "sample": f"{args.ref_spectra} fine spectra of 1 of 24 coarse channels per step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def gb300_arm(args, rank, local_rank, world):
+    import torch
+
+    import synthetic as SY
+    import vgb
+
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    vgb.lib()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        import torch.distributed as dist
+
+        t = torch.tensor([x], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    volt = make_voltages(torch, args.resident, seed=1234 + rank)
+    W = make_weights(torch, vgb, SY)
+    h = SY.analysis_filter_int16()
+    syn = SY.synthesis_filter(scale=SY.synthesis_scale(h)).astype(np.float32)
+    pipe = vgb.Pipeline(NCC, NANT, NBLK, nstokes=4, pfb_flags=0, do_ipfb=True, invw=1.0 / NI)
+    pipe.set_filters(h, syn)
+    pipe.set_weights(W, on_device=True)
+    stream = pipe.stream()
+
+    # ---- device-resident throughput --------------------------------------
+    for i in range(args.warmup):
+        pipe.run_device(volt[i % args.resident])
+    pipe.sync()
+    pipe.enable_timing(True)
+    stage = np.zeros(4)
+    barrier()
+    clocks = ClockSampler(local_rank)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    launches = 0
+    for i in range(args.steps):
+        pipe.run_device(volt[i % args.resident])
+        launches += pipe.launch_count()
+        stage += np.array(pipe.stage_ms())   # synchronises on this second's last stage
+    ev1.record(stream)
+    ev1.synchronize()
+    barrier()
+    clk = clocks.stop()
+    pipe.enable_timing(False)
+    elapsed_s = max_over_ranks(ev0.elapsed_time(ev1) / 1e3)
+    value = world * args.steps / elapsed_s
+    stage /= args.steps
+
+    # ---- end to end through the host API ------------------------------------
+    hin = torch.empty(NCC * SECOND_BYTES, dtype=torch.int8, pin_memory=True)
+    hin.copy_(volt[0].reshape(-1))
+    ps = torch.empty(PSRFITS_BYTES, dtype=torch.uint8, pin_memory=True)
+    vd = torch.empty(VDIF_BYTES, dtype=torch.uint8, pin_memory=True)
+    off = torch.empty(NCC * 4 * K, dtype=torch.float32, pin_memory=True)
+    scl = torch.empty(NCC * 4 * K, dtype=torch.float32, pin_memory=True)
+    pipe.set_host_outputs(ps, off, scl, vd)
+    del volt
+    for _ in range(min(args.warmup, 3)):
+        pipe.run_host(hin)
+    pipe.sync()
+    barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    for _ in range(e2e_steps):
+        pipe.run_host(hin)
+    pipe.sync()
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e = {"value": world * e2e_steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": NCC * SECOND_BYTES,
+           "d2h_bytes_per_step": PSRFITS_BYTES + VDIF_BYTES + STAT_BYTES,
+           "steps": e2e_steps, "ms_per_step": 1e3 * e2e_s / e2e_steps,
+           "path": "vgb_pipeline_run_host from pinned host memory, products back to pinned host buffers; "
+                   "next second's copy overlaps this second's compute"}
+    pipe.close()
+
+    # ---- roofline of the dominant kernel (fused PFB + beamformer) -----------
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    alg_bytes = NCC * SECOND_BYTES          # the voltages it must read, per launch
+    achieved = alg_bytes / (stage[0] / 1e3) / 1e9
+    roofline = {"kernel": "beam_kernel (fused PFB + tied-array/incoherent beam + Stokes)", "bound": "hbm",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                "traffic": args.traffic, "alg_bytes_per_launch": alg_bytes,
+                "stage_ms": {"pfb_beam": stage[0], "renormalise": stage[1], "ipfb_vdif": stage[2],
+                             "history": stage[3]}}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "ncc": NCC, "ntiles": NANT, "nbeams": 1, "nstokes": 4,
+                       "step": "one data-second (24 coarse channels x 1 s)",
+                       "l2": "inputs larger than L2: each step reads a different 15.7 GB second",
+                       "resident_seconds": args.resident},
+            "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_line(args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--resident", type=int, default=2, help="distinct seconds kept in HBM")
+    ap.add_argument("--e2e-steps", type=int, default=40)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ref-spectra", type=int, default=400, help="reference arm: spectra per step")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per beam_kernel launch from an ncu capture (profiles/)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, local_rank, world = dist_env()
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+    else:
+        gb300_arm(args, rank, local_rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -242,6 +242,22 @@ int vgb_pipeline_device_products(vgb_pipeline *p, const float **S, const void **
                                  const uint8_t **psrfits, const uint8_t **vdif);
 /* Kernel launches the last vgb_pipeline_run_* issued. */
 int vgb_pipeline_launch_count(vgb_pipeline *p);
+/* The CUDA stream the pipeline computes on (cudaStream_t as void *). */
+void *vgb_pipeline_stream(vgb_pipeline *p);
+/* Host buffers (pinned for speed; each nullable) that every following
+ * vgb_pipeline_run_* fills asynchronously, on the compute stream right after
+ * the second's kernels: the vgb_pipeline_fetch products without a
+ * synchronisation, so the next second's host-to-device copy overlaps this
+ * second's compute. Call vgb_pipeline_sync() before reading them. */
+int vgb_pipeline_set_host_outputs(vgb_pipeline *p, uint8_t *psrfits, float *offsets, float *scales,
+                                  uint8_t *vdif);
+/* Wait for everything the pipeline has queued; reports kernel status. */
+int vgb_pipeline_sync(vgb_pipeline *p);
+/* Record CUDA events around each stage of every second (off by default). */
+int vgb_pipeline_enable_timing(vgb_pipeline *p, int on);
+/* Milliseconds per stage of the last second: [0] fused PFB + beamformer,
+ * [1] renormalise, [2] inverse PFB + VDIF, [3] history carry. Synchronises. */
+int vgb_pipeline_stage_ms(vgb_pipeline *p, float *ms, int n);
 
 #ifdef __cplusplus
 }

@@ -352,6 +352,12 @@ struct vgb_pipeline {
     long long second = 0;            // seconds completed
     int launches = 0;
     int host_buf = 0;
+    // asynchronous host outputs
+    uint8_t *h_psrfits = nullptr, *h_vdif = nullptr;
+    float *h_off = nullptr, *h_scl = nullptr;
+    // per-stage timing
+    bool timing = false;
+    cudaEvent_t ev_stage[5] = {};
 };
 
 namespace {
@@ -383,16 +389,22 @@ int pipeline_second(vgb_pipeline *p, const char2 *volt, long long cc_stride_byte
     v.ninputs = p->ninputs;
     v.nblocks = c.nblocks;
     const unsigned flags = c.pfb_flags | (p->fp32_wola ? VGB_WOLA_FP32 : 0u);
+    auto mark = [&](int i) {
+        return p->timing ? check_cuda(cudaEventRecord(p->ev_stage[i], p->s_comp), "stage event") : VGB_SUCCESS;
+    };
+    if ((rc = mark(0))) return rc;
     rc = vgb_beamform_mwax(&v, c.ncc, p->nspectra, p->d_filter, kP, kK, flags, p->d_W, c.nant, c.invw, c.nstokes,
                            p->d_S, p->d_e, p->d_incoh, p->s_comp);
     if (rc) return rc;
     p->launches++;
+    if ((rc = mark(1))) return rc;
     // spliced PSRFITS rows: [s][st][cc*128 + c]
     const long long row = (long long)c.nstokes * c.ncc * kK;
     rc = vgb_renormalise(p->d_S, c.ncc, 1, p->nspectra, c.nstokes, kK, p->d_psrfits, kK, 0, row,
                          (long long)c.ncc * kK, p->d_off, p->d_scl, p->s_comp);
     if (rc) return rc;
     p->launches++;
+    if ((rc = mark(2))) return rc;
     if (c.do_ipfb) {
         const long long ejob = (long long)p->nspectra * kK * 16;
         rc = vgb_ipfb(p->d_e, ejob, p->second > 0 ? p->d_ehist[cur] : nullptr, (long long)kHistFrames * kK * 16,
@@ -407,13 +419,33 @@ int pipeline_second(vgb_pipeline *p, const char2 *volt, long long cc_stride_byte
                         "carry beam history");
         if (rc) return rc;
     }
+    if ((rc = mark(3))) return rc;
     // carry the last 12 voltage frames of each input
     rc = launch_hist_gather(volt, (long long)p->ninputs * kVSPVB, cc_stride_bytes / 2, p->ninputs, c.nblocks, c.ncc,
                             p->d_hist[nxt], (long long)p->ninputs * kHistFrames * kK, p->s_comp);
     if (rc) return rc;
     p->launches++;
+    if ((rc = mark(4))) return rc;
     p->second++;
-    return VGB_SUCCESS;
+    // asynchronous copies of the products into the caller's host buffers
+    const size_t ns = p->nspectra;
+    if (p->h_psrfits)
+        rc = check_cuda(cudaMemcpyAsync(p->h_psrfits, p->d_psrfits, ns * c.nstokes * c.ncc * kK,
+                                        cudaMemcpyDeviceToHost, p->s_comp),
+                        "D2H psrfits");
+    if (!rc && p->h_off)
+        rc = check_cuda(cudaMemcpyAsync(p->h_off, p->d_off, sizeof(float) * c.ncc * c.nstokes * kK,
+                                        cudaMemcpyDeviceToHost, p->s_comp),
+                        "D2H offsets");
+    if (!rc && p->h_scl)
+        rc = check_cuda(cudaMemcpyAsync(p->h_scl, p->d_scl, sizeof(float) * c.ncc * c.nstokes * kK,
+                                        cudaMemcpyDeviceToHost, p->s_comp),
+                        "D2H scales");
+    if (!rc && p->h_vdif && c.do_ipfb)
+        rc = check_cuda(cudaMemcpyAsync(p->h_vdif, p->d_vdif, (size_t)c.ncc * ns * 544, cudaMemcpyDeviceToHost,
+                                        p->s_comp),
+                        "D2H vdif");
+    return rc;
 }
 
 } // namespace
@@ -434,6 +466,7 @@ int vgb_pipeline_create(const vgb_pipeline_config *cfg, vgb_pipeline **out)
     int rc = VGB_SUCCESS;
     rc = rc ? rc : check_cuda(cudaStreamCreateWithFlags(&p->s_comp, cudaStreamNonBlocking), "stream");
     rc = rc ? rc : check_cuda(cudaStreamCreateWithFlags(&p->s_copy, cudaStreamNonBlocking), "stream");
+    for (int i = 0; i < 5 && !rc; i++) rc = check_cuda(cudaEventCreate(&p->ev_stage[i]), "event");
     for (int b = 0; b < 2 && !rc; b++) {
         rc = check_cuda(cudaEventCreateWithFlags(&p->ev_copied[b], cudaEventDisableTiming), "event");
         rc = rc ? rc : check_cuda(cudaEventCreateWithFlags(&p->ev_consumed[b], cudaEventDisableTiming), "event");
@@ -479,6 +512,8 @@ int vgb_pipeline_destroy(vgb_pipeline *p)
                     p->d_vdif, p->d_hdr};
     for (void *b : bufs)
         if (b) cudaFree(b);
+    for (int i = 0; i < 5; i++)
+        if (p->ev_stage[i]) cudaEventDestroy(p->ev_stage[i]);
     for (int b = 0; b < 2; b++) {
         if (p->ev_copied[b]) cudaEventDestroy(p->ev_copied[b]);
         if (p->ev_consumed[b]) cudaEventDestroy(p->ev_consumed[b]);
@@ -622,5 +657,43 @@ int vgb_pipeline_device_products(vgb_pipeline *p, const float **S_, const void *
 }
 
 int vgb_pipeline_launch_count(vgb_pipeline *p) { return p ? p->launches : 0; }
+
+void *vgb_pipeline_stream(vgb_pipeline *p) { return p ? (void *)p->s_comp : nullptr; }
+
+int vgb_pipeline_set_host_outputs(vgb_pipeline *p, uint8_t *psrfits, float *offsets, float *scales, uint8_t *vdif)
+{
+    if (!p) return set_error(VGB_ERR_INVALID, "NULL pipeline");
+    if (vdif && !p->cfg.do_ipfb) return set_error(VGB_ERR_STATE, "pipeline was created without the IPFB");
+    p->h_psrfits = psrfits;
+    p->h_off = offsets;
+    p->h_scl = scales;
+    p->h_vdif = vdif;
+    return VGB_SUCCESS;
+}
+
+int vgb_pipeline_sync(vgb_pipeline *p)
+{
+    if (!p) return set_error(VGB_ERR_INVALID, "NULL pipeline");
+    int rc = check_cuda(cudaStreamSynchronize(p->s_copy), "sync copy stream");
+    rc = rc ? rc : check_cuda(cudaStreamSynchronize(p->s_comp), "sync compute stream");
+    return rc ? rc : vgb_check_device_status(p->s_comp, nullptr);
+}
+
+int vgb_pipeline_enable_timing(vgb_pipeline *p, int on)
+{
+    if (!p) return set_error(VGB_ERR_INVALID, "NULL pipeline");
+    p->timing = on != 0;
+    return VGB_SUCCESS;
+}
+
+int vgb_pipeline_stage_ms(vgb_pipeline *p, float *ms, int n)
+{
+    if (!p || !ms) return set_error(VGB_ERR_INVALID, "NULL argument");
+    if (!p->timing || p->second == 0) return set_error(VGB_ERR_STATE, "timing not enabled or nothing run");
+    int rc = check_cuda(cudaEventSynchronize(p->ev_stage[4]), "sync stage events");
+    for (int i = 0; i < n && i < 4 && !rc; i++)
+        rc = check_cuda(cudaEventElapsedTime(&ms[i], p->ev_stage[i], p->ev_stage[i + 1]), "stage time");
+    return rc;
+}
 
 } // extern "C"

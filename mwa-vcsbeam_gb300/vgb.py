@@ -99,6 +99,11 @@ _SIGS = {
     "vgb_pipeline_device_products": (I, [V, ctypes.POINTER(V), ctypes.POINTER(V), ctypes.POINTER(V),
                                          ctypes.POINTER(V), ctypes.POINTER(V)]),
     "vgb_pipeline_launch_count": (I, [V]),
+    "vgb_pipeline_stream": (V, [V]),
+    "vgb_pipeline_set_host_outputs": (I, [V, V, V, V, V]),
+    "vgb_pipeline_sync": (I, [V]),
+    "vgb_pipeline_enable_timing": (I, [V, I]),
+    "vgb_pipeline_stage_ms": (I, [V, ctypes.POINTER(Fl), I]),
 }
 
 
@@ -297,3 +302,24 @@ class Pipeline:
 
     def launch_count(self) -> int:
         return int(lib().vgb_pipeline_launch_count(self.h))
+
+    def stream(self):
+        """The pipeline's compute stream as a torch ExternalStream."""
+        import torch
+
+        return torch.cuda.ExternalStream(lib().vgb_pipeline_stream(self.h))
+
+    def set_host_outputs(self, psrfits=None, offsets=None, scales=None, vdif=None):
+        self._host_outputs = (psrfits, offsets, scales, vdif)  # keep them alive
+        check(lib().vgb_pipeline_set_host_outputs(self.h, ptr(psrfits), ptr(offsets), ptr(scales), ptr(vdif)))
+
+    def sync(self):
+        check(lib().vgb_pipeline_sync(self.h))
+
+    def enable_timing(self, on: bool = True):
+        check(lib().vgb_pipeline_enable_timing(self.h, int(on)))
+
+    def stage_ms(self):
+        arr = (Fl * 4)()
+        check(lib().vgb_pipeline_stage_ms(self.h, arr, 4))
+        return list(arr)
