@@ -39,9 +39,13 @@ NCC, NANT, NBLK, K, P = 24, 128, 20, 128, 12
 NI = 2 * NANT
 NSPEC = NBLK * 500
 SECOND_BYTES = NBLK * NI * 64000 * 2           # one coarse channel, one second
-PSRFITS_BYTES = NSPEC * 4 * NCC * K
-VDIF_BYTES = NCC * NSPEC * 544
-STAT_BYTES = 2 * NCC * 4 * K * 4
+
+
+def out_bytes(ncc):
+    """PSRFITS bytes, VDIF bytes and scale/offset bytes per data-second."""
+    return NSPEC * 4 * ncc * K, ncc * NSPEC * 544, 2 * ncc * 4 * K * 4
+
+
 WORKLOAD = ("full band: 24 coarse channels x 128 tiles x 2 pols, 8-bit MWAX voltages (sigma 16), "
             "fine PFB 12x128 -> 1 tied-array beam + incoherent, full Stokes 100 us -> 8-bit PSRFITS; "
             "inverse PFB -> 8-bit VDIF; FP32")
@@ -103,20 +107,20 @@ class ClockSampler:
 # --------------------------------------------------------------------------
 # synthetic workload on the device
 # --------------------------------------------------------------------------
-def make_voltages(torch, nsec: int, seed: int):
+def make_voltages(torch, nsec: int, ncc: int, seed: int):
     """[nsec][cc][block][input][sample][2] int8, Gaussian sigma 16 clipped."""
     g = torch.Generator(device="cuda")
     g.manual_seed(seed)
-    out = torch.empty((nsec, NCC, SECOND_BYTES), dtype=torch.int8, device="cuda")
+    out = torch.empty((nsec, ncc, SECOND_BYTES), dtype=torch.int8, device="cuda")
     for s in range(nsec):
-        for cc in range(NCC):
+        for cc in range(ncc):
             x = torch.randn(SECOND_BYTES, generator=g, device="cuda", dtype=torch.float32)
             out[s, cc] = x.mul_(16.0).round_().clamp_(-127, 127).to(torch.int8)
             del x
     return out
 
 
-def make_weights(torch, vgb, SY):
+def make_weights(torch, vgb, SY, ncc):
     """W [cc][tile][128][2][2] complex float = phi * J^-1 built on the device
     in FP64 (vgb_jones, vgb_phase, vgb_weights)."""
     D = SY.calibration_jones(NANT, K, seed=11)
@@ -132,10 +136,10 @@ def make_weights(torch, vgb, SY):
 
     J = torch.empty(NANT * K * 8, dtype=torch.float64, device="cuda")
     vgb.jones(d(D), d(B), 1, NANT, K, J)
-    W = torch.empty((NCC, NANT * K, 8), dtype=torch.float32, device="cuda")
+    W = torch.empty((ncc, NANT * K, 8), dtype=torch.float32, device="cuda")
     phi = torch.empty(NANT * K * 2, dtype=torch.float64, device="cuda")
     geo = [d(x) for x in (unit, east, north, height, cable)]
-    for cc in range(NCC):
+    for cc in range(ncc):
         freqs = d(SY.fine_chan_freqs_hz(SY.coarse_chan_start_hz(cc)))
         vgb.phase(*geo, freqs, 1, NANT, K, SY.MWA_ALTITUDE_METRES, phi)
         vgb.weights(J, phi, NANT * K, W[cc])
@@ -237,11 +241,12 @@ def gb300_arm(args, rank, local_rank, world):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    volt = make_voltages(torch, args.resident, seed=1234 + rank)
-    W = make_weights(torch, vgb, SY)
+    ncc = args.ncc
+    volt = make_voltages(torch, args.resident, ncc, seed=1234 + rank)
+    W = make_weights(torch, vgb, SY, ncc)
     h = SY.analysis_filter_int16()
     syn = SY.synthesis_filter(scale=SY.synthesis_scale(h)).astype(np.float32)
-    pipe = vgb.Pipeline(NCC, NANT, NBLK, nstokes=4, pfb_flags=0, do_ipfb=True, invw=1.0 / NI)
+    pipe = vgb.Pipeline(ncc, NANT, NBLK, nstokes=4, pfb_flags=0, do_ipfb=True, invw=1.0 / NI)
     pipe.set_filters(h, syn)
     pipe.set_weights(W, on_device=True)
     stream = pipe.stream()
@@ -268,35 +273,38 @@ def gb300_arm(args, rank, local_rank, world):
     clk = clocks.stop()
     pipe.enable_timing(False)
     elapsed_s = max_over_ranks(ev0.elapsed_time(ev1) / 1e3)
-    value = world * args.steps / elapsed_s
+    value = world * args.steps * ncc / NCC / elapsed_s
     stage /= args.steps
 
     # ---- end to end through the host API ------------------------------------
-    hin = torch.empty(NCC * SECOND_BYTES, dtype=torch.int8, pin_memory=True)
-    hin.copy_(volt[0].reshape(-1))
-    ps = torch.empty(PSRFITS_BYTES, dtype=torch.uint8, pin_memory=True)
-    vd = torch.empty(VDIF_BYTES, dtype=torch.uint8, pin_memory=True)
-    off = torch.empty(NCC * 4 * K, dtype=torch.float32, pin_memory=True)
-    scl = torch.empty(NCC * 4 * K, dtype=torch.float32, pin_memory=True)
-    pipe.set_host_outputs(ps, off, scl, vd)
-    del volt
-    for _ in range(min(args.warmup, 3)):
-        pipe.run_host(hin)
-    pipe.sync()
-    barrier()
-    t0 = time.perf_counter()
-    e2e_steps = max(1, min(args.steps, args.e2e_steps))
-    for _ in range(e2e_steps):
-        pipe.run_host(hin)
-    pipe.sync()
-    barrier()
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e = {"value": world * e2e_steps / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": NCC * SECOND_BYTES,
-           "d2h_bytes_per_step": PSRFITS_BYTES + VDIF_BYTES + STAT_BYTES,
-           "steps": e2e_steps, "ms_per_step": 1e3 * e2e_s / e2e_steps,
-           "path": "vgb_pipeline_run_host from pinned host memory, products back to pinned host buffers; "
-                   "next second's copy overlaps this second's compute"}
+    psr_b, vdif_b, stat_b = out_bytes(ncc)
+    e2e = None
+    if args.e2e_steps > 0:
+        hin = torch.empty(ncc * SECOND_BYTES, dtype=torch.int8, pin_memory=True)
+        hin.copy_(volt[0].reshape(-1))
+        ps = torch.empty(psr_b, dtype=torch.uint8, pin_memory=True)
+        vd = torch.empty(vdif_b, dtype=torch.uint8, pin_memory=True)
+        off = torch.empty(ncc * 4 * K, dtype=torch.float32, pin_memory=True)
+        scl = torch.empty(ncc * 4 * K, dtype=torch.float32, pin_memory=True)
+        pipe.set_host_outputs(ps, off, scl, vd)
+        del volt
+        for _ in range(min(args.warmup, 3)):
+            pipe.run_host(hin)
+        pipe.sync()
+        barrier()
+        t0 = time.perf_counter()
+        e2e_steps = max(1, min(args.steps, args.e2e_steps))
+        for _ in range(e2e_steps):
+            pipe.run_host(hin)
+        pipe.sync()
+        barrier()
+        e2e_s = max_over_ranks(time.perf_counter() - t0)
+        e2e = {"value": world * e2e_steps * ncc / NCC / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": ncc * SECOND_BYTES,
+               "d2h_bytes_per_step": psr_b + vdif_b + stat_b,
+               "steps": e2e_steps, "ms_per_step": 1e3 * e2e_s / e2e_steps,
+               "path": "vgb_pipeline_run_host from pinned host memory, products back to pinned host buffers; "
+                       "next second's copy overlaps this second's compute"}
     pipe.close()
 
     # ---- roofline of the dominant kernel (fused PFB + beamformer) -----------
@@ -306,7 +314,7 @@ def gb300_arm(args, rank, local_rank, world):
     except Exception:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    alg_bytes = NCC * SECOND_BYTES          # the voltages it must read, per launch
+    alg_bytes = ncc * SECOND_BYTES          # the voltages it must read, per launch
     achieved = alg_bytes / (stage[0] / 1e3) / 1e9
     roofline = {"kernel": "beam_kernel (fused PFB + tied-array/incoherent beam + Stokes)", "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -318,7 +326,8 @@ def gb300_arm(args, rank, local_rank, world):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "ncc": NCC, "ntiles": NANT, "nbeams": 1, "nstokes": 4,
+            "config": {"workload": WORKLOAD if ncc == NCC else WORKLOAD.replace("24 coarse", f"{ncc} coarse"),
+                       "ncc": ncc, "ntiles": NANT, "nbeams": 1, "nstokes": 4,
                        "step": "one data-second (24 coarse channels x 1 s)",
                        "l2": "inputs larger than L2: each step reads a different 15.7 GB second",
                        "resident_seconds": args.resident},
@@ -340,6 +349,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--resident", type=int, default=2, help="distinct seconds kept in HBM")
+    ap.add_argument("--ncc", type=int, default=NCC, help="coarse channels (24 = the full band; fewer for "
+                    "profiling captures; value stays in full-band data-seconds)")
     ap.add_argument("--e2e-steps", type=int, default=40)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
