@@ -198,6 +198,33 @@ int vgb_ipfb(const void *e, long long e_job_stride, const void *hist, long long 
              const float *coeffs, int ntaps, int nchan, int nsamples, int njobs, float *out_f, uint8_t *vdif,
              const uint32_t *hdr, int frame_offset, void *stream);
 
+/*
+ * MWAX voltages to 8-bit PSRFITS bytes without allocating any memory. This
+ * entry point has no counterpart in the reference. It is for callers that
+ * cannot allocate device memory while they run, such as a real-time
+ * observing pipeline that reserves all GPU memory at start-up and must not
+ * fail or stall on an allocation mid-observation. It runs the fused PFB +
+ * beamformer (vgb_beamform_mwax) and then the per-channel renormalise
+ * (vgb_renormalise). The full-resolution Stokes passed between them live in a
+ * fixed 24 MiB array inside the library, which every GPU that loads the
+ * library holds until the process exits. The limit is
+ * ncc x nspectra x nstokes x 128 float values <= 6,291,456, i.e. one
+ * full-Stokes second of one coarse channel; larger requests are rejected
+ * with VGB_ERR_INVALID.
+ *   out      [ncc][nspectra][nstokes][128] bytes (C_IDX per channel)
+ *   offsets, scales  [ncc][nstokes][128]
+ * The first call on each device looks up the array's device address (with
+ * that device current); make that first call before any stream capture.
+ * All calls share the one array, which keeps the last call's contents.
+ * Nothing in it needs to start at zero, because each call writes every
+ * value it reads. Calls that overlap on the GPU (e.g. on different streams)
+ * race on it.
+ */
+int vgb_beamform_mwax_psrfits_noalloc(const vgb_voltages *v, int ncc, int nspectra, const int32_t *filter,
+                                      int ntaps, int nchan, unsigned pfb_flags, const void *W, int nant,
+                                      float invw, int nstokes, uint8_t *out, float *offsets, float *scales,
+                                      void *stream);
+
 /* ---- streaming pipeline: one second of all coarse channels per step ---- */
 typedef struct vgb_pipeline vgb_pipeline;
 

@@ -87,6 +87,8 @@ _SIGS = {
     "vgb_incoh_beam": (I, [V, LL, I, V, V]),
     "vgb_renormalise": (I, [V, I, I, I, I, I, V, LL, LL, LL, LL, V, V, V]),
     "vgb_ipfb": (I, [V, LL, V, LL, V, I, I, I, I, V, V, V, I, V]),
+    "vgb_beamform_mwax_psrfits_noalloc": (I, [ctypes.POINTER(Voltages), I, I, V, I, I, U, V, I, Fl, I, V, V, V,
+                                              V]),
     "vgb_pipeline_create": (I, [ctypes.POINTER(PipelineConfig), ctypes.POINTER(V)]),
     "vgb_pipeline_destroy": (I, [V]),
     "vgb_pipeline_set_filters": (I, [V, V, V]),
@@ -171,6 +173,15 @@ def beamform_mwax(v: Voltages, ncc, nspectra, filt, flags, W, nant, invw, nstoke
                   stream=None):
     check(lib().vgb_beamform_mwax(ctypes.byref(v), ncc, nspectra, ptr(filt), NTAPS, NCHAN, flags, ptr(W), nant,
                                   float(invw), nstokes, ptr(S), ptr(e), ptr(incoh), stream_ptr(stream)))
+
+
+def beamform_mwax_psrfits_noalloc(v: Voltages, ncc, nspectra, filt, flags, W, nant, invw, nstokes, out, offsets,
+                                  scales, stream=None):
+    """Voltages to PSRFITS bytes with no allocation (a fixed 24 MiB array in
+    the library holds the intermediate Stokes; see the C header)."""
+    check(lib().vgb_beamform_mwax_psrfits_noalloc(ctypes.byref(v), ncc, nspectra, ptr(filt), NTAPS, NCHAN, flags,
+                                                  ptr(W), nant, float(invw), nstokes, ptr(out), ptr(offsets),
+                                                  ptr(scales), stream_ptr(stream)))
 
 
 def fpfb(v: Voltages, ncc, nspectra, filt, i_idx, flags, out, stream=None):
