@@ -1,17 +1,18 @@
 // Fused forward fine PFB and tied-array / incoherent beamformer for MWAX
 // voltages, GB300 (sm_103a).
 //
-// One CTA owns a tile of T = 16 consecutive fine spectra of one coarse
-// channel and walks the RF inputs four at a time (two tiles x two pols). Per
-// step:
-//   1. the TMA unit copies the 27 voltage frames (T + 11) each input needs
-//      into shared memory (1-D bulk copies, double-buffered with mbarriers:
-//      the next step's frames land while this step computes);
-//   2. weighted overlap-add, exactly (pfb.cpp:121-179), one thread per
-//      (input, sample-in-frame) with its 12 filter taps in registers;
+// One CTA (256 threads, ~93 KB of shared memory, two CTAs per SM) owns a
+// tile of T = 8 consecutive fine spectra of one coarse channel and walks the
+// RF inputs four at a time (two tiles x two pols). Per step:
+//   1. the TMA unit copies the 19 voltage frames (T + 11) each input needs,
+//      and the two tiles' weight rows, into shared memory (1-D bulk copies,
+//      double-buffered with mbarriers: step i+1 lands while step i computes);
+//   2. weighted overlap-add, exactly (pfb.cpp:121-179): one thread per
+//      (input, pair of adjacent samples), the pair's 12 taps in registers,
+//      packed FP32x2 FMAs (or int32 when FP32 would not be exact);
 //   3. the FPGA rounding (pfb.cpp:202-242) or the 2^-14 scaling
 //      (pfb.cpp:256-268);
-//   4. a 128-point FFT (16 x 8, eight threads per transform);
+//   4. a 128-point FFT (16 x 8, eight threads per transform, in place);
 //   5. fftshift, 1/K, the (im, re) ordering of pfb.cpp:328-339 and, for the
 //      4-bit mode, the round-and-clip of vcsbeam.h.in:453-457;
 //   6. beamformer back end: ex/ey = (phi J^-1)[a][c] v (form_beam.cpp:174-177,
@@ -23,18 +24,16 @@
 
 namespace vgb {
 
-constexpr int kT = 16;                     // spectra per CTA
-constexpr int kG = 4;                      // inputs per step
-constexpr int kThreads = 512;              // = kG * kK
+constexpr int kT = 8;                      // spectra per CTA
+constexpr int kG = 4;                      // inputs per step (two tiles)
+constexpr int kThreads = 256;
 constexpr int kWin = kT + kP - 1;          // frames per input per step
 constexpr int kFrameBytes = kK * 2;        // 256
-constexpr int kStageBytes = kG * kWin * kFrameBytes;
-constexpr int kXRow = kK + 8;              // bufX row (float2), padded
 
 struct FrontSmem {
-    char2 stage[2][kG][kWin][kK];          // TMA destinations
-    float2 bufB[kG * kT][kFftRow];         // WOLA output / FFT work rows
-    float2 bufX[kG * kT][kXRow];           // fine-channel voltages (shifted order)
+    char2 stage[2][kG][kWin][kK];          // TMA destinations: frames
+    float4 wst[2][2][kK][2];               // TMA destinations: weights of the step's two tiles
+    float2 buf[kG * kT][kFftRow];          // WOLA output -> FFT (in place) -> voltages
     float2 tw[128];                        // W128 twiddles, [k1][j]
     uint64_t bar[2];
 };
@@ -73,23 +72,30 @@ __device__ __forceinline__ uint32_t issue_frames(const VoltView &vv, int cc, int
     return bytes;
 }
 
-// Producer: one thread queues the frames of step `it` into stage `s`.
-__device__ __forceinline__ void produce(FrontSmem &sm, const VoltView &vv, int cc, int it, int m0,
-                                       int nspectra, unsigned *status)
+// Producer: one thread queues step `it`'s frames (and, when W is given, the
+// weight rows of its two tiles) into stage it & 1.
+__device__ __forceinline__ void produce(FrontSmem &sm, const VoltView &vv, int cc, int it, int m0, int nspectra,
+                                       const float4 *Wcc, int nant, unsigned *status)
 {
     const int s = it & 1;
     const int w_end = min(m0 + kWin, nspectra + kP - 1);
-    // Count first so expect_tx is armed before any copy can complete.
     uint32_t total = 0;
-    for (int li = 0; li < kG; li++) {
-        const int i = it * kG + li;
-        if (i < vv.ninputs) total += (w_end - m0) * kFrameBytes;
+    for (int li = 0; li < kG; li++)
+        if (it * kG + li < vv.ninputs) total += (w_end - m0) * kFrameBytes;
+    int nw = 0;
+    if (Wcc) {
+        nw = min(2, nant - 2 * it);
+        total += nw * kK * 32;
     }
     mbar_arrive_expect_tx(&sm.bar[s], total);
     uint32_t issued = 0;
     for (int li = 0; li < kG; li++) {
         const int i = it * kG + li;
         if (i < vv.ninputs) issued += issue_frames(vv, cc, i, m0, w_end, sm.stage[s][li][0], &sm.bar[s], status);
+    }
+    if (nw > 0) {
+        bulk_g2s(sm.wst[s][0][0], Wcc + (long long)(2 * it) * kK * 2, nw * kK * 32, &sm.bar[s]);
+        issued += nw * kK * 32;
     }
     if (issued != total) {
         // Some frames were outside the buffers: complete the remaining
@@ -101,91 +107,109 @@ __device__ __forceinline__ void produce(FrontSmem &sm, const VoltView &vv, int c
     }
 }
 
-// char2 (as a 16-bit word) -> two exact floats, via the 2^23 magic number.
-__device__ __forceinline__ void c2_to_f(uint32_t v, float &re, float &im)
+// Four int8 values (two char2) -> packed floats (re0, re1), (im0, im1), exact,
+// via the 2^23 magic number: bytes are offset to unsigned, placed under the
+// exponent of 2^23 and the 2^23 + 128 bias subtracted.
+__device__ __forceinline__ void c4_to_f(uint32_t w, float2 &re, float2 &im)
 {
-    const uint32_t u = v ^ 0x8080u; // offset binary: byte + 128
-    re = __uint_as_float(0x4B000000u | (u & 0xFFu)) - 8388736.0f;
-    im = __uint_as_float(0x4B000000u | ((u >> 8) & 0xFFu)) - 8388736.0f;
+    const uint32_t u = w ^ 0x80808080u;
+    const float2 bias = make_float2(-8388736.0f, -8388736.0f);
+    re = padd(make_float2(__uint_as_float(__byte_perm(u, 0x4B000000u, 0x7540)),
+                          __uint_as_float(__byte_perm(u, 0x4B000000u, 0x7542))),
+              bias);
+    im = padd(make_float2(__uint_as_float(__byte_perm(u, 0x4B000000u, 0x7541)),
+                          __uint_as_float(__byte_perm(u, 0x4B000000u, 0x7543))),
+              bias);
 }
-__device__ __forceinline__ void c2_to_i(uint32_t v, int &re, int &im)
+
+__device__ __forceinline__ void c4_to_i(uint32_t w, int (&re)[2], int (&im)[2])
 {
-    re = (int)(signed char)(v & 0xFFu);
-    im = (int)(signed char)((v >> 8) & 0xFFu);
+    re[0] = (int)(signed char)(w & 0xFFu);
+    im[0] = (int)(signed char)((w >> 8) & 0xFFu);
+    re[1] = (int)(signed char)((w >> 16) & 0xFFu);
+    im[1] = (int)(signed char)(w >> 24);
+}
+
+// FPGA rounding (pfb.cpp:225-231) of an integer-valued float |X| < 2^24:
+// (X + 0x2000) >> 14 for X > 0, X >> 14 otherwise, both exact in FP32.
+__device__ __forceinline__ float fpga_round(float X)
+{
+    return floorf(fmaf(X, 1.0f / 16384.0f, X > 0.f ? 0.5f : 0.f));
 }
 
 // ---------------------------------------------------------------------------
-// Steps 2-3: weighted overlap-add for thread (li, n) into bufB rows.
-// kInt32: accumulate in int32 (any filter); else FP32, exact when every
-// partial sum stays below 2^24 (the host checks the filter).
+// Steps 2-3: weighted overlap-add for thread (li, n0..n0+1) into buf rows.
 // ---------------------------------------------------------------------------
 template <bool kInt32, bool kFpga>
-__device__ __forceinline__ void wola_step(FrontSmem &sm, int s, int li, int n, const int (&hc)[kP])
+__device__ __forceinline__ void wola_step(FrontSmem &sm, int s, int li, int n0, const int (&hc)[2][kP])
 {
-    const uint16_t *x = reinterpret_cast<const uint16_t *>(sm.stage[s][li][0]) + n;
+    const uint32_t *x = reinterpret_cast<const uint32_t *>(sm.stage[s][li][0] + n0);
     if (kInt32) {
-        int ar[kT], ai[kT];
+        int ar[kT][2], ai[kT][2];
 #pragma unroll
-        for (int m = 0; m < kT; m++) ar[m] = ai[m] = 0;
+        for (int m = 0; m < kT; m++) ar[m][0] = ar[m][1] = ai[m][0] = ai[m][1] = 0;
 #pragma unroll
         for (int w = 0; w < kWin; w++) {
-            int xr, xi;
-            c2_to_i(x[w * kK], xr, xi);
+            int xr[2], xi[2];
+            c4_to_i(x[w * (kK / 2)], xr, xi);
 #pragma unroll
             for (int p = 0; p < kP; p++) {
                 const int m = w - p;
                 if (m >= 0 && m < kT) {
-                    ar[m] += hc[p] * xr;
-                    ai[m] += hc[p] * xi;
+#pragma unroll
+                    for (int q = 0; q < 2; q++) {
+                        ar[m][q] += hc[q][p] * xr[q];
+                        ai[m][q] += hc[q][p] * xi[q];
+                    }
                 }
             }
         }
 #pragma unroll
         for (int m = 0; m < kT; m++) {
-            float2 b;
+            float4 b;
             if (kFpga) {
-                int X = ar[m], Y = ai[m];
-                if (X > 0) X += 0x2000;
-                if (Y > 0) Y += 0x2000;
-                b = make_float2((float)(X >> 14), (float)(Y >> 14));
+                int v[4] = {ar[m][0], ai[m][0], ar[m][1], ai[m][1]};
+#pragma unroll
+                for (int q = 0; q < 4; q++) v[q] = (v[q] > 0 ? v[q] + 0x2000 : v[q]) >> 14;
+                b = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
             } else {
-                b = make_float2((float)ar[m] * (1.0f / 16384.0f), (float)ai[m] * (1.0f / 16384.0f));
+                const float sc = 1.0f / 16384.0f;
+                b = make_float4((float)ar[m][0] * sc, (float)ai[m][0] * sc, (float)ar[m][1] * sc,
+                                (float)ai[m][1] * sc);
             }
-            sm.bufB[li * kT + m][n] = b;
+            *reinterpret_cast<float4 *>(&sm.buf[li * kT + m][n0]) = b;
         }
     } else {
-        float hf[kP];
+        float2 h2[kP];
 #pragma unroll
-        for (int p = 0; p < kP; p++) hf[p] = (float)hc[p];
-        float ar[kT], ai[kT];
+        for (int p = 0; p < kP; p++) h2[p] = make_float2((float)hc[0][p], (float)hc[1][p]);
+        float2 ar[kT], ai[kT];
 #pragma unroll
-        for (int m = 0; m < kT; m++) ar[m] = ai[m] = 0.f;
+        for (int m = 0; m < kT; m++) ar[m] = ai[m] = make_float2(0.f, 0.f);
 #pragma unroll
         for (int w = 0; w < kWin; w++) {
-            float xr, xi;
-            c2_to_f(x[w * kK], xr, xi);
+            float2 xr, xi;
+            c4_to_f(x[w * (kK / 2)], xr, xi);
 #pragma unroll
             for (int p = 0; p < kP; p++) {
                 const int m = w - p;
                 if (m >= 0 && m < kT) {
-                    ar[m] = fmaf(hf[p], xr, ar[m]);
-                    ai[m] = fmaf(hf[p], xi, ai[m]);
+                    ar[m] = __ffma2_rn(h2[p], xr, ar[m]);
+                    ai[m] = __ffma2_rn(h2[p], xi, ai[m]);
                 }
             }
         }
 #pragma unroll
         for (int m = 0; m < kT; m++) {
-            float2 b;
+            float4 b;
             if (kFpga) {
-                // (X + 0x2000) >> 14 for X > 0, X >> 14 otherwise; exact in
-                // FP32 because |X| < 2^24.
-                const float X = ar[m] * (1.0f / 16384.0f), Y = ai[m] * (1.0f / 16384.0f);
-                b = make_float2(ar[m] > 0.f ? floorf(X + 0.5f) : floorf(X),
-                                ai[m] > 0.f ? floorf(Y + 0.5f) : floorf(Y));
+                b = make_float4(fpga_round(ar[m].x), fpga_round(ai[m].x), fpga_round(ar[m].y), fpga_round(ai[m].y));
             } else {
-                b = make_float2(ar[m] * (1.0f / 16384.0f), ai[m] * (1.0f / 16384.0f));
+                const float2 sc = make_float2(1.0f / 16384.0f, 1.0f / 16384.0f);
+                const float2 r = __fmul2_rn(ar[m], sc), i = __fmul2_rn(ai[m], sc);
+                b = make_float4(r.x, i.x, r.y, i.y);
             }
-            sm.bufB[li * kT + m][n] = b;
+            *reinterpret_cast<float4 *>(&sm.buf[li * kT + m][n0]) = b;
         }
     }
 }
@@ -197,17 +221,18 @@ __device__ __forceinline__ float demote4(float x)
     return fminf(fmaxf(r, -8.0f), 7.0f);
 }
 
-// Steps 4-5: FFT of row (li, m) by the 8 threads of a group; writes the
-// shifted, scaled, (im, re)-ordered voltages into bufX.
+// Steps 4-5: FFT of row g = (li, m) by the 8 threads of a group, in place;
+// the row then holds the shifted, scaled, (im, re)-ordered voltages at k'.
 template <bool kDemote>
 __device__ __forceinline__ void fft_step(FrontSmem &sm, int tid)
 {
     const int g = tid >> 3, j = tid & 7;
-    float2 *row = sm.bufB[g];
+    float2 *row = sm.buf[g];
     fft128_pass1<-1>(row, sm.tw, j);
     __syncwarp();
     float2 out[2][8];
     fft128_pass2<-1>(row, j, out);
+    __syncwarp();
 #pragma unroll
     for (int h = 0; h < 2; h++)
 #pragma unroll
@@ -220,7 +245,7 @@ __device__ __forceinline__ void fft_step(FrontSmem &sm, int tid)
                 vr = demote4(vr);
                 vi = demote4(vi);
             }
-            sm.bufX[g][kp] = make_float2(vr, vi);
+            row[kp] = make_float2(vr, vi);
         }
 }
 
@@ -239,14 +264,18 @@ __device__ __forceinline__ void init_front(FrontSmem &sm, int tid)
     }
 }
 
-__device__ __forceinline__ void load_taps(const int *filter, int n, int (&hc)[kP])
+// Taps of samples n0, n0+1: h[K P - K p - n - 1] (pfb.cpp:159).
+__device__ __forceinline__ void load_taps(const int *filter, int n0, int (&hc)[2][kP])
 {
 #pragma unroll
-    for (int p = 0; p < kP; p++) hc[p] = __ldg(filter + kK * kP - kK * p - n - 1);
+    for (int q = 0; q < 2; q++)
+#pragma unroll
+        for (int p = 0; p < kP; p++) hc[q][p] = __ldg(filter + kK * kP - kK * p - (n0 + q) - 1);
 }
 
-// Wait for step `it`'s frames; every thread learns whether any thread timed
-// out, so the CTA leaves together.
+// Wait for step `it`'s data; every thread learns whether any thread timed
+// out, so the CTA leaves together. The barrier also orders the previous
+// step's reads of the buffers before this step's writes.
 __device__ __forceinline__ bool wait_frames(FrontSmem &sm, int it, unsigned *status)
 {
     const bool ok = mbar_wait_bounded(&sm.bar[it & 1], (it >> 1) & 1, 1u << 22);
@@ -256,21 +285,17 @@ __device__ __forceinline__ bool wait_frames(FrontSmem &sm, int it, unsigned *sta
 }
 
 // Before leaving early, give copies in flight a bounded chance to land.
-__device__ __forceinline__ void drain(FrontSmem &sm, int it, int nsteps)
+__device__ __forceinline__ void drain(FrontSmem &sm, int it)
 {
-    if (threadIdx.x == 0) {
-        mbar_wait_bounded(&sm.bar[it & 1], (it >> 1) & 1, 1u << 20);
-        if (it + 1 < nsteps) mbar_wait_bounded(&sm.bar[(it + 1) & 1], ((it + 1) >> 1) & 1, 1u << 20);
-    }
+    if (threadIdx.x == 0) mbar_wait_bounded(&sm.bar[it & 1], (it >> 1) & 1, 1u << 20);
     __syncthreads();
 }
 
 // ---------------------------------------------------------------------------
 // Beamformer kernel.
 // ---------------------------------------------------------------------------
-
 template <bool kInt32, bool kFpga, bool kDemote>
-__global__ void __launch_bounds__(kThreads, 1) beam_kernel(const BeamArgs a)
+__global__ void __launch_bounds__(kThreads, 2) beam_kernel(const BeamArgs a)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     FrontSmem &sm = *reinterpret_cast<FrontSmem *>(smem_raw);
@@ -278,30 +303,31 @@ __global__ void __launch_bounds__(kThreads, 1) beam_kernel(const BeamArgs a)
     const int cc = blockIdx.y;
     const int m0 = blockIdx.x * kT;
     const int nsteps = (a.vv.ninputs + kG - 1) / kG;
+    const float4 *Wcc = a.W + cc * a.W_cc;
 
     init_front(sm, tid);
-    int hc[kP];
-    const int n = tid & (kK - 1), li = tid >> 7;
-    load_taps(a.filter, n, hc);
+    int hc[2][kP];
+    const int li = tid >> 6, n0 = 2 * (tid & 63);
+    load_taps(a.filter, n0, hc);
     __syncthreads();
-    if (tid == 0) produce(sm, a.vv, cc, 0, m0, a.nspectra, a.status);
+    if (tid == 0) produce(sm, a.vv, cc, 0, m0, a.nspectra, Wcc, a.nant, a.status);
 
-    // beam accumulators for (k', m = mq + 4 mi)
-    const int kp = tid & (kK - 1), mq = tid >> 7;
+    // beam accumulators for (k', m = mh + 2 mi)
+    const int kp = tid & (kK - 1), mh = tid >> 7;
     float acc[4][9];
 #pragma unroll
     for (int mi = 0; mi < 4; mi++)
 #pragma unroll
         for (int q = 0; q < 9; q++) acc[mi][q] = 0.f;
 
-    const float4 *Wcc = a.W + cc * a.W_cc;
     for (int it = 0; it < nsteps; it++) {
-        if (tid == 0 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, a.status);
         if (!wait_frames(sm, it, a.status)) {
-            drain(sm, it, nsteps);
+            drain(sm, it);
             return;
         }
-        wola_step<kInt32, kFpga>(sm, it & 1, li, n, hc);
+        // everyone has finished step it-1, so its buffers may be refilled
+        if (tid == 0 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, Wcc, a.nant, a.status);
+        wola_step<kInt32, kFpga>(sm, it & 1, li, n0, hc);
         __syncthreads();
         fft_step<kDemote>(sm, tid);
         __syncthreads();
@@ -309,13 +335,13 @@ __global__ void __launch_bounds__(kThreads, 1) beam_kernel(const BeamArgs a)
         for (int aa = 0; aa < 2; aa++) {
             const int ant = it * 2 + aa;
             if (ant >= a.nant) break;
-            const float4 wa = __ldg(Wcc + ((long long)ant * kK + kp) * 2);
-            const float4 wb = __ldg(Wcc + ((long long)ant * kK + kp) * 2 + 1);
+            const float4 wa = sm.wst[it & 1][aa][kp][0];
+            const float4 wb = sm.wst[it & 1][aa][kp][1];
 #pragma unroll
             for (int mi = 0; mi < 4; mi++) {
-                const int m = mq + 4 * mi;
-                const float2 vq = sm.bufX[(2 * aa) * kT + m][kp];
-                const float2 vp = sm.bufX[(2 * aa + 1) * kT + m][kp];
+                const int m = mh + 2 * mi;
+                const float2 vq = sm.buf[(2 * aa) * kT + m][kp];
+                const float2 vp = sm.buf[(2 * aa + 1) * kT + m][kp];
                 const float exr = wa.x * vq.x - wa.y * vq.y + wa.z * vp.x - wa.w * vp.y;
                 const float exi = wa.x * vq.y + wa.y * vq.x + wa.z * vp.y + wa.w * vp.x;
                 const float eyr = wb.x * vq.x - wb.y * vq.y + wb.z * vp.x - wb.w * vp.y;
@@ -337,7 +363,7 @@ __global__ void __launch_bounds__(kThreads, 1) beam_kernel(const BeamArgs a)
     // form_beam.cpp:322-338
 #pragma unroll
     for (int mi = 0; mi < 4; mi++) {
-        const int m = m0 + mq + 4 * mi;
+        const int m = m0 + mh + 2 * mi;
         if (m >= a.nspectra) continue;
         const float *c = acc[mi];
         const float bnXX = c[0] * c[0] + c[1] * c[1] - c[4];
@@ -359,9 +385,8 @@ __global__ void __launch_bounds__(kThreads, 1) beam_kernel(const BeamArgs a)
 // ---------------------------------------------------------------------------
 // PFB-only kernel: packed legacy-order output (pfb.cpp:297-343).
 // ---------------------------------------------------------------------------
-
 template <bool kInt32, bool kFpga, bool kDemote>
-__global__ void __launch_bounds__(kThreads, 1) pack_kernel(const PackArgs a)
+__global__ void __launch_bounds__(kThreads, 2) pack_kernel(const PackArgs a)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     FrontSmem &sm = *reinterpret_cast<FrontSmem *>(smem_raw);
@@ -372,38 +397,37 @@ __global__ void __launch_bounds__(kThreads, 1) pack_kernel(const PackArgs a)
     const int nsteps = (I + kG - 1) / kG;
 
     init_front(sm, tid);
-    int hc[kP];
-    const int n = tid & (kK - 1), li = tid >> 7;
-    load_taps(a.filter, n, hc);
+    int hc[2][kP];
+    const int li = tid >> 6, n0 = 2 * (tid & 63);
+    load_taps(a.filter, n0, hc);
     __syncthreads();
-    if (tid == 0) produce(sm, a.vv, cc, 0, m0, a.nspectra, a.status);
+    if (tid == 0) produce(sm, a.vv, cc, 0, m0, a.nspectra, nullptr, 0, a.status);
 
     const bool int4 = (a.flags & VGB_PFB_COMPLEX_INT4) != 0;
     const bool imag_first = (a.flags & VGB_PFB_IMAG_PART_FIRST) != 0;
+    const int kp = tid & (kK - 1), mh = tid >> 7;
     for (int it = 0; it < nsteps; it++) {
-        if (tid == 0 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, a.status);
         if (!wait_frames(sm, it, a.status)) {
-            drain(sm, it, nsteps);
+            drain(sm, it);
             return;
         }
-        wola_step<kInt32, kFpga>(sm, it & 1, li, n, hc);
+        if (tid == 0 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, nullptr, 0, a.status);
+        wola_step<kInt32, kFpga>(sm, it & 1, li, n0, hc);
         __syncthreads();
         fft_step<kDemote>(sm, tid);
         __syncthreads();
-        // thread -> (k', spectrum row) pairs; one input per pass
 #pragma unroll
         for (int r = 0; r < kG; r++) {
             const int i = it * kG + r;
             if (i >= I) break;
             const int io = __ldg(a.i_idx + i);
-            const int kp = tid & (kK - 1);
 #pragma unroll
-            for (int mi = 0; mi < kT / 4; mi++) {
-                const int ml = (tid >> 7) + 4 * mi;
+            for (int mi = 0; mi < kT / 2; mi++) {
+                const int ml = mh + 2 * mi;
                 const int m = m0 + ml;
                 if (m >= a.nspectra) continue;
-                // bufX holds (im, re)/K: the reference's default output order
-                const float2 v = sm.bufX[r * kT + ml][kp];
+                // buf holds (im, re)/K: the reference's default output order
+                const float2 v = sm.buf[r * kT + ml][kp];
                 const float hi = imag_first ? v.y : v.x; // first (high / .x) component
                 const float lo = imag_first ? v.x : v.y;
                 const long long o = cc * a.out_cc + ((long long)m * kK + kp) * I + io;
@@ -479,10 +503,6 @@ int launch_pack(const PackArgs &a, int ncc, bool int32_wola, bool fpga, bool dem
     dim3 grid((a.nspectra + kT - 1) / kT, ncc);
     return dispatch<PackSel>(a, grid, int32_wola, fpga, demote, st);
 }
-
-} // namespace vgb
-
-namespace vgb {
 
 // Gather the last P frames of a second into the compact history layout
 // [cc][input][P][K] char2 that the next second reads (the reference keeps a

@@ -135,33 +135,43 @@ template <int SIGN> __device__ __forceinline__ float2 mul_i(float2 a)
     return SIGN > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
-// In-register radix-2 DFT of length 4 with exponent sign SIGN.
+// Packed FP32x2 arithmetic (sm_100+): one instruction updates both halves of
+// a complex value. Rounding is that of the scalar operations (RN per lane;
+// a - b is an FMA with -1, exact before its single rounding).
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
+// In-register DFT of length 4 with exponent sign SIGN (packed butterflies;
+// the +-i rotation is folded into scalar adds).
 template <int SIGN> __device__ __forceinline__ void dft4(float2 &a0, float2 &a1, float2 &a2, float2 &a3)
 {
-    float2 t0 = cadd(a0, a2), t1 = csub(a0, a2);
-    float2 t2 = cadd(a1, a3), t3 = mul_i<SIGN>(csub(a1, a3));
-    a0 = cadd(t0, t2);
-    a2 = csub(t0, t2);
-    a1 = cadd(t1, t3);
-    a3 = csub(t1, t3);
+    const float2 t0 = padd(a0, a2), t1 = psub(a0, a2);
+    const float2 t2 = padd(a1, a3), d = psub(a1, a3);
+    a0 = padd(t0, t2);
+    a2 = psub(t0, t2);
+    if (SIGN > 0) {
+        a1 = make_float2(t1.x - d.y, t1.y + d.x);
+        a3 = make_float2(t1.x + d.y, t1.y - d.x);
+    } else {
+        a1 = make_float2(t1.x + d.y, t1.y - d.x);
+        a3 = make_float2(t1.x - d.y, t1.y + d.x);
+    }
 }
 
 // Length-8 DFT in registers, natural order in and out.
 template <int SIGN> __device__ __forceinline__ void dft8(float2 *x)
 {
     const float r = 0.70710678118654752440f;
-    // stage 1: 4 butterflies of distance 4
     float2 a[8];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-        a[i] = cadd(x[i], x[i + 4]);
-        a[i + 4] = csub(x[i], x[i + 4]);
+        a[i] = padd(x[i], x[i + 4]);
+        a[i + 4] = psub(x[i], x[i + 4]);
     }
     // twiddles W8^{SIGN*i} on the odd half: i = 1, 2, 3
     a[5] = make_float2(r * (a[5].x - SIGN * a[5].y), r * (a[5].y + SIGN * a[5].x));
     a[6] = mul_i<SIGN>(a[6]);
     a[7] = make_float2(r * (-a[7].x - SIGN * a[7].y), r * (-a[7].y + SIGN * a[7].x));
-    // two length-4 DFTs: evens -> X[0,2,4,6], odds -> X[1,3,5,7]
     dft4<SIGN>(a[0], a[1], a[2], a[3]);
     dft4<SIGN>(a[4], a[5], a[6], a[7]);
     x[0] = a[0];
@@ -206,7 +216,7 @@ template <int SIGN> __device__ __forceinline__ void dft16(float2 *x)
             case 9: c = -c1; s = -s1; break;
             default: c = 1.f; s = 0.f; break;
             }
-            y[n2 * 4 + k1] = cmul_tw<SIGN>(y[n2 * 4 + k1], c, s);
+            y[n2 * 4 + k1] = (e == 4) ? mul_i<SIGN>(y[n2 * 4 + k1]) : cmul_tw<SIGN>(y[n2 * 4 + k1], c, s);
         }
     }
 #pragma unroll
