@@ -218,28 +218,17 @@ def gb300_arm(args, rank, local_rank, world):
     import synthetic as SY
     import vgb
 
-    torch.cuda.set_device(local_rank)
-    if world > 1:
-        import torch.distributed as dist
+    from sharding import RankContext
 
-        dist.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+    ctx = RankContext()
     vgb.lib()
 
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
+        ctx.barrier()
         torch.cuda.synchronize()
 
-    def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        import torch.distributed as dist
-
-        t = torch.tensor([x], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    max_over_ranks = ctx.max
 
     ncc = args.ncc
     volt = make_voltages(torch, args.resident, ncc, seed=1234 + rank)
@@ -336,10 +325,7 @@ def gb300_arm(args, rank, local_rank, world):
         line["cpu_baseline"] = cpu_baseline_line(args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.destroy_process_group()
+    ctx.close()
 
 
 def main():
