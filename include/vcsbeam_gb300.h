@@ -225,6 +225,15 @@ int vgb_beamform_mwax_psrfits_noalloc(const vgb_voltages *v, int ncc, int nspect
                                       float invw, int nstokes, uint8_t *out, float *offsets, float *scales,
                                       void *stream);
 
+/*
+ * BF16 GEMM on the tensor cores (tcgen05, accumulators in tensor memory):
+ * C[M][N] (FP32, row-major) = A[M][K] * B[N][K]^T, A and B row-major bf16
+ * ("K-major"). M, N multiples of 128, K a multiple of 64. The building block
+ * of the many-beam beamformer; no reference counterpart (the reference has
+ * no tensor-core path, form_beam.cpp:239-371 sums tiles with one thread).
+ */
+int vgb_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, void *stream);
+
 /* ---- streaming pipeline: one second of all coarse channels per step ---- */
 typedef struct vgb_pipeline vgb_pipeline;
 

@@ -1,0 +1,139 @@
+// 5th-generation tensor core (tcgen05) and tensor-TMA helpers, sm_100+/sm_103a.
+//
+// Conventions used by the kernels here:
+//  * operands are bf16, K-major (each row of an operand tile holds 64
+//    consecutive K elements = 128 bytes), staged by 2-D TMA loads with
+//    128-byte swizzling into 1024-byte aligned shared memory; that is the
+//    canonical SWIZZLE_128B K-major layout the MMA reads (8-row groups of
+//    1 KB, stride 1024 B);
+//  * accumulators are FP32 in tensor memory (TMEM), row i of a 128-row tile
+//    in TMEM lane i, column j in TMEM column base + j;
+//  * one thread issues MMAs; tcgen05.commit arrives on an mbarrier when the
+//    MMAs issued before it have completed.
+#pragma once
+
+#include <cuda.h>
+#include <cstdint>
+
+#include "vgb_internal.cuh"
+
+namespace vgb {
+
+// ---------------------------------------------------------------------------
+// TMEM allocation (one full warp executes each of these)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst_smem, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
+                 "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish()
+{
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// ---------------------------------------------------------------------------
+// Descriptors
+// ---------------------------------------------------------------------------
+// Instruction descriptor, kind::f16: FP32 accumulate, BF16 A and B, both
+// K-major, M = 128, N (multiple of 16, 16..256), optional negation of A.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t N, bool negate_a = false)
+{
+    return (1u << 4)                    // D format: F32
+           | (1u << 7)                  // A format: BF16
+           | (1u << 10)                 // B format: BF16
+           | ((negate_a ? 1u : 0u) << 13) | (0u << 15) // A K-major
+           | (0u << 16)                 // B K-major
+           | ((N >> 3) << 17)           // N >> 3
+           | ((128u >> 4) << 24);       // M >> 4
+}
+
+// Shared-memory matrix descriptor for a SWIZZLE_128B K-major tile whose
+// 1024-byte aligned start is `saddr` (shared-space byte address).
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);    // start address
+    d |= (uint64_t)1 << 16;                      // leading byte offset (16 B; unused for this layout)
+    d |= (uint64_t)(1024u >> 4) << 32;           // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;                      // descriptor version for tcgen05
+    d |= (uint64_t)2 << 61;                      // 128-byte swizzle
+    return d;
+}
+
+// Descriptor of the k-th 16-element (32-byte) K slice inside the same tile.
+__device__ __forceinline__ uint64_t sdesc_advance_k(uint64_t d, int k) { return d + (uint64_t)((k * 32) >> 4); }
+
+// ---------------------------------------------------------------------------
+// MMA, commit, TMEM loads
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// 32 consecutive FP32 columns of this thread's TMEM lane (warp w of a
+// warpgroup reads lanes 32w..32w+31; `taddr` carries the lane in bits 16+).
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// ---------------------------------------------------------------------------
+// Tensor TMA (2-D tiled, global -> shared, mbarrier completion)
+// ---------------------------------------------------------------------------
+// The x coordinate (innermost, in elements) must be a multiple of 8 for bf16
+// (16 bytes); callers only pass multiples of 64.
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void prefetch_tmap(const CUtensorMap *map)
+{
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+// Host: build a 2-D tensor map over a row-major bf16 matrix [rows][cols]
+// (row stride `row_bytes`), box = 64 columns x `box_rows` rows, 128-byte
+// swizzle. Defined in tc_gemm.cu (the driver entry point is looked up at
+// run time so the library loads without a driver).
+int make_tmap_bf16(CUtensorMap *map, const void *base, uint64_t rows, uint64_t cols, uint64_t row_bytes,
+                   uint32_t box_rows);
+
+} // namespace vgb

@@ -31,7 +31,7 @@ int check_launch(const char *what) { return check_cuda(cudaGetLastError(), what)
 // One status word per device, raised by kernels with atomicOr.
 __device__ unsigned g_status;
 
-static unsigned *status_ptr()
+unsigned *status_word()
 {
     static unsigned *ptrs[64] = {};
     int dev = 0;
@@ -111,7 +111,7 @@ int vgb_filter_fp32_exact(const int32_t *filter, int ntaps, int nchan)
 
 int vgb_check_device_status(void *stream, unsigned *flags_out)
 {
-    unsigned *p = status_ptr();
+    unsigned *p = status_word();
     if (!p) return set_error(VGB_ERR_CUDA, "device status word unavailable");
     int rc = check_cuda(cudaStreamSynchronize(S(stream)), "cudaStreamSynchronize");
     if (rc) return rc;
@@ -158,7 +158,7 @@ int vgb_beamform_mwax(const vgb_voltages *v, int ncc, int nspectra, const int32_
     a.e_cc = (long long)nspectra * kK;
     a.incoh = incoh;
     a.inc_cc = (long long)nspectra * kK;
-    a.status = status_ptr();
+    a.status = status_word();
     if (!a.status) return set_error(VGB_ERR_CUDA, "device status word unavailable");
     return launch_beam(a, ncc, !(pfb_flags & VGB_WOLA_FP32), (pfb_flags & VGB_PFB_EMULATE_FPGA) != 0,
                        (pfb_flags & VGB_PFB_COMPLEX_INT4) != 0, S(stream));
@@ -179,7 +179,7 @@ int vgb_fpfb(const vgb_voltages *v, int ncc, int nspectra, const int32_t *filter
     a.flags = pfb_flags;
     a.out = out;
     a.out_cc = (long long)nspectra * kK * v->ninputs;
-    a.status = status_ptr();
+    a.status = status_word();
     if (!a.status) return set_error(VGB_ERR_CUDA, "device status word unavailable");
     return launch_pack(a, ncc, !(pfb_flags & VGB_WOLA_FP32), (pfb_flags & VGB_PFB_EMULATE_FPGA) != 0,
                        (pfb_flags & VGB_PFB_COMPLEX_INT4) != 0, S(stream));

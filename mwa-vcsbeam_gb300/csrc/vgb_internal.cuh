@@ -51,6 +51,9 @@ struct VoltView {
 int set_error(int code, const char *fmt, ...);
 int check_cuda(cudaError_t e, const char *what);
 int check_launch(const char *what);
+// Device address of the current device's status word (kernels atomicOr
+// kErr* bits into it), or NULL.
+unsigned *status_word();
 
 // ---------------------------------------------------------------------------
 // PTX helpers: shared-memory addresses, mbarriers, 1-D bulk (TMA) copies.

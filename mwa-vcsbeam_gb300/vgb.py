@@ -89,6 +89,7 @@ _SIGS = {
     "vgb_ipfb": (I, [V, LL, V, LL, V, I, I, I, I, V, V, V, I, V]),
     "vgb_beamform_mwax_psrfits_noalloc": (I, [ctypes.POINTER(Voltages), I, I, V, I, I, U, V, I, Fl, I, V, V, V,
                                               V]),
+    "vgb_gemm_bf16": (I, [V, V, V, I, I, I, V]),
     "vgb_pipeline_create": (I, [ctypes.POINTER(PipelineConfig), ctypes.POINTER(V)]),
     "vgb_pipeline_destroy": (I, [V]),
     "vgb_pipeline_set_filters": (I, [V, V, V]),
@@ -182,6 +183,11 @@ def beamform_mwax_psrfits_noalloc(v: Voltages, ncc, nspectra, filt, flags, W, na
     check(lib().vgb_beamform_mwax_psrfits_noalloc(ctypes.byref(v), ncc, nspectra, ptr(filt), NTAPS, NCHAN, flags,
                                                   ptr(W), nant, float(invw), nstokes, ptr(out), ptr(offsets),
                                                   ptr(scales), stream_ptr(stream)))
+
+
+def gemm_bf16(A, B, C, M, N, K, stream=None):
+    """C[M][N] = A[M][K] @ B[N][K]^T on the tensor cores (bf16 in, FP32 out)."""
+    check(lib().vgb_gemm_bf16(ptr(A), ptr(B), ptr(C), M, N, K, stream_ptr(stream)))
 
 
 def fpfb(v: Voltages, ncc, nspectra, filt, i_idx, flags, out, stream=None):

@@ -1,0 +1,35 @@
+"""The tcgen05 BF16 GEMM (vgb_gemm_bf16) against a plain PyTorch FP32
+matmul of the same bf16 inputs. Tolerance: 1e-5 of the largest |C| (each
+bf16 x bf16 product is exact in FP32; only the summation order differs)."""
+import pytest
+
+from helpers import torch_cuda
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 128, 64), (256, 384, 512), (384, 256, 1024)])
+def test_gemm_bf16_matches_fp32_reference(M, N, K):
+    torch = torch_cuda()
+    import vgb
+
+    g = torch.Generator(device="cuda").manual_seed(M * 7 + N * 3 + K)
+    A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
+    B = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
+    C = torch.full((M, N), float("nan"), device="cuda")
+    vgb.gemm_bf16(A, B, C, M, N, K)
+    torch.cuda.synchronize()
+    assert vgb.check_device_status() == 0
+    ref = A.float() @ B.float().T
+    err = (C - ref).abs().max().item() / ref.abs().max().item()
+    assert err < 1e-5, err
+
+
+def test_gemm_rejects_bad_shapes():
+    torch = torch_cuda()
+    import vgb
+
+    A = torch.zeros(100, 64, dtype=torch.bfloat16, device="cuda")
+    C = torch.zeros(100, 128, device="cuda")
+    with pytest.raises(vgb.VGBError, match="multiples of 128"):
+        vgb.gemm_bf16(A, A, C, 100, 128, 64)
