@@ -234,6 +234,67 @@ int vgb_beamform_mwax_psrfits_noalloc(const vgb_voltages *v, int ncc, int nspect
  */
 int vgb_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, void *stream);
 
+/*
+ * Batched form: C[b] = A[b] B[b]^T for b < batch, A[b] at A + b*M*K elements,
+ * B[b] at B + b*N*K, C[b] at C + b*M*N. fp16 != 0 selects FP16 operands
+ * instead of BF16 (both operands the same type). Same shape rules.
+ */
+int vgb_gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, int batch, int fp16,
+                     void *stream);
+
+/* ---- many-beam beamformer on the tensor cores ----
+ *
+ * Replaces, for npointing > 1, the per-pointing loop of vmBeamformChunk
+ * (vmApplyJ_kernel + vmBeamform_kernel, form_beam.cpp:510-582, 122-371)
+ * and the host tables it consumes (vmCalcJ, jones.c:97-188; vmCalcPhi /
+ * calc_geometric_delays, geometry.c:40-213), followed by the per-channel
+ * 8-bit scale-and-offset of vmSendSToFits (form_beam.cpp:408-449, 653-673).
+ * Output Stokes are integrated over 10 samples (1 ms at 10 kHz); a value is
+ * the sum of the reference's 10 per-sample Stokes values.
+ *
+ * Precision modes: split BF16 weights (hi + lo, FP32 accumulate; within 1e-3
+ * of the FP64 chain), single BF16, single FP16. Voltages are exact in all. */
+#define VGB_MB_SPLIT_BF16 0
+#define VGB_MB_BF16 1
+#define VGB_MB_FP16 2
+#define VGB_MB_INT4 0 /* legacy 4+4-bit bytes, high nibble real (v_IDX order) */
+#define VGB_MB_INT8 1 /* int8 re, im pairs, same order */
+
+typedef struct vgb_multibeam vgb_multibeam;
+
+typedef struct vgb_multibeam_config {
+    int ncc;        /* coarse channels per call */
+    int nfine;      /* fine channels per coarse channel (128) */
+    int nant;       /* tiles, a multiple of 16; ninput = 2*nant */
+    int npointing;  /* beams */
+    int nsamples;   /* samples per channel per call, a multiple of 10 */
+    int nstokes;    /* 1 (I) or 4 (I, Q, U, V) */
+    int precision;  /* VGB_MB_* precision mode */
+    int input;      /* VGB_MB_INT4 or VGB_MB_INT8 */
+    float invw;     /* 1 / unflagged RF inputs */
+} vgb_multibeam_config;
+
+int vgb_multibeam_create(const vgb_multibeam_config *cfg, vgb_multibeam **out);
+void vgb_multibeam_destroy(vgb_multibeam *mb);
+/* Device pointers: unit [npointing][3] (E, N, H direction cosines), tile
+ * east/north/height/cable [nant] in metres; href the array reference height. */
+int vgb_multibeam_set_geometry(vgb_multibeam *mb, const double *unit, const double *east, const double *north,
+                               const double *height, const double *cable, double href, void *stream);
+/* Device pointers: D [ncc][nant][nfine][2][2] and B [ncc][npointing][nant][2][2]
+ * complex double (calibration and primary-beam Jones, D_IDX / PB order);
+ * freqs [ncc][nfine] Hz (lower channel edges); polQ/polP [nant] input indices
+ * (vmSetPolIdxLists, jones.c:40-64). */
+int vgb_multibeam_set_jones(vgb_multibeam *mb, const double *D, const double *B, const double *freqs,
+                            const uint32_t *polQ, const uint32_t *polP, void *stream);
+/* v: device [ncc][nsamples][nfine][2*nant] voltages. S (nullable): device
+ * float [ncc][nfine][npointing][nstokes][nsamples/10]. out (nullable):
+ * device uint8 [ncc][npointing][nsamples/10][nstokes][nfine] with offsets and
+ * scales [ncc][npointing][nstokes][nfine]. */
+int vgb_multibeam_run(vgb_multibeam *mb, const void *v, float *S, uint8_t *out, float *offsets, float *scales,
+                      void *stream);
+/* Kernels the last vgb_multibeam_run launched. */
+int vgb_multibeam_launches(const vgb_multibeam *mb);
+
 /* ---- streaming pipeline: one second of all coarse channels per step ---- */
 typedef struct vgb_pipeline vgb_pipeline;
 

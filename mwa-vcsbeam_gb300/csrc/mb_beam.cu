@@ -1,0 +1,940 @@
+// Many-beam tied-array beamformer on the 5th-generation tensor cores.
+//
+// The reference forms each pointing separately: vmApplyJ_kernel multiplies
+// every tile's dual-pol voltage by that tile's inverse Jones matrix and
+// vmBeamform_kernel sums phi * Jv over tiles with one thread, then detects
+// (form_beam.cpp:122-204, 239-371). For B pointings that is, per fine
+// channel, a complex contraction (beams x 2 pols) x (tiles x 2 pols) x time:
+//
+//   E[p, x](s) = sum_{a, q} W[p, x, a, q] v[a, q](s),  W = phi[p, a, c] J^-1[p, a, c]
+//
+// Here it runs as a real GEMM per fine channel on tcgen05:
+//   rows    m = 4 p + 2 x + rho       (beam, output pol, re/im of E)
+//   columns s                         (samples; 256 per tile, 250 used)
+//   K       k = 4 a + 2 q + sigma     (tile, input pol, re/im of v)
+// with A = [[Wr, -Wi], [Wi, Wr]] (the real embedding of W) and B the
+// voltages, which are exact in bf16/fp16. In the split precision mode the
+// weights are two bf16 planes, A = A_hi + A_lo (|A - A_hi - A_lo| <= 2^-17
+// |A|), both multiplied into the same FP32 accumulator in tensor memory.
+//
+// Detection (form_beam.cpp:300-371) removes each tile's own power:
+//   bnXX = |sum_a ex_a|^2 - sum_a |ex_a|^2, bnYY likewise, bnXY = ... ex ey*.
+// The subtracted sum is linear in the per-tile coherency C_a = v_a v_a^H and
+// does not depend on phi:  sum_a |ex_a|^2 = sum_a w_x C_a w_x^H with w_x the
+// x row of J^-1. Summed over the 10 samples of an integration it is a second,
+// much smaller GEMM,
+//   R[(p, st)](t) = sum_{a, j} Q[(p, st), (a, j)] Cint[(a, j)](t),
+// j in {C_QQ, C_PP, Re C_QP, Im C_QP}, st the Stokes parameter. It runs on the
+// FP16 tensor path (tc_gemm.cu): integrated coherencies of 4-bit voltages are
+// exact in FP16, those of 8-bit voltages are split into exact hi + lo halves,
+// and Q is split hi + lo with a power-of-two scale per row.
+//
+// The beam GEMM's epilogue reads the accumulators back with tcgen05.ld,
+// forms XX, YY, XY per sample across the four lanes that hold one beam,
+// integrates 10 samples, subtracts R and writes Stokes
+//   I = w (XX + YY), Q = w (XX - YY), U = 2 w Re XY, V = -2 w Im XY
+// (w = 1 / unflagged inputs, metadata.c:1554-1561), 1 ms per value.
+//
+// Weights: J^-1 = inv(D B / |D B|_F) (jones.c:97-157) is evaluated as
+// |D B|_F B^-1 D^-1, with D^-1 (per tile, channel) and B^-1 (per beam, tile)
+// inverted in FP64 and |D B|_F^2 = tr(D^H D B B^H); the geometric delay and
+// the wrap of the phase turns dt * f (geometry.c:40-101) are FP64; the
+// per-(beam, tile, channel) product and the sine/cosine of the wrapped phase
+// are FP32 (relative error ~1e-7, below the 2^-17 of the split weights).
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "tcgen05.cuh"
+#include "vgb_launch.cuh"
+
+namespace vgb {
+
+constexpr int kMbN = 256;      // samples per MMA tile
+constexpr int kMbInt = 10;     // samples per integration (1 ms at 10 kHz)
+constexpr int kMbUsed = 250;   // samples of a tile that are used: 25 integrations
+constexpr int kMbNint = kMbUsed / kMbInt;
+constexpr int kMbStages = 3;
+constexpr int kMbBeamsPerTile = 32;  // 128 rows / 4
+constexpr int kMbThreads = 192;      // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr uint32_t kMbPolls = 1u << 26;
+
+// ---------------------------------------------------------------------------
+// Tables
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 zmul2(double2 a, double2 b)
+{
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// 2x2 complex inverse in FP64 (same formula as jones.c's inv2x2S).
+__device__ __forceinline__ void zinv2x2(const double2 (&m)[4], double2 (&o)[4])
+{
+    const double2 det = make_double2(m[0].x * m[3].x - m[0].y * m[3].y - (m[1].x * m[2].x - m[1].y * m[2].y),
+                                     m[0].x * m[3].y + m[0].y * m[3].x - (m[1].x * m[2].y + m[1].y * m[2].x));
+    const double scale = 1.0 / (det.x * det.x + det.y * det.y);
+    const double2 inv = make_double2(scale * det.x, -scale * det.y);
+    const double2 ninv = make_double2(-inv.x, -inv.y);
+    o[0] = zmul2(inv, m[3]);
+    o[1] = zmul2(ninv, m[1]);
+    o[2] = zmul2(ninv, m[2]);
+    o[3] = zmul2(inv, m[0]);
+}
+
+// Per (beam, tile): geometric delay (geometry.c:40-101, same operation order
+// as the single-beam phase kernel), B^-1 and H = B B^H. Beams >= npointing are
+// zero (their weights vanish).
+__global__ void mb_pa_kernel(const double *unit, const double *east, const double *north, const double *height,
+                             const double *cable, double href, const double2 *Bj, int npointing, int Bp, int nant,
+                             double *dt, float4 *Binv, float4 *H)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= Bp * nant) return;
+    const int a = idx % nant, p = idx / nant;
+    if (p >= npointing) {
+        dt[idx] = 0.0;
+        Binv[2 * idx] = Binv[2 * idx + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        H[idx] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    if (unit) {
+        const double L = cable[a] - 0.0;
+        const double w = (east[a] - 0.0) * unit[3 * p + 0] + (north[a] - 0.0) * unit[3 * p + 1] +
+                         (height[a] - href) * unit[3 * p + 2];
+        dt[idx] = (w - L) / 299792458.0;
+    }
+    if (Bj) {
+        double2 b[4], bi[4];
+        for (int i = 0; i < 4; i++) b[i] = Bj[4 * (long long)idx + i];
+        zinv2x2(b, bi);
+        Binv[2 * idx] = make_float4((float)bi[0].x, (float)bi[0].y, (float)bi[1].x, (float)bi[1].y);
+        Binv[2 * idx + 1] = make_float4((float)bi[2].x, (float)bi[2].y, (float)bi[3].x, (float)bi[3].y);
+        // H = B B^H: H11 = |b00|^2 + |b01|^2, H22 = |b10|^2 + |b11|^2, H12 = b00 b10* + b01 b11*
+        const double h11 = b[0].x * b[0].x + b[0].y * b[0].y + b[1].x * b[1].x + b[1].y * b[1].y;
+        const double h22 = b[2].x * b[2].x + b[2].y * b[2].y + b[3].x * b[3].x + b[3].y * b[3].y;
+        const double h12r = b[0].x * b[2].x + b[0].y * b[2].y + b[1].x * b[3].x + b[1].y * b[3].y;
+        const double h12i = b[0].y * b[2].x - b[0].x * b[2].y + b[1].y * b[3].x - b[1].x * b[3].y;
+        H[idx] = make_float4((float)h11, (float)h22, (float)h12r, (float)h12i);
+    }
+}
+
+// Per (channel, tile) of one coarse channel: D^-1 and G = D^H D, from the
+// calibration solution D [tile][channel][2][2] (D_IDX order).
+__global__ void mb_ca_kernel(const double2 *D, int nant, int nfine, float4 *Dinv, float4 *G)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nant * nfine) return;
+    const int a = idx % nant, c = idx / nant; // output order [c][a]
+    double2 d[4], di[4];
+    for (int i = 0; i < 4; i++) d[i] = D[4 * ((long long)a * nfine + c) + i];
+    zinv2x2(d, di);
+    Dinv[2 * idx] = make_float4((float)di[0].x, (float)di[0].y, (float)di[1].x, (float)di[1].y);
+    Dinv[2 * idx + 1] = make_float4((float)di[2].x, (float)di[2].y, (float)di[3].x, (float)di[3].y);
+    // G = D^H D: G11 = |d00|^2 + |d10|^2, G22 = |d01|^2 + |d11|^2, G12 = d00* d01 + d10* d11
+    const double g11 = d[0].x * d[0].x + d[0].y * d[0].y + d[2].x * d[2].x + d[2].y * d[2].y;
+    const double g22 = d[1].x * d[1].x + d[1].y * d[1].y + d[3].x * d[3].x + d[3].y * d[3].y;
+    const double g12r = d[0].x * d[1].x + d[0].y * d[1].y + d[2].x * d[3].x + d[2].y * d[3].y;
+    const double g12i = d[0].x * d[1].y - d[0].y * d[1].x + d[2].x * d[3].y - d[2].y * d[3].x;
+    G[idx] = make_float4((float)g11, (float)g22, (float)g12r, (float)g12i);
+}
+
+struct MbWeightArgs {
+    const double *dt;     // [Bp][A]
+    const float4 *Binv;   // [Bp][A][2]
+    const float4 *H;      // [Bp][A]
+    const float4 *Dinv;   // [nfine][A][2]
+    const float4 *G;      // [nfine][A]
+    const double *freq;   // [nfine] Hz
+    int A, Bp, nfine, nst, planes, fp16, int8;
+    int Mrows, Mq, KA, Kq;
+    uint16_t *Aw;         // [planes][nfine][Mrows][KA]
+    __half *Aq;           // [nfine][Mq][Kq]
+    float *qscale;        // [nfine][Mq]
+};
+
+__device__ __forceinline__ float2 cmul32(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cmulc32(float2 a, float2 b) // a * conj(b)
+{
+    return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+
+// J^-1 for (channel c, beam p, tile a); zero when |D B|_F = 0 (jones.c:144-147).
+__device__ __forceinline__ void mb_jinv(const MbWeightArgs &w, int c, int p, int a, float2 (&J)[4])
+{
+    const long long pa = (long long)p * w.A + a, ca = (long long)c * w.A + a;
+    const float4 h = w.H[pa], g = w.G[ca];
+    const float tr = g.x * h.x + g.y * h.y + 2.f * (g.z * h.z + g.w * h.w);
+    if (!(tr > 0.f)) {
+        J[0] = J[1] = J[2] = J[3] = make_float2(0.f, 0.f);
+        return;
+    }
+    const float n = sqrtf(tr);
+    const float4 b0 = w.Binv[2 * pa], b1 = w.Binv[2 * pa + 1];
+    const float4 d0 = w.Dinv[2 * ca], d1 = w.Dinv[2 * ca + 1];
+    const float2 b[4] = {make_float2(b0.x, b0.y), make_float2(b0.z, b0.w), make_float2(b1.x, b1.y),
+                         make_float2(b1.z, b1.w)};
+    const float2 d[4] = {make_float2(d0.x, d0.y), make_float2(d0.z, d0.w), make_float2(d1.x, d1.y),
+                         make_float2(d1.z, d1.w)};
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+        for (int col = 0; col < 2; col++) {
+            const float2 t = cmul32(b[2 * r], d[col]);
+            const float2 u = cmul32(b[2 * r + 1], d[2 + col]);
+            J[2 * r + col] = make_float2(n * (t.x + u.x), n * (t.y + u.y));
+        }
+}
+
+// Autocorrelation coefficients of Stokes st over (C_QQ, C_PP, Re C_QP, Im C_QP).
+__device__ __forceinline__ void mb_qrow(const float2 (&J)[4], int st, float (&q)[4])
+{
+    const float2 al = J[0], be = J[1], ga = J[2], de = J[3];
+    const float2 ab = cmulc32(al, be), gd = cmulc32(ga, de);
+    const float2 ag = cmulc32(al, ga), bd = cmulc32(be, de), ad = cmulc32(al, de), bg = cmulc32(be, ga);
+    const float xx[4] = {al.x * al.x + al.y * al.y, be.x * be.x + be.y * be.y, 2.f * ab.x, -2.f * ab.y};
+    const float yy[4] = {ga.x * ga.x + ga.y * ga.y, de.x * de.x + de.y * de.y, 2.f * gd.x, -2.f * gd.y};
+    const float rexy[4] = {ag.x, bd.x, ad.x + bg.x, bg.y - ad.y};
+    const float imxy[4] = {ag.y, bd.y, ad.y + bg.y, ad.x - bg.x};
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+        q[j] = st == 0 ? xx[j] + yy[j] : st == 1 ? xx[j] - yy[j] : st == 2 ? 2.f * rexy[j] : -2.f * imxy[j];
+}
+
+__device__ __forceinline__ uint16_t to_bits(float x, bool fp16)
+{
+    return fp16 ? __half_as_ushort(__float2half_rn(x)) : __bfloat16_as_ushort(__float2bfloat16_rn(x));
+}
+__device__ __forceinline__ float from_bits(uint16_t b, bool fp16)
+{
+    return fp16 ? __half2float(__ushort_as_half(b)) : __bfloat162float(__ushort_as_bfloat16(b));
+}
+
+// One block per (beam, channel); the threads step over tiles. Pass 1 finds the
+// largest |Q| of each Stokes row (its power-of-two scale), pass 2 writes the
+// embedded weights (hi, lo planes) and the scaled, split Q rows.
+__global__ void __launch_bounds__(128) mb_weights_kernel(const MbWeightArgs w)
+{
+    const int p = blockIdx.x, c = blockIdx.y;
+    __shared__ float smax[4][4];
+    float mx[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int a = threadIdx.x; a < w.A; a += blockDim.x) {
+        float2 J[4];
+        mb_jinv(w, c, p, a, J);
+        for (int st = 0; st < w.nst; st++) {
+            float q[4];
+            mb_qrow(J, st, q);
+            for (int j = 0; j < 4; j++) mx[st] = fmaxf(mx[st], fabsf(q[j]));
+        }
+    }
+    for (int st = 0; st < 4; st++) {
+        for (int o = 16; o; o >>= 1) mx[st] = fmaxf(mx[st], __shfl_xor_sync(0xffffffffu, mx[st], o));
+        if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5][st] = mx[st];
+    }
+    __syncthreads();
+    float inv_scale[4];
+    for (int st = 0; st < 4; st++) {
+        const float m = fmaxf(fmaxf(smax[0][st], smax[1][st]), fmaxf(smax[2][st], smax[3][st]));
+        int e = 0;
+        if (m > 0.f && isfinite(m)) frexpf(m, &e); // m = f 2^e, f in [0.5, 1)
+        inv_scale[st] = ldexpf(1.f, -e);
+        if (threadIdx.x == 0 && st < w.nst) w.qscale[(long long)c * w.Mq + p * w.nst + st] = ldexpf(1.f, e);
+    }
+    const double f = (double)(uint32_t)w.freq[c];
+    const bool h16 = w.fp16 != 0;
+    for (int a = threadIdx.x; a < w.A; a += blockDim.x) {
+        float2 J[4];
+        mb_jinv(w, c, p, a, J);
+        // phase turns dt * f in FP64, wrapped to [-1/2, 1/2], then sin/cos in FP32
+        const double turns = w.dt[(long long)p * w.A + a] * f;
+        const float r = (float)(turns - rint(turns));
+        float sn, cs;
+        sincospif(2.f * r, &sn, &cs);
+        const float2 ph = make_float2(cs, sn);
+        float2 W[4];
+        for (int i = 0; i < 4; i++) W[i] = cmul32(ph, J[i]);
+        for (int x = 0; x < 2; x++)
+            for (int rho = 0; rho < 2; rho++) {
+                float val[4];
+                for (int q = 0; q < 2; q++) {
+                    const float2 v = W[2 * x + q];
+                    val[2 * q + 0] = rho == 0 ? v.x : v.y;
+                    val[2 * q + 1] = rho == 0 ? -v.y : v.x;
+                }
+                uint16_t hi[4], lo[4];
+                for (int j = 0; j < 4; j++) {
+                    hi[j] = to_bits(val[j], h16);
+                    lo[j] = to_bits(val[j] - from_bits(hi[j], h16), h16);
+                }
+                const long long row = (long long)c * w.Mrows + 4 * p + 2 * x + rho;
+                uint2 *d0 = reinterpret_cast<uint2 *>(w.Aw + row * w.KA + 4 * a);
+                *d0 = make_uint2(hi[0] | ((uint32_t)hi[1] << 16), hi[2] | ((uint32_t)hi[3] << 16));
+                if (w.planes == 2) {
+                    uint2 *d1 = reinterpret_cast<uint2 *>(w.Aw + ((long long)w.nfine * w.Mrows + row) * w.KA + 4 * a);
+                    *d1 = make_uint2(lo[0] | ((uint32_t)lo[1] << 16), lo[2] | ((uint32_t)lo[3] << 16));
+                }
+            }
+        for (int st = 0; st < w.nst; st++) {
+            float q[4];
+            mb_qrow(J, st, q);
+            uint16_t hi[4], lo[4];
+            for (int j = 0; j < 4; j++) {
+                const float s = q[j] * inv_scale[st];
+                const __half h = __float2half_rn(s);
+                hi[j] = __half_as_ushort(h);
+                lo[j] = __half_as_ushort(__float2half_rn(s - __half2float(h)));
+            }
+            __half *row = w.Aq + ((long long)c * w.Mq + p * w.nst + st) * w.Kq;
+            const uint2 H2 = make_uint2(hi[0] | ((uint32_t)hi[1] << 16), hi[2] | ((uint32_t)hi[3] << 16));
+            const uint2 L2 = make_uint2(lo[0] | ((uint32_t)lo[1] << 16), lo[2] | ((uint32_t)lo[3] << 16));
+            // 4-bit voltages: [Q_hi | Q_lo] against [C]; 8-bit: [Q_hi | Q_hi | Q_lo] against [C_hi | C_lo]
+            *reinterpret_cast<uint2 *>(row + 4 * a) = H2;
+            if (w.int8) {
+                *reinterpret_cast<uint2 *>(row + w.KA + 4 * a) = H2;
+                *reinterpret_cast<uint2 *>(row + 2 * w.KA + 4 * a) = L2;
+            } else {
+                *reinterpret_cast<uint2 *>(row + w.KA + 4 * a) = L2;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Voltages: legacy [s][c][input] (4+4-bit bytes, high nibble real, or int8
+// re, im) -> B operand V [c][s][4A] (bf16 or fp16, exact) and the integrated
+// per-tile coherencies C [c][t][Kb] (fp16; exact hi/lo halves for 8-bit).
+// ---------------------------------------------------------------------------
+struct MbConvArgs {
+    const uint8_t *v;
+    int int8, fp16;
+    int ns, nfine, ni, A, nint, nint_p, Kb;
+    const uint32_t *polQ, *polP;
+    uint16_t *V;
+    __half *C;
+};
+
+__device__ __forceinline__ int nib4(uint32_t x) { return ((int)(x << 28)) >> 28; }
+
+__global__ void __launch_bounds__(128) mb_convert_kernel(const MbConvArgs g)
+{
+    const int t = blockIdx.x, c = blockIdx.y;
+    const bool h16 = g.fp16 != 0;
+    for (int a = threadIdx.x; a < g.A; a += blockDim.x) {
+        const uint32_t iq = g.polQ[a], ip = g.polP[a];
+        int cqq = 0, cpp = 0, cr = 0, ci = 0;
+        for (int k = 0; k < kMbInt; k++) {
+            const int s = t * kMbInt + k;
+            const long long base = ((long long)s * g.nfine + c) * g.ni;
+            int qr, qi, pr, pi;
+            if (g.int8) {
+                const char2 vq = reinterpret_cast<const char2 *>(g.v)[base + iq];
+                const char2 vp = reinterpret_cast<const char2 *>(g.v)[base + ip];
+                qr = vq.x; qi = vq.y; pr = vp.x; pi = vp.y;
+            } else {
+                const uint32_t bq = g.v[base + iq], bp = g.v[base + ip];
+                qr = nib4(bq >> 4); qi = nib4(bq); pr = nib4(bp >> 4); pi = nib4(bp);
+            }
+            cqq += qr * qr + qi * qi;
+            cpp += pr * pr + pi * pi;
+            cr += qr * pr + qi * pi; // Re(vQ vP*)
+            ci += qi * pr - qr * pi; // Im(vQ vP*)
+            const uint2 o = make_uint2(to_bits((float)qr, h16) | ((uint32_t)to_bits((float)qi, h16) << 16),
+                                       to_bits((float)pr, h16) | ((uint32_t)to_bits((float)pi, h16) << 16));
+            *reinterpret_cast<uint2 *>(g.V + ((long long)c * g.ns + s) * (4 * g.A) + 4 * a) = o;
+        }
+        const int cv[4] = {cqq, cpp, cr, ci};
+        uint16_t hi[4], lo[4];
+        for (int j = 0; j < 4; j++) {
+            const __half h = __float2half_rn((float)cv[j]);
+            hi[j] = __half_as_ushort(h);
+            lo[j] = __half_as_ushort(__float2half_rn((float)(cv[j] - (int)__half2float(h))));
+        }
+        __half *row = g.C + ((long long)c * g.nint_p + t) * g.Kb;
+        *reinterpret_cast<uint2 *>(row + 4 * a) =
+            make_uint2(hi[0] | ((uint32_t)hi[1] << 16), hi[2] | ((uint32_t)hi[3] << 16));
+        if (g.int8)
+            *reinterpret_cast<uint2 *>(row + 4 * g.A + 4 * a) =
+                make_uint2(lo[0] | ((uint32_t)lo[1] << 16), lo[2] | ((uint32_t)lo[3] << 16));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The beam GEMM (persistent, one CTA per SM)
+// ---------------------------------------------------------------------------
+struct MbSmem {
+    uint8_t a[kMbStages][2][128 * 128]; // weight planes: 128 rows x 64 K (bf16/fp16)
+    uint8_t b[kMbStages][kMbN * 128];   // voltages: 256 samples x 64 K
+    uint64_t full[kMbStages], empty[kMbStages];
+    uint64_t tfull[2], tempty[2], drain;
+    uint32_t tmem;
+};
+
+struct MbBeamArgs {
+    int nfine, ns, nint, B, Mrows, mtiles, ntn, nk;
+    long long total;      // tiles: nfine * ntn * mtiles
+    const float *R;       // [nfine][Mq][nint_p]
+    const float *qscale;  // [nfine][Mq]
+    int Mq, nint_p;
+    float invw;
+    float *S;             // [nfine][B][nst][nint]
+    unsigned *status;
+};
+
+template <int kPlanes, bool kF16, int kNst>
+__global__ void __launch_bounds__(kMbThreads, 1)
+    mb_beam_kernel(const __grid_constant__ CUtensorMap tw, const __grid_constant__ CUtensorMap tv, const MbBeamArgs g)
+{
+    extern __shared__ uint8_t mb_raw[];
+    MbSmem &sm = *reinterpret_cast<MbSmem *>((reinterpret_cast<uintptr_t>(mb_raw) + 1023) & ~uintptr_t(1023));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        prefetch_tmap(&tw);
+        prefetch_tmap(&tv);
+        for (int s = 0; s < kMbStages; s++) {
+            mbar_init(&sm.full[s], 1);
+            mbar_init(&sm.empty[s], 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&sm.tfull[b], 1);
+            mbar_init(&sm.tempty[b], 4);
+        }
+        mbar_init(&sm.drain, 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    if (warp == 0) {
+        tmem_alloc(&sm.tmem, 512);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = sm.tmem;
+    const int per_tile = g.ntn * g.mtiles;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---- TMA producer ----
+            uint32_t it = 0;
+            bool ok = true;
+            for (long long tile = blockIdx.x; tile < g.total && ok; tile += gridDim.x) {
+                const int m = (int)(tile % g.mtiles);
+                const int n = (int)((tile / g.mtiles) % g.ntn);
+                const int c = (int)(tile / per_tile);
+                const int arow = c * g.Mrows + m * 128;
+                const int brow = c * g.ns + n * kMbUsed;
+                for (int kc = 0; kc < g.nk; kc++, it++) {
+                    const int s = it % kMbStages;
+                    const uint32_t r = it / kMbStages;
+                    if (r > 0 && !mbar_wait_bounded(&sm.empty[s], (r - 1) & 1, kMbPolls)) {
+                        atomicOr(g.status, kErrWaitTimeout);
+                        ok = false;
+                        break;
+                    }
+                    mbar_arrive_expect_tx(&sm.full[s], kPlanes * 128 * 128 + kMbN * 128);
+                    tma_load_2d(sm.a[s][0], &tw, kc * 64, arow, &sm.full[s]);
+                    if (kPlanes == 2) tma_load_2d(sm.a[s][1], &tw, kc * 64, arow + g.nfine * g.Mrows, &sm.full[s]);
+                    tma_load_2d(sm.b[s], &tv, kc * 64, brow, &sm.full[s]);
+                }
+            }
+            // every load issued must have landed before the CTA leaves
+            for (uint32_t k = (it > kMbStages ? it - kMbStages : 0); k < it; k++)
+                mbar_wait_bounded(&sm.full[k % kMbStages], (k / kMbStages) & 1, kMbPolls);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // ---- MMA issuer ----
+            const uint32_t idesc = idesc_bf16_f32(kMbN, false, kF16);
+            uint32_t it = 0, tc = 0;
+            bool ok = true;
+            for (long long tile = blockIdx.x; tile < g.total && ok; tile += gridDim.x, tc++) {
+                const int buf = tc & 1;
+                const uint32_t u = tc >> 1;
+                if (u > 0 && !mbar_wait_bounded(&sm.tempty[buf], (u - 1) & 1, kMbPolls)) {
+                    atomicOr(g.status, kErrWaitTimeout);
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d = tmem + buf * kMbN;
+                for (int kc = 0; kc < g.nk; kc++, it++) {
+                    const int s = it % kMbStages;
+                    if (!mbar_wait_bounded(&sm.full[s], (it / kMbStages) & 1, kMbPolls)) {
+                        atomicOr(g.status, kErrWaitTimeout);
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint64_t a0 = sdesc_sw128(smem_u32(sm.a[s][0]));
+                    const uint64_t a1 = sdesc_sw128(smem_u32(sm.a[s][1]));
+                    const uint64_t bd = sdesc_sw128(smem_u32(sm.b[s]));
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        tc_mma(d, sdesc_advance_k(a0, k), sdesc_advance_k(bd, k), idesc, (kc | k) != 0);
+                        if (kPlanes == 2) tc_mma(d, sdesc_advance_k(a1, k), sdesc_advance_k(bd, k), idesc, 1);
+                    }
+                    tc_commit(&sm.empty[s]);
+                }
+                if (ok) tc_commit(&sm.tfull[buf]);
+            }
+            // all MMAs this thread issued have completed before teardown
+            tc_commit(&sm.drain);
+            mbar_wait_bounded(&sm.drain, 0, kMbPolls);
+        }
+    } else {
+        // ---- epilogue: warps 2-5, TMEM lane quarter = warp % 4 ----
+        const int q4 = warp & 3;
+        const int row = 32 * q4 + lane;
+        const int l = lane & 3;
+        const int bl = row >> 2;
+        uint32_t tc = 0;
+        for (long long tile = blockIdx.x; tile < g.total; tile += gridDim.x, tc++) {
+            const int buf = tc & 1;
+            const int m = (int)(tile % g.mtiles);
+            const int n = (int)((tile / g.mtiles) % g.ntn);
+            const int c = (int)(tile / per_tile);
+            const int p = m * kMbBeamsPerTile + bl;
+            const int t0 = n * kMbNint;
+            const int nv = min(kMbNint, g.nint - t0);
+            const int st = kNst == 4 ? l : 0;
+            const bool writer = p < g.B && (kNst == 4 || l == 0);
+            const long long rrow = (long long)c * g.Mq + (long long)p * kNst + st;
+            float rv[kMbNint];
+            float qs = 0.f;
+            if (writer) qs = g.qscale[rrow];
+#pragma unroll
+            for (int i = 0; i < kMbNint; i++) rv[i] = (writer && i < nv) ? g.R[rrow * g.nint_p + t0 + i] : 0.f;
+            float *srow = g.S + (((long long)c * g.B + p) * kNst + st) * g.nint + t0;
+
+            if (!mbar_wait_bounded(&sm.tfull[buf], (tc >> 1) & 1, kMbPolls)) {
+                if (lane == 0) atomicOr(g.status, kErrWaitTimeout);
+                break;
+            }
+            tc_fence_after();
+            float sq = 0.f, pb = 0.f, pc = 0.f;
+#pragma unroll
+            for (int j = 0; j < kMbN / 32; j++) {
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(32 * q4) << 16) + buf * kMbN + 32 * j, v);
+#pragma unroll
+                for (int col = 0; col < 32; col++) {
+                    const int gcol = 32 * j + col;
+                    if (gcol < kMbUsed) {
+                        const float x = v[col];
+                        sq = fmaf(x, x, sq);
+                        if (kNst == 4) {
+                            const float xb = __shfl_xor_sync(0xffffffffu, x, 2);
+                            const float xc = __shfl_xor_sync(0xffffffffu, x, 3);
+                            pb = fmaf(x, xb, pb);
+                            pc = fmaf(x, xc, pc);
+                        }
+                        if (gcol % kMbInt == kMbInt - 1) {
+                            const int ti = gcol / kMbInt;
+                            float val;
+                            if (kNst == 4) {
+                                // lanes of a beam: 0 Xr, 1 Xi, 2 Yr, 3 Yi
+                                const float t1 = sq + __shfl_xor_sync(0xffffffffu, sq, 1);
+                                const float t1o = __shfl_xor_sync(0xffffffffu, t1, 2);
+                                const float xx = l < 2 ? t1 : t1o, yy = l < 2 ? t1o : t1;
+                                const float re = pb + __shfl_xor_sync(0xffffffffu, pb, 1);
+                                const float d = __shfl_xor_sync(0xffffffffu, pc, 1) - pc;
+                                const float im = (l == 0 || l == 3) ? d : -d;
+                                val = l == 0 ? xx + yy : l == 1 ? xx - yy : l == 2 ? 2.f * re : -2.f * im;
+                            } else {
+                                float t1 = sq + __shfl_xor_sync(0xffffffffu, sq, 1);
+                                t1 += __shfl_xor_sync(0xffffffffu, t1, 2);
+                                val = t1;
+                            }
+                            if (writer && ti < nv) srow[ti] = g.invw * (val - qs * rv[ti]);
+                            sq = pb = pc = 0.f;
+                        }
+                    }
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&sm.tempty[buf]);
+        }
+    }
+    __syncwarp();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 512);
+}
+
+// ---------------------------------------------------------------------------
+// Scale-and-offset to 8 bits (form_beam.cpp:408-449 arithmetic, the same as
+// renorm_kernel) from the beam-major Stokes [c][p][st][t], written in the
+// PSRFITS order out[p][t][st][c] through a shared-memory transpose.
+// ---------------------------------------------------------------------------
+struct MbRenormArgs {
+    const float *S;
+    int nfine, B, nst, nint;
+    uint8_t *out;
+    long long out_p, out_s, out_st;
+    float *offsets, *scales; // [(p * nst + st) * nfine + c]
+};
+
+__global__ void __launch_bounds__(256) mb_renorm_kernel(const MbRenormArgs a)
+{
+    __shared__ float s_off[32], s_scl[32];
+    __shared__ uint8_t tileu[32][33];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int c0 = blockIdx.x * 32;
+    const int st = blockIdx.y % a.nst, p = blockIdx.y / a.nst;
+    for (int k = 0; k < 4; k++) {
+        const int cs = wid + 8 * k, c = c0 + cs;
+        if (c >= a.nfine) continue;
+        const float *row = a.S + (((long long)c * a.B + p) * a.nst + st) * a.nint;
+        const float s0 = row[0];
+        float mn = s0, mx = s0;
+        for (int t = lane; t < a.nint; t += 32) {
+            const float v = row[t];
+            mn = (v < mn ? v : mn);
+            mx = (v > mx ? v : mx);
+        }
+        for (int o = 16; o; o >>= 1) {
+            const float v0 = __shfl_xor_sync(0xffffffffu, mn, o), v1 = __shfl_xor_sync(0xffffffffu, mx, o);
+            mn = (v0 < mn ? v0 : mn);
+            mx = (v1 > mx ? v1 : mx);
+        }
+        if (lane == 0) {
+            const float scale = (float)((double)(mx - mn) / 256.0);
+            s_off[cs] = mn;
+            s_scl[cs] = scale;
+            const long long si = ((long long)p * a.nst + st) * a.nfine + c;
+            a.scales[si] = scale;
+            a.offsets[si] = mn;
+        }
+    }
+    __syncthreads();
+    for (int t0 = 0; t0 < a.nint; t0 += 32) {
+        for (int k = 0; k < 4; k++) {
+            const int cs = wid + 8 * k, c = c0 + cs, t = t0 + lane;
+            uint8_t u = 0;
+            if (c < a.nfine && t < a.nint) {
+                const float v = (a.S[(((long long)c * a.B + p) * a.nst + st) * a.nint + t] - s_off[cs]) / s_scl[cs];
+                u = sat_u8((double)v + 0.5);
+            }
+            tileu[lane][cs] = u;
+        }
+        __syncthreads();
+        const int t = t0 + (threadIdx.x >> 3), cg = (threadIdx.x & 7) * 4;
+        if (t < a.nint) {
+            uint8_t *o = a.out + p * a.out_p + (long long)t * a.out_s + st * a.out_st + c0 + cg;
+            for (int k = 0; k < 4; k++)
+                if (c0 + cg + k < a.nfine) o[k] = tileu[threadIdx.x >> 3][cg + k];
+        }
+        __syncthreads();
+    }
+}
+
+} // namespace vgb
+
+using namespace vgb;
+
+// ---------------------------------------------------------------------------
+// Host object
+// ---------------------------------------------------------------------------
+struct vgb_multibeam {
+    vgb_multibeam_config cfg;
+    int nch, Bp, Mrows, Mq, KA, Kq, Kb, nint, nint_p, planes, ntn, mtiles, nk, fp16, int8;
+    double *d_dt = nullptr;
+    float4 *d_Binv = nullptr, *d_H = nullptr, *d_Dinv = nullptr, *d_G = nullptr;
+    double *d_freq = nullptr;
+    uint32_t *d_polQ = nullptr, *d_polP = nullptr;
+    uint16_t *d_Aw = nullptr, *d_V = nullptr;
+    __half *d_Aq = nullptr, *d_C = nullptr;
+    float *d_qscale = nullptr, *d_R = nullptr, *d_S = nullptr;
+    CUtensorMap tmW, tmV;
+    bool have_geometry = false, have_jones = false;
+    int nsm = 0;
+    int last_launches = 0; // kernels the last run launched
+};
+
+namespace {
+
+template <typename T> int mb_alloc(T **p, size_t n, const char *what)
+{
+    if (cudaMalloc(reinterpret_cast<void **>(p), n * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return set_error(VGB_ERR_ALLOC, "multibeam: cannot allocate %s (%zu bytes)", what, n * sizeof(T));
+    }
+    return VGB_SUCCESS;
+}
+
+void mb_free(vgb_multibeam *mb)
+{
+    void *ptrs[] = {mb->d_dt, mb->d_Binv, mb->d_H, mb->d_Dinv, mb->d_G, mb->d_freq, mb->d_polQ, mb->d_polP,
+                    mb->d_Aw, mb->d_V, mb->d_Aq, mb->d_C, mb->d_qscale, mb->d_R, mb->d_S};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+}
+
+template <int kPlanes, bool kF16, int kNst> int mb_launch_beam(vgb_multibeam *mb, const MbBeamArgs &a, cudaStream_t st)
+{
+    auto kern = mb_beam_kernel<kPlanes, kF16, kNst>;
+    const int smem = (int)sizeof(MbSmem) + 1024;
+    int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                        "cudaFuncSetAttribute(mb_beam_kernel)");
+    if (rc) return rc;
+    const long long grid = a.total < mb->nsm ? a.total : mb->nsm;
+    kern<<<(unsigned)grid, kMbThreads, smem, st>>>(mb->tmW, mb->tmV, a);
+    return check_launch("mb_beam_kernel");
+}
+
+} // namespace
+
+extern "C" int vgb_multibeam_create(const vgb_multibeam_config *cfg, vgb_multibeam **out)
+{
+    if (!cfg || !out) return set_error(VGB_ERR_INVALID, "multibeam: NULL argument");
+    *out = nullptr;
+    const vgb_multibeam_config &c = *cfg;
+    if (c.ncc <= 0 || c.nfine <= 0 || c.nfine > 4096)
+        return set_error(VGB_ERR_INVALID, "multibeam: ncc and nfine must be positive (nfine <= 4096)");
+    if (c.nant <= 0 || c.nant % 16)
+        return set_error(VGB_ERR_INVALID, "multibeam: nant must be a positive multiple of 16 (got %d)", c.nant);
+    if (c.npointing <= 0) return set_error(VGB_ERR_INVALID, "multibeam: npointing must be positive");
+    if (c.nsamples <= 0 || c.nsamples % kMbInt)
+        return set_error(VGB_ERR_INVALID, "multibeam: nsamples must be a positive multiple of %d", kMbInt);
+    if (c.nstokes != 1 && c.nstokes != 4) return set_error(VGB_ERR_INVALID, "multibeam: nstokes must be 1 or 4");
+    if (c.precision != VGB_MB_SPLIT_BF16 && c.precision != VGB_MB_BF16 && c.precision != VGB_MB_FP16)
+        return set_error(VGB_ERR_UNSUPPORTED, "multibeam: unknown precision %d", c.precision);
+    if (c.input != VGB_MB_INT4 && c.input != VGB_MB_INT8)
+        return set_error(VGB_ERR_UNSUPPORTED, "multibeam: unknown input format %d", c.input);
+
+    vgb_multibeam *mb = new vgb_multibeam();
+    mb->cfg = c;
+    mb->nch = c.nfine;
+    mb->Bp = (c.npointing + kMbBeamsPerTile - 1) / kMbBeamsPerTile * kMbBeamsPerTile;
+    mb->Mrows = 4 * mb->Bp;
+    mb->mtiles = mb->Mrows / 128;
+    mb->Mq = (c.nstokes * mb->Bp + 127) / 128 * 128;
+    mb->KA = 4 * c.nant;
+    mb->nk = mb->KA / 64;
+    mb->int8 = c.input == VGB_MB_INT8;
+    mb->Kb = mb->int8 ? 8 * c.nant : 4 * c.nant;
+    mb->Kq = mb->int8 ? 12 * c.nant : 8 * c.nant;
+    mb->nint = c.nsamples / kMbInt;
+    mb->nint_p = (mb->nint + 127) / 128 * 128;
+    mb->planes = c.precision == VGB_MB_SPLIT_BF16 ? 2 : 1;
+    mb->fp16 = c.precision == VGB_MB_FP16;
+    mb->ntn = (c.nsamples + kMbUsed - 1) / kMbUsed;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&mb->nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (mb->nsm <= 0) mb->nsm = 1;
+
+    const size_t nf = c.nfine, A = c.nant;
+    int rc = VGB_SUCCESS;
+    if (!rc) rc = mb_alloc(&mb->d_dt, (size_t)mb->Bp * A, "delays");
+    if (!rc) rc = mb_alloc(&mb->d_Binv, (size_t)c.ncc * mb->Bp * A * 2, "B^-1");
+    if (!rc) rc = mb_alloc(&mb->d_H, (size_t)c.ncc * mb->Bp * A, "B B^H");
+    if (!rc) rc = mb_alloc(&mb->d_Dinv, (size_t)c.ncc * nf * A * 2, "D^-1");
+    if (!rc) rc = mb_alloc(&mb->d_G, (size_t)c.ncc * nf * A, "D^H D");
+    if (!rc) rc = mb_alloc(&mb->d_freq, (size_t)c.ncc * nf, "frequencies");
+    if (!rc) rc = mb_alloc(&mb->d_polQ, A, "polQ");
+    if (!rc) rc = mb_alloc(&mb->d_polP, A, "polP");
+    if (!rc) rc = mb_alloc(&mb->d_Aw, (size_t)mb->planes * nf * mb->Mrows * mb->KA, "weights");
+    if (!rc) rc = mb_alloc(&mb->d_V, nf * c.nsamples * mb->KA, "voltages");
+    if (!rc) rc = mb_alloc(&mb->d_Aq, nf * mb->Mq * mb->Kq, "autocorrelation weights");
+    if (!rc) rc = mb_alloc(&mb->d_C, nf * mb->nint_p * mb->Kb, "coherencies");
+    if (!rc) rc = mb_alloc(&mb->d_qscale, nf * mb->Mq, "row scales");
+    if (!rc) rc = mb_alloc(&mb->d_R, nf * mb->Mq * mb->nint_p, "autocorrelation terms");
+    if (!rc) rc = mb_alloc(&mb->d_S, nf * c.npointing * c.nstokes * mb->nint, "Stokes");
+    if (!rc)
+        rc = check_cuda(cudaMemset(mb->d_Aq, 0, nf * mb->Mq * mb->Kq * sizeof(__half)), "cudaMemset");
+    if (!rc) rc = check_cuda(cudaMemset(mb->d_C, 0, nf * mb->nint_p * mb->Kb * sizeof(__half)), "cudaMemset");
+    if (!rc)
+        rc = make_tmap_bf16(&mb->tmW, mb->d_Aw, (uint64_t)mb->planes * nf * mb->Mrows, mb->KA, (uint64_t)mb->KA * 2,
+                            128, mb->fp16);
+    if (!rc)
+        rc = make_tmap_bf16(&mb->tmV, mb->d_V, (uint64_t)nf * c.nsamples, mb->KA, (uint64_t)mb->KA * 2, kMbN,
+                            mb->fp16);
+    if (rc) {
+        mb_free(mb);
+        delete mb;
+        return rc;
+    }
+    *out = mb;
+    return VGB_SUCCESS;
+}
+
+extern "C" void vgb_multibeam_destroy(vgb_multibeam *mb)
+{
+    if (!mb) return;
+    cudaDeviceSynchronize();
+    mb_free(mb);
+    delete mb;
+}
+
+extern "C" int vgb_multibeam_set_geometry(vgb_multibeam *mb, const double *unit, const double *east,
+                                          const double *north, const double *height, const double *cable,
+                                          double href, void *stream)
+{
+    if (!mb || !unit || !east || !north || !height || !cable)
+        return set_error(VGB_ERR_INVALID, "multibeam_set_geometry: NULL argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int n = mb->Bp * mb->cfg.nant;
+    mb_pa_kernel<<<(n + 255) / 256, 256, 0, st>>>(unit, east, north, height, cable, href, nullptr,
+                                                   mb->cfg.npointing, mb->Bp, mb->cfg.nant, mb->d_dt, mb->d_Binv,
+                                                   mb->d_H);
+    int rc = check_launch("mb_pa_kernel");
+    if (!rc) mb->have_geometry = true;
+    return rc;
+}
+
+extern "C" int vgb_multibeam_set_jones(vgb_multibeam *mb, const double *D, const double *Bj, const double *freqs,
+                                       const uint32_t *polQ, const uint32_t *polP, void *stream)
+{
+    if (!mb || !D || !Bj || !freqs || !polQ || !polP)
+        return set_error(VGB_ERR_INVALID, "multibeam_set_jones: NULL argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const vgb_multibeam_config &c = mb->cfg;
+    const int A = c.nant, nf = c.nfine;
+    int rc = VGB_SUCCESS;
+    for (int cc = 0; cc < c.ncc && !rc; cc++) {
+        const int npa = mb->Bp * A;
+        // B^-1 and B B^H: the delays pass is skipped (unit == NULL)
+        mb_pa_kernel<<<(npa + 255) / 256, 256, 0, st>>>(
+            nullptr, nullptr, nullptr, nullptr, nullptr, 0.0,
+            reinterpret_cast<const double2 *>(Bj) + 4ll * cc * c.npointing * A, c.npointing, mb->Bp, A, mb->d_dt,
+            mb->d_Binv + 2ll * cc * npa, mb->d_H + (long long)cc * npa);
+        if ((rc = check_launch("mb_pa_kernel"))) break;
+        mb_ca_kernel<<<(nf * A + 255) / 256, 256, 0, st>>>(reinterpret_cast<const double2 *>(D) + 4ll * cc * A * nf,
+                                                           A, nf, mb->d_Dinv + 2ll * cc * nf * A,
+                                                           mb->d_G + (long long)cc * nf * A);
+        rc = check_launch("mb_ca_kernel");
+    }
+    if (!rc)
+        rc = check_cuda(cudaMemcpyAsync(mb->d_freq, freqs, sizeof(double) * c.ncc * nf, cudaMemcpyDeviceToDevice, st),
+                        "cudaMemcpyAsync(freqs)");
+    if (!rc)
+        rc = check_cuda(cudaMemcpyAsync(mb->d_polQ, polQ, sizeof(uint32_t) * A, cudaMemcpyDeviceToDevice, st),
+                        "cudaMemcpyAsync(polQ)");
+    if (!rc)
+        rc = check_cuda(cudaMemcpyAsync(mb->d_polP, polP, sizeof(uint32_t) * A, cudaMemcpyDeviceToDevice, st),
+                        "cudaMemcpyAsync(polP)");
+    if (!rc) mb->have_jones = true;
+    return rc;
+}
+
+extern "C" int vgb_multibeam_run(vgb_multibeam *mb, const void *v, float *S, uint8_t *out, float *offsets,
+                                 float *scales, void *stream)
+{
+    if (!mb || !v) return set_error(VGB_ERR_INVALID, "multibeam_run: NULL argument");
+    if (!mb->have_geometry || !mb->have_jones)
+        return set_error(VGB_ERR_STATE, "multibeam_run: set_geometry and set_jones must come first");
+    if (out && (!offsets || !scales))
+        return set_error(VGB_ERR_INVALID, "multibeam_run: PSRFITS output needs offsets and scales");
+    unsigned *status = status_word();
+    if (!status) return set_error(VGB_ERR_CUDA, "device status word unavailable");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const vgb_multibeam_config &c = mb->cfg;
+    const int A = c.nant, nf = c.nfine, ns = c.nsamples;
+    const long long vbytes_cc = (long long)ns * nf * 2 * A * (mb->int8 ? 2 : 1);
+    const long long s_cc = (long long)nf * c.npointing * c.nstokes * mb->nint;
+    int rc = VGB_SUCCESS;
+    mb->last_launches = 0;
+    for (int cc = 0; cc < c.ncc && !rc; cc++) {
+        mb->last_launches += out ? 5 : 4;
+        MbWeightArgs w{};
+        w.dt = mb->d_dt;
+        w.Binv = mb->d_Binv + 2ll * cc * mb->Bp * A;
+        w.H = mb->d_H + (long long)cc * mb->Bp * A;
+        w.Dinv = mb->d_Dinv + 2ll * cc * nf * A;
+        w.G = mb->d_G + (long long)cc * nf * A;
+        w.freq = mb->d_freq + (long long)cc * nf;
+        w.A = A;
+        w.Bp = mb->Bp;
+        w.nfine = nf;
+        w.nst = c.nstokes;
+        w.planes = mb->planes;
+        w.fp16 = mb->fp16;
+        w.int8 = mb->int8;
+        w.Mrows = mb->Mrows;
+        w.Mq = mb->Mq;
+        w.KA = mb->KA;
+        w.Kq = mb->Kq;
+        w.Aw = mb->d_Aw;
+        w.Aq = mb->d_Aq;
+        w.qscale = mb->d_qscale;
+        mb_weights_kernel<<<dim3(mb->Bp, nf), 128, 0, st>>>(w);
+        if ((rc = check_launch("mb_weights_kernel"))) break;
+
+        MbConvArgs g{};
+        g.v = static_cast<const uint8_t *>(v) + cc * vbytes_cc;
+        g.int8 = mb->int8;
+        g.fp16 = mb->fp16;
+        g.ns = ns;
+        g.nfine = nf;
+        g.ni = 2 * A;
+        g.A = A;
+        g.nint = mb->nint;
+        g.nint_p = mb->nint_p;
+        g.Kb = mb->Kb;
+        g.polQ = mb->d_polQ;
+        g.polP = mb->d_polP;
+        g.V = mb->d_V;
+        g.C = mb->d_C;
+        mb_convert_kernel<<<dim3(mb->nint, nf), 128, 0, st>>>(g);
+        if ((rc = check_launch("mb_convert_kernel"))) break;
+
+        // autocorrelation terms R = Q C^T per channel (FP16 tensor path)
+        if ((rc = gemm_batched(mb->d_Aq, mb->d_C, mb->d_R, mb->Mq, mb->nint_p, mb->Kq, nf, true, st, mb->Kb))) break;
+
+        MbBeamArgs b{};
+        b.nfine = nf;
+        b.ns = ns;
+        b.nint = mb->nint;
+        b.B = c.npointing;
+        b.Mrows = mb->Mrows;
+        b.mtiles = mb->mtiles;
+        b.ntn = mb->ntn;
+        b.nk = mb->nk;
+        b.total = (long long)nf * mb->ntn * mb->mtiles;
+        b.R = mb->d_R;
+        b.qscale = mb->d_qscale;
+        b.Mq = mb->Mq;
+        b.nint_p = mb->nint_p;
+        b.invw = c.invw;
+        b.S = S ? S + cc * s_cc : mb->d_S;
+        b.status = status;
+        if (mb->planes == 2)
+            rc = c.nstokes == 4 ? mb_launch_beam<2, false, 4>(mb, b, st) : mb_launch_beam<2, false, 1>(mb, b, st);
+        else if (mb->fp16)
+            rc = c.nstokes == 4 ? mb_launch_beam<1, true, 4>(mb, b, st) : mb_launch_beam<1, true, 1>(mb, b, st);
+        else
+            rc = c.nstokes == 4 ? mb_launch_beam<1, false, 4>(mb, b, st) : mb_launch_beam<1, false, 1>(mb, b, st);
+        if (rc) break;
+
+        if (out) {
+            MbRenormArgs r{};
+            r.S = b.S;
+            r.nfine = nf;
+            r.B = c.npointing;
+            r.nst = c.nstokes;
+            r.nint = mb->nint;
+            const long long out_st = nf, out_s = (long long)c.nstokes * nf, out_p = out_s * mb->nint;
+            r.out = out + cc * out_p * c.npointing;
+            r.out_p = out_p;
+            r.out_s = out_s;
+            r.out_st = out_st;
+            const long long stat_cc = (long long)c.npointing * c.nstokes * nf;
+            r.offsets = offsets + cc * stat_cc;
+            r.scales = scales + cc * stat_cc;
+            mb_renorm_kernel<<<dim3((nf + 31) / 32, c.npointing * c.nstokes), 256, 0, st>>>(r);
+            rc = check_launch("mb_renorm_kernel");
+        }
+    }
+    return rc;
+}
+
+extern "C" int vgb_multibeam_launches(const vgb_multibeam *mb)
+{
+    // per coarse channel: weights, convert, R GEMM, beam GEMM (+ renormalise)
+    return mb ? mb->last_launches : 0;
+}

@@ -131,12 +131,6 @@ int launch_weights(const double2 *J, const double2 *phi, long long n, float4 *W,
 // with val + 0.5 in FP64, as the reference's GPU build performs it: truncate
 // to an integer and keep the low 8 bits, so a channel's maximum sample
 // (256.5) becomes 0; NaN becomes 0. val is never negative here.
-__device__ __forceinline__ uint8_t sat_u8(double t)
-{
-    if (t != t || t <= 0.0) return 0;
-    return (uint8_t)((unsigned)t & 0xFFu);
-}
-
 // One warp lane per channel; the 8 warps of a block split the samples.
 __global__ void __launch_bounds__(256) renorm_kernel(const RenormArgs a)
 {

@@ -3,9 +3,9 @@
 // many-beam beamformer, exported on its own (vgb_gemm_bf16) so it can be
 // tested and measured against cuBLAS-free references.
 //
-// One CTA (4 warps) computes a 128 x 128 tile: warp 0 lane 0 streams 64-wide
-// K chunks of A and B through a 4-stage ring with 2-D TMA loads
-// (SWIZZLE_128B), warp 1 lane 0 issues four 128x128x16 tcgen05 MMAs per chunk
+// One CTA (4 warps) computes a 128 x BN tile (BN = 128 or 256): warp 0 lane 0
+// streams 64-wide K chunks of A and B through a 4-stage ring with 2-D TMA loads
+// (SWIZZLE_128B), warp 1 lane 0 issues four 128xBNx16 tcgen05 MMAs per chunk
 // into an FP32 accumulator in tensor memory and releases each stage with
 // tcgen05.commit, and all four warps read the accumulator back with
 // tcgen05.ld for the epilogue. Every wait is bounded; on expiry the CTA flags
@@ -21,9 +21,10 @@ constexpr int kGemmStages = 4;
 constexpr int kTileBytes = 128 * 64 * 2; // one 128-row x 64-column bf16 tile
 constexpr uint32_t kWaitPolls = 1u << 24;
 
+template <int BN>
 struct GemmSmem {
     uint8_t a[kGemmStages][kTileBytes];
-    uint8_t b[kGemmStages][kTileBytes];
+    uint8_t b[kGemmStages][BN * 128];
     uint64_t full[kGemmStages];
     uint64_t empty[kGemmStages];
     uint64_t done;
@@ -45,7 +46,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 }
 
 int make_tmap_bf16(CUtensorMap *map, const void *base, uint64_t rows, uint64_t cols, uint64_t row_bytes,
-                   uint32_t box_rows)
+                   uint32_t box_rows, bool fp16)
 {
     auto fn = encode_fn();
     if (!fn) return set_error(VGB_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
@@ -56,21 +57,24 @@ int make_tmap_bf16(CUtensorMap *map, const void *base, uint64_t rows, uint64_t c
     cuuint64_t strides[1] = {row_bytes};
     cuuint32_t box[2] = {64, box_rows};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+    CUresult r = fn(map, fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_error(VGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return VGB_SUCCESS;
 }
 
+template <bool kF16, int BN>
 __global__ void __launch_bounds__(128, 1)
     gemm_bf16_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, float *C,
-                     int N, int K, unsigned *status)
+                     int M, int N, int K, int Kb, unsigned *status)
 {
     extern __shared__ uint8_t gemm_raw[];
-    GemmSmem &sm = *reinterpret_cast<GemmSmem *>((reinterpret_cast<uintptr_t>(gemm_raw) + 1023) & ~uintptr_t(1023));
+    GemmSmem<BN> &sm =
+        *reinterpret_cast<GemmSmem<BN> *>((reinterpret_cast<uintptr_t>(gemm_raw) + 1023) & ~uintptr_t(1023));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.y * 128, n0 = blockIdx.x * 128;
+    const int m0 = blockIdx.y * 128, n0 = blockIdx.x * BN;
+    const int batch = blockIdx.z; // A rows batch*M.., B rows batch*N.., C batch*M*N..
     const int nk = K / 64;
 
     if (threadIdx.x == 0) {
@@ -85,7 +89,7 @@ __global__ void __launch_bounds__(128, 1)
     }
     __syncwarp();
     if (warp == 0) {
-        tmem_alloc(&sm.tmem, 128);
+        tmem_alloc(&sm.tmem, BN);
         tmem_relinquish();
     }
     tc_fence_before();
@@ -102,13 +106,13 @@ __global__ void __launch_bounds__(128, 1)
                 atomicOr(status, kErrWaitTimeout);
                 break;
             }
-            mbar_arrive_expect_tx(&sm.full[s], 2 * kTileBytes);
-            tma_load_2d(sm.a[s], &ta, kc * 64, m0, &sm.full[s]);
-            tma_load_2d(sm.b[s], &tb, kc * 64, n0, &sm.full[s]);
+            mbar_arrive_expect_tx(&sm.full[s], kTileBytes + BN * 128);
+            tma_load_2d(sm.a[s], &ta, kc * 64, batch * M + m0, &sm.full[s]);
+            tma_load_2d(sm.b[s], &tb, (kc * 64) % Kb, batch * N + n0, &sm.full[s]);
             issued++;
         }
     } else if (warp == 1 && lane == 0) {
-        const uint32_t idesc = idesc_bf16_f32(128);
+        const uint32_t idesc = idesc_bf16_f32(BN, false, kF16);
         for (int kc = 0; kc < nk; kc++) {
             const int s = kc % kGemmStages;
             if (!mbar_wait_bounded(&sm.full[s], (kc / kGemmStages) & 1, kWaitPolls)) {
@@ -132,10 +136,11 @@ __global__ void __launch_bounds__(128, 1)
     if (done) {
         const int row = m0 + warp * 32 + lane;
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
+        for (int c = 0; c < BN / 32; c++) {
             float v[32];
             tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + c * 32, v);
-            float4 *out = reinterpret_cast<float4 *>(C + (long long)row * N + n0 + c * 32);
+            float4 *out =
+                reinterpret_cast<float4 *>(C + ((long long)batch * M + row) * N + n0 + c * 32);
 #pragma unroll
             for (int j = 0; j < 8; j++) out[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
         }
@@ -149,31 +154,61 @@ __global__ void __launch_bounds__(128, 1)
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, 128);
+    if (warp == 0) tmem_dealloc(tmem, BN);
 }
 
 } // namespace vgb
 
 using namespace vgb;
 
-extern "C" int vgb_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, void *stream)
+namespace vgb {
+
+// C[b] = A[b] B[b]^T for b < batch: A rows b*M.., B rows b*N.., C rows b*M.. of
+// contiguous row-major operands (bf16, or fp16 with `fp16`). B may be
+// narrower than A along K (Kb columns, a multiple of 64): column k of A meets
+// column k mod Kb of B, i.e. B is read as [B | B | ...] cut to K columns.
+int gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, int batch, bool fp16,
+                 cudaStream_t st, int Kb)
 {
     if (!A || !B || !C) return set_error(VGB_ERR_INVALID, "gemm: NULL operand");
-    if (M <= 0 || N <= 0 || K <= 0 || M % 128 || N % 128 || K % 64)
+    if (Kb <= 0) Kb = K;
+    if (M <= 0 || N <= 0 || K <= 0 || batch <= 0 || M % 128 || N % 128 || K % 64 || Kb % 64)
         return set_error(VGB_ERR_INVALID, "gemm: M and N must be multiples of 128 and K of 64 (got %d, %d, %d)", M, N,
                          K);
     if ((reinterpret_cast<uintptr_t>(C) & 15)) return set_error(VGB_ERR_INVALID, "gemm: C must be 16-byte aligned");
+    const int bn = (N % 256 == 0) ? 256 : 128;
     CUtensorMap ta, tb;
-    int rc = make_tmap_bf16(&ta, A, M, K, (uint64_t)K * 2, 128);
+    int rc = make_tmap_bf16(&ta, A, (uint64_t)M * batch, K, (uint64_t)K * 2, 128, fp16);
     if (rc) return rc;
-    if ((rc = make_tmap_bf16(&tb, B, N, K, (uint64_t)K * 2, 128))) return rc;
+    if ((rc = make_tmap_bf16(&tb, B, (uint64_t)N * batch, Kb, (uint64_t)Kb * 2, bn, fp16))) return rc;
     unsigned *status = status_word();
     if (!status) return set_error(VGB_ERR_CUDA, "device status word unavailable");
-    const int smem = (int)sizeof(GemmSmem) + 1024;
-    if ((rc = check_cuda(cudaFuncSetAttribute(gemm_bf16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
-                         "cudaFuncSetAttribute(gemm)")))
-        return rc;
-    dim3 grid(N / 128, M / 128);
-    gemm_bf16_kernel<<<grid, 128, smem, static_cast<cudaStream_t>(stream)>>>(ta, tb, C, N, K, status);
+    dim3 grid(N / bn, M / 128, batch);
+    auto go = [&](auto kern, int smem) {
+        int r = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                           "cudaFuncSetAttribute(gemm)");
+        if (!r) kern<<<grid, 128, smem, st>>>(ta, tb, C, M, N, K, Kb, status);
+        return r;
+    };
+    if (fp16)
+        rc = bn == 256 ? go(gemm_bf16_kernel<true, 256>, (int)sizeof(GemmSmem<256>) + 1024)
+                       : go(gemm_bf16_kernel<true, 128>, (int)sizeof(GemmSmem<128>) + 1024);
+    else
+        rc = bn == 256 ? go(gemm_bf16_kernel<false, 256>, (int)sizeof(GemmSmem<256>) + 1024)
+                       : go(gemm_bf16_kernel<false, 128>, (int)sizeof(GemmSmem<128>) + 1024);
+    if (rc) return rc;
     return check_launch("gemm_bf16_kernel");
+}
+
+} // namespace vgb
+
+extern "C" int vgb_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, void *stream)
+{
+    return gemm_batched(A, B, C, M, N, K, 1, false, static_cast<cudaStream_t>(stream), K);
+}
+
+extern "C" int vgb_gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, int batch, int fp16,
+                                void *stream)
+{
+    return gemm_batched(A, B, C, M, N, K, batch, fp16 != 0, static_cast<cudaStream_t>(stream), K);
 }

@@ -43,13 +43,14 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 // ---------------------------------------------------------------------------
 // Descriptors
 // ---------------------------------------------------------------------------
-// Instruction descriptor, kind::f16: FP32 accumulate, BF16 A and B, both
-// K-major, M = 128, N (multiple of 16, 16..256), optional negation of A.
-__host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t N, bool negate_a = false)
+// Instruction descriptor, kind::f16: FP32 accumulate, BF16 (or, with
+// fp16 = true, FP16) A and B, both K-major, M = 128, N (multiple of 16,
+// 16..256), optional negation of A.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t N, bool negate_a = false, bool fp16 = false)
 {
     return (1u << 4)                    // D format: F32
-           | (1u << 7)                  // A format: BF16
-           | (1u << 10)                 // B format: BF16
+           | ((fp16 ? 0u : 1u) << 7)    // A format: BF16 (1) or F16 (0)
+           | ((fp16 ? 0u : 1u) << 10)   // B format: the same type as A
            | ((negate_a ? 1u : 0u) << 13) | (0u << 15) // A K-major
            | (0u << 16)                 // B K-major
            | ((N >> 3) << 17)           // N >> 3
@@ -134,6 +135,6 @@ __device__ __forceinline__ void prefetch_tmap(const CUtensorMap *map)
 // swizzle. Defined in tc_gemm.cu (the driver entry point is looked up at
 // run time so the library loads without a driver).
 int make_tmap_bf16(CUtensorMap *map, const void *base, uint64_t rows, uint64_t cols, uint64_t row_bytes,
-                   uint32_t box_rows);
+                   uint32_t box_rows, bool fp16 = false);
 
 } // namespace vgb

@@ -99,6 +99,20 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t phase,
     return false;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// The reference's (uint8_t)(x + 0.5) as its GPU build evaluates it: NaN and
+// values <= 0 give 0, larger values keep the low 8 bits of the truncated
+// integer (a channel maximum of 256.5 wraps to 0).
+__device__ __forceinline__ uint8_t sat_u8(double t)
+{
+    if (t != t || t <= 0.0) return 0;
+    return (uint8_t)((unsigned)t & 0xFFu);
+}
+
 // 1-D bulk copy global -> shared through the TMA unit. dst, src and bytes
 // must be multiples of 16 (callers copy whole 256-byte frames).
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)

@@ -49,6 +49,25 @@ class Voltages(ctypes.Structure):
     ]
 
 
+class MultibeamConfig(ctypes.Structure):
+    _fields_ = [
+        ("ncc", ctypes.c_int),
+        ("nfine", ctypes.c_int),
+        ("nant", ctypes.c_int),
+        ("npointing", ctypes.c_int),
+        ("nsamples", ctypes.c_int),
+        ("nstokes", ctypes.c_int),
+        ("precision", ctypes.c_int),
+        ("input", ctypes.c_int),
+        ("invw", ctypes.c_float),
+    ]
+
+
+MB_SPLIT_BF16, MB_BF16, MB_FP16 = 0, 1, 2
+MB_INT4, MB_INT8 = 0, 1
+MB_INT = 10  # samples per integration
+
+
 class PipelineConfig(ctypes.Structure):
     _fields_ = [
         ("ncc", ctypes.c_int),
@@ -90,6 +109,13 @@ _SIGS = {
     "vgb_beamform_mwax_psrfits_noalloc": (I, [ctypes.POINTER(Voltages), I, I, V, I, I, U, V, I, Fl, I, V, V, V,
                                               V]),
     "vgb_gemm_bf16": (I, [V, V, V, I, I, I, V]),
+    "vgb_multibeam_create": (I, [V, V]),
+    "vgb_multibeam_destroy": (None, [V]),
+    "vgb_multibeam_set_geometry": (I, [V, V, V, V, V, V, ctypes.c_double, V]),
+    "vgb_multibeam_set_jones": (I, [V, V, V, V, V, V, V]),
+    "vgb_multibeam_run": (I, [V, V, V, V, V, V, V]),
+    "vgb_multibeam_launches": (I, [V]),
+    "vgb_gemm_batched": (I, [V, V, V, I, I, I, I, I, V]),
     "vgb_pipeline_create": (I, [ctypes.POINTER(PipelineConfig), ctypes.POINTER(V)]),
     "vgb_pipeline_destroy": (I, [V]),
     "vgb_pipeline_set_filters": (I, [V, V, V]),
@@ -190,6 +216,11 @@ def gemm_bf16(A, B, C, M, N, K, stream=None):
     check(lib().vgb_gemm_bf16(ptr(A), ptr(B), ptr(C), M, N, K, stream_ptr(stream)))
 
 
+def gemm_batched(A, B, C, M, N, K, batch, fp16=False, stream=None):
+    """C[b] = A[b] @ B[b]^T for b < batch (bf16, or fp16 operands; FP32 out)."""
+    check(lib().vgb_gemm_batched(ptr(A), ptr(B), ptr(C), M, N, K, batch, int(bool(fp16)), stream_ptr(stream)))
+
+
 def fpfb(v: Voltages, ncc, nspectra, filt, i_idx, flags, out, stream=None):
     check(lib().vgb_fpfb(ctypes.byref(v), ncc, nspectra, ptr(filt), NTAPS, NCHAN, ptr(i_idx), flags, ptr(out),
                          stream_ptr(stream)))
@@ -262,6 +293,48 @@ def filter_fp32_exact(h: np.ndarray) -> bool:
 # --------------------------------------------------------------------------
 # pipeline
 # --------------------------------------------------------------------------
+
+class Multibeam:
+    """Many-beam beamformer on the tensor cores (vgb_multibeam_*): tables on
+    the device, then voltages -> integrated Stokes (and 8-bit PSRFITS)."""
+
+    def __init__(self, ncc, nfine, nant, npointing, nsamples, nstokes=4, precision=MB_SPLIT_BF16, input=MB_INT4,
+                 invw=None):
+        cfg = MultibeamConfig(ncc=ncc, nfine=nfine, nant=nant, npointing=npointing, nsamples=nsamples,
+                              nstokes=nstokes, precision=precision, input=input,
+                              invw=float(invw if invw is not None else 1.0 / (2 * nant)))
+        h = V()
+        check(lib().vgb_multibeam_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+        self.cfg = cfg
+        self.nint = nsamples // MB_INT
+
+    def close(self):
+        if self.h:
+            lib().vgb_multibeam_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_geometry(self, unit, east, north, height, cable, href=0.0, stream=None):
+        check(lib().vgb_multibeam_set_geometry(self.h, ptr(unit), ptr(east), ptr(north), ptr(height), ptr(cable),
+                                               float(href), stream_ptr(stream)))
+
+    def set_jones(self, D, B, freqs, polQ, polP, stream=None):
+        check(lib().vgb_multibeam_set_jones(self.h, ptr(D), ptr(B), ptr(freqs), ptr(polQ), ptr(polP),
+                                            stream_ptr(stream)))
+
+    def run(self, v, S=None, out=None, offsets=None, scales=None, stream=None):
+        check(lib().vgb_multibeam_run(self.h, ptr(v), ptr(S), ptr(out), ptr(offsets), ptr(scales),
+                                      stream_ptr(stream)))
+
+    def launches(self) -> int:
+        return lib().vgb_multibeam_launches(self.h)
+
 
 class Pipeline:
     """One second of all coarse channels per step (vgb_pipeline_*)."""

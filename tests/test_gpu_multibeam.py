@@ -1,0 +1,155 @@
+"""The many-beam tensor-core beamformer (vgb_multibeam_*) against the FP64
+oracle chain: the reference's tables (vmCalcJ, vmCalcPhi), its beamformer
+per sample (vmApplyJ + vmBeamform, autocorrelations removed) and a sum over
+each 10-sample integration.
+
+Tolerances (largest |difference| over the largest |reference| of each Stokes
+parameter): split-BF16 weights 1e-3; single FP16 weights 4e-3; single BF16
+weights 3e-2 (reported, the mode exists to show what the split buys). The
+8-bit PSRFITS bytes are checked bit-exact against the oracle's renormalise of
+the library's own Stokes (the byte stage is integer-exact given its input).
+"""
+import numpy as np
+import pytest
+
+import synthetic as SY
+from helpers import dev, host, pol_lists, torch_cuda
+
+pytestmark = pytest.mark.gpu
+
+NINT = 10
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return torch_cuda()
+
+
+@pytest.fixture(scope="module")
+def vgb_mod(torch):
+    import vgb
+
+    vgb.lib()
+    return vgb
+
+
+def make_case(O, nant, npointing, nfine, ns, seed=1, int8=False, flag_tile=None, cc=0):
+    D = SY.calibration_jones(nant, nfine, seed=seed)
+    rng = np.random.default_rng(seed + 50)  # a per-channel ripple so D^-1 differs across channels
+    D = D * (1.0 + 0.05 * np.exp(2j * np.pi * rng.uniform(size=(nant, nfine, 1, 1))))
+    if flag_tile is not None:
+        D[flag_tile] = 0.0
+    B = SY.identity_beam(npointing, nant) + 0.05 * (1 + 1j) * O.gauss(seed + 100, npointing * nant * 4).reshape(
+        npointing, nant, 2, 2)
+    B = np.ascontiguousarray(B)
+    east, north, height, cable = SY.tile_layout(nant, seed=seed + 7)
+    side = int(np.ceil(np.sqrt(npointing)))
+    az, za = SY.grid_pointings(side, 0.02)
+    unit = np.ascontiguousarray(SY.unit_vectors(az[:npointing], za[:npointing]))
+    freqs = SY.fine_chan_freqs_hz(SY.coarse_chan_start_hz(cc))[:nfine].astype(np.float64)
+    polQ, polP = pol_lists(SY.legacy_input_order(nant))
+    if int8:
+        raw = O.gen_int8(seed + 5, ns * nfine * 2 * nant * 2, sigma_num=16).reshape(ns, nfine, 2 * nant, 2)
+        v_oracle = raw[..., 0].astype(np.float64) + 1j * raw[..., 1].astype(np.float64)
+        v_dev = raw.view(np.uint8)
+    else:
+        v_dev = O.gen_int4_bytes(seed + 5, ns * nfine * 2 * nant).reshape(ns, nfine, 2 * nant)
+        v_oracle = v_dev
+    return dict(D=D, B=B, east=east, north=north, height=height, cable=cable, unit=unit, freqs=freqs, polQ=polQ,
+                polP=polP, v_dev=np.ascontiguousarray(v_dev), v_oracle=v_oracle)
+
+
+def oracle_stokes(O, case, nstokes, invw):
+    """[c][p][st][t] float64: the reference's per-sample Stokes summed over
+    each integration."""
+    J = O.calc_j(case["D"], case["B"])
+    phi = O.calc_phi(case["unit"], case["east"], case["north"], case["height"], case["cable"], case["freqs"])
+    S, _ = O.beamform(case["v_oracle"], J, phi, case["polQ"], case["polP"], invw, nstokes=nstokes, want_e=False)
+    npnt, ns, nst, nc = S.shape
+    Si = S.astype(np.float64).reshape(npnt, ns // NINT, NINT, nst, nc).sum(axis=2)
+    return np.ascontiguousarray(Si.transpose(3, 0, 2, 1))
+
+
+def run_mb(vgb, torch, case, nant, npointing, nfine, ns, nstokes, precision, int8=False, invw=None, psrfits=False):
+    mb = vgb.Multibeam(1, nfine, nant, npointing, ns, nstokes=nstokes, precision=precision,
+                       input=vgb.MB_INT8 if int8 else vgb.MB_INT4, invw=invw)
+    mb.set_geometry(dev(case["unit"]), dev(case["east"]), dev(case["north"]), dev(case["height"]),
+                    dev(case["cable"]))
+    mb.set_jones(dev(case["D"]), dev(case["B"]), dev(case["freqs"]), dev(case["polQ"]), dev(case["polP"]))
+    nint = ns // NINT
+    S = torch.full((nfine * npointing * nstokes * nint,), float("nan"), dtype=torch.float32, device="cuda")
+    out = off = scl = None
+    if psrfits:
+        out = torch.empty(npointing * nint * nstokes * nfine, dtype=torch.uint8, device="cuda")
+        off = torch.empty(npointing * nstokes * nfine, dtype=torch.float32, device="cuda")
+        scl = torch.empty_like(off)
+    mb.run(dev(case["v_dev"]), S=S, out=out, offsets=off, scales=scl)
+    torch.cuda.synchronize()
+    assert vgb.check_device_status() == 0
+    res = dict(S=host(S).reshape(nfine, npointing, nstokes, nint), launches=mb.launches())
+    if psrfits:
+        res["out"] = host(out).reshape(npointing, nint, nstokes, nfine)
+        res["off"] = host(off).reshape(npointing, nstokes, nfine)
+        res["scl"] = host(scl).reshape(npointing, nstokes, nfine)
+    mb.close()
+    return res
+
+
+def stokes_err(S, ref):
+    return [float(np.abs(S[:, :, st] - ref[:, :, st]).max() / np.abs(ref[:, :, st]).max())
+            for st in range(ref.shape[2])]
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-3), (2, 4e-3), (1, 3e-2)])
+def test_multibeam_full_stokes(vgb_mod, torch, oracle_mod, precision, tol):
+    nant, npnt, nfine, ns = 32, 40, 4, 500
+    case = make_case(oracle_mod, nant, npnt, nfine, ns)
+    invw = 1.0 / (2 * nant)
+    ref = oracle_stokes(oracle_mod, case, 4, invw)
+    res = run_mb(vgb_mod, torch, case, nant, npnt, nfine, ns, 4, precision, invw=invw)
+    errs = stokes_err(res["S"], ref)
+    print("precision", precision, "Stokes errors", errs)
+    assert max(errs) < tol, errs
+    assert res["launches"] == 4
+
+
+def test_multibeam_split_beats_single(vgb_mod, torch, oracle_mod):
+    nant, npnt, nfine, ns = 32, 64, 2, 250
+    case = make_case(oracle_mod, nant, npnt, nfine, ns, seed=3)
+    ref = oracle_stokes(oracle_mod, case, 4, 1.0)
+    e_split = max(stokes_err(run_mb(vgb_mod, torch, case, nant, npnt, nfine, ns, 4, 0, invw=1.0)["S"], ref))
+    e_single = max(stokes_err(run_mb(vgb_mod, torch, case, nant, npnt, nfine, ns, 4, 1, invw=1.0)["S"], ref))
+    assert e_split * 10 < e_single, (e_split, e_single)
+
+
+def test_multibeam_stokes_i_int8_flagged(vgb_mod, torch, oracle_mod):
+    """8-bit voltages (coherencies split into exact FP16 halves), Stokes I
+    only, one tile flagged (D = 0 -> zero weight, jones.c:144-147), a sample
+    count that leaves the last tile partly used."""
+    nant, npnt, nfine, ns = 48, 33, 3, 370
+    case = make_case(oracle_mod, nant, npnt, nfine, ns, seed=9, int8=True, flag_tile=5)
+    invw = 1.0 / (2 * nant - 2)
+    ref = oracle_stokes(oracle_mod, case, 1, invw)
+    res = run_mb(vgb_mod, torch, case, nant, npnt, nfine, ns, 1, 0, int8=True, invw=invw)
+    errs = stokes_err(res["S"], ref)
+    assert max(errs) < 1e-3, errs
+
+
+def test_multibeam_psrfits_bytes(vgb_mod, torch, oracle_mod):
+    nant, npnt, nfine, ns = 32, 36, 40, 300
+    case = make_case(oracle_mod, nant, npnt, nfine, ns, seed=4)
+    res = run_mb(vgb_mod, torch, case, nant, npnt, nfine, ns, 4, 0, psrfits=True)
+    # oracle renormalise of the library's own Stokes, in the PSRFITS order [p][t][st][c]
+    S_pfits = np.ascontiguousarray(res["S"].transpose(1, 3, 2, 0))
+    off, scl, u8 = oracle_mod.renormalise(S_pfits)
+    assert np.array_equal(res["off"], off)
+    assert np.array_equal(res["scl"], scl)
+    assert np.array_equal(res["out"], u8)
+    assert res["launches"] == 5
+
+
+def test_multibeam_rejects_bad_config(vgb_mod):
+    with pytest.raises(vgb_mod.VGBError, match="multiple of 16"):
+        vgb_mod.Multibeam(1, 4, 20, 8, 100)
+    with pytest.raises(vgb_mod.VGBError, match="multiple of 10"):
+        vgb_mod.Multibeam(1, 4, 32, 8, 105)

@@ -8,7 +8,7 @@ from helpers import torch_cuda
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 128, 64), (256, 384, 512), (384, 256, 1024)])
+@pytest.mark.parametrize("M,N,K", [(128, 128, 64), (256, 384, 512), (384, 256, 1024), (128, 512, 192)])
 def test_gemm_bf16_matches_fp32_reference(M, N, K):
     torch = torch_cuda()
     import vgb
@@ -21,6 +21,25 @@ def test_gemm_bf16_matches_fp32_reference(M, N, K):
     torch.cuda.synchronize()
     assert vgb.check_device_status() == 0
     ref = A.float() @ B.float().T
+    err = (C - ref).abs().max().item() / ref.abs().max().item()
+    assert err < 1e-5, err
+
+
+@pytest.mark.parametrize("fp16", [False, True])
+def test_gemm_batched(fp16):
+    torch = torch_cuda()
+    import vgb
+
+    M, N, K, nb = 256, 256, 128, 3
+    dt = torch.float16 if fp16 else torch.bfloat16
+    g = torch.Generator(device="cuda").manual_seed(11 + fp16)
+    A = torch.randn(nb, M, K, device="cuda", generator=g).to(dt)
+    B = torch.randn(nb, N, K, device="cuda", generator=g).to(dt)
+    C = torch.full((nb, M, N), float("nan"), device="cuda")
+    vgb.gemm_batched(A, B, C, M, N, K, nb, fp16)
+    torch.cuda.synchronize()
+    assert vgb.check_device_status() == 0
+    ref = A.float() @ B.float().transpose(1, 2)
     err = (C - ref).abs().max().item() / ref.abs().max().item()
     assert err < 1e-5, err
 
