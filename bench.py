@@ -13,6 +13,11 @@ flush is needed); two distinct seconds stay resident and alternate.
   e2e    the same through the pipeline's host API: every step copies its
          second of voltages from pinned host memory to the device and its
          PSRFITS + VDIF products back
+  multibeam  the many-beam path (vgb_multibeam_*): 256 beams on 128 tiles
+         (8-bit, Stokes I) and 1024 beams on 256 tiles (4-bit, full Stokes),
+         1 ms integrations into 8-bit PSRFITS, one coarse channel-second per
+         step, in four weight precisions: split BF16 and single FP16/BF16 on
+         the tensor cores, FP32 on the CUDA cores (the plain baseline)
   --impl reference  the reference's CPU path timed on the host cores: the
          reference has no CPU implementation of its kernels, so this is the
          oracle's OpenMP FP32 transcription of them (oracle/oracle.c).
@@ -202,6 +207,7 @@ def reference_arm(args, rank, world):
         vals.append(dt)
     data_s = args.steps * args.ref_spectra / NSPEC / NCC
     value = data_s / total_dt
+
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total_dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
@@ -312,6 +318,10 @@ def gb300_arm(args, rank, local_rank, world):
                 "stage_ms": {"pfb_beam": stage[0], "renormalise": stage[1], "ipfb_vdif": stage[2],
                              "history": stage[3]}}
 
+    mb_section = None
+    if rank == 0 and not args.no_multibeam:
+        mb_section, mb_launches = multibeam_section(torch, vgb, SY, args.mb_iters)
+
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -321,11 +331,114 @@ def gb300_arm(args, rank, local_rank, world):
                        "l2": "inputs larger than L2: each step reads a different 15.7 GB second",
                        "resident_seconds": args.resident},
             "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+    if mb_section is not None:
+        mb_section["gpu_launches"] = mb_launches
+        line["multibeam"] = mb_section
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_line(args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
+
+
+# --------------------------------------------------------------------------
+# many-beam tensor-core path (beams on the tensor cores vs the FP32 CUDA cores)
+# --------------------------------------------------------------------------
+MB_CASES = {
+    # name: (tiles, beams, grid spacing deg, nstokes, 8-bit input, description)
+    "C3": (128, 256, 0.02, 1, True, "24 cc x 128 fine ch, 128 tiles x 2 pols, 8-bit voltages, 256 beams "
+                                    "(16x16 grid, 0.02 deg), Stokes I at 1 ms"),
+    "C4": (256, 1024, 0.02, 4, False, "24 cc x 128 fine ch, 256 tiles x 2 pols, 4-bit voltages, 1024 beams "
+                                      "(32x32 grid), full Stokes at 1 ms"),
+}
+MB_MODES = (("split_bf16", 0), ("fp16", 2), ("bf16", 1), ("fp32_cuda_cores", 3))
+
+
+def multibeam_section(torch, vgb, SY, iters: int):
+    """Each mode runs one coarse channel-second (128 fine channels x 10000
+    samples) per step through vgb_multibeam_run on device-resident voltages;
+    RTF counts 24 coarse channels per data-second. Stokes go to 8-bit PSRFITS
+    bytes (renormalise included)."""
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak_tf = float(peaks.get("bf16_tflops", 1900.0))
+    out = {}
+    launches = 0
+    for name, (nant, npnt, spacing, nst, int8, desc) in MB_CASES.items():
+        nfine, ns = K, 10000
+        D = SY.calibration_jones(nant, nfine)
+        Bj = SY.identity_beam(npnt, nant)
+        e, n, h, c = SY.tile_layout(nant)
+        side = int(round(np.sqrt(npnt)))
+        az, za = SY.grid_pointings(side, spacing)
+        unit = SY.unit_vectors(az, za)
+        freqs = SY.fine_chan_freqs_hz(SY.coarse_chan_start_hz(0))
+        polQ = np.arange(0, 2 * nant, 2, dtype=np.int32)
+        polP = polQ + 1
+        to = lambda a: torch.from_numpy(np.ascontiguousarray(
+            a.view(np.float64) if a.dtype == np.complex128 else a)).cuda()
+        nbytes = ns * nfine * 2 * nant * (2 if int8 else 1)
+        g = torch.Generator(device="cuda").manual_seed(77)
+        if int8:
+            v = torch.randn(nbytes, device="cuda", generator=g).mul_(16).round_().clamp_(-127, 127).to(torch.int8)
+        else:
+            re = torch.randn(nbytes, device="cuda", generator=g).mul_(2.5).round_().clamp_(-8, 7).to(torch.int32)
+            im = torch.randn(nbytes, device="cuda", generator=g).mul_(2.5).round_().clamp_(-8, 7).to(torch.int32)
+            v = (((re & 15) << 4) | (im & 15)).to(torch.uint8)
+        nint = ns // 10
+        psr = torch.empty(npnt * nint * nst * nfine, dtype=torch.uint8, device="cuda")
+        off = torch.empty(npnt * nst * nfine, device="cuda")
+        scl = torch.empty_like(off)
+        case = {"workload": desc, "step": "one coarse channel-second (128 fine channels x 10000 samples)",
+                "alg_tflop_per_cc_s": 32.0 * npnt * nant * ns * nfine / 1e12, "modes": {}}
+        for mode, prec in MB_MODES:
+            mb = vgb.Multibeam(1, nfine, nant, npnt, ns, nstokes=nst, precision=prec,
+                               input=vgb.MB_INT8 if int8 else vgb.MB_INT4)
+            mb.set_geometry(to(unit), to(e), to(n), to(h), to(c))
+            mb.set_jones(to(D), to(Bj), to(freqs), to(polQ), to(polP))
+            n_it = iters if prec != 3 else max(1, iters // 4)
+            for _ in range(2):
+                mb.run(v, out=psr, offsets=off, scales=scl)
+            torch.cuda.synchronize()
+            st = torch.cuda.current_stream()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(n_it):
+                mb.run(v, out=psr, offsets=off, scales=scl, stream=st)
+                launches += mb.launches()
+            e1.record(st)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / n_it
+            mb.enable_timing(True)
+            mb.run(v, out=psr, offsets=off, scales=scl, stream=st)
+            launches += mb.launches()
+            stages = mb.stage_ms()
+            mb.close()
+            if vgb.check_device_status() != 0:
+                raise RuntimeError("device status raised in the many-beam bench")
+            alg = case["alg_tflop_per_cc_s"]
+            beam_ms = stages["beam_gemm"]
+            entry = {"ms_per_cc_s": ms, "rtf_24cc": 1e3 / (NCC * ms), "stage_ms": stages,
+                     "beam_gemm_alg_tflops": alg / (beam_ms / 1e3)}
+            if prec != 3:
+                planes = 2 if prec == 0 else 1
+                mma_tf = alg * planes * 256 / 250 / (beam_ms / 1e3)
+                entry["roofline"] = {"kernel": "mb_beam_kernel", "bound": "tensor",
+                                     "achieved": alg / (beam_ms / 1e3), "peak": peak_tf, "unit": "TFLOP/s",
+                                     "frac": alg / (beam_ms / 1e3) / peak_tf,
+                                     "mma_issued_tflops": mma_tf, "mma_frac": mma_tf / peak_tf,
+                                     "peak_source": "measured" if "bf16_tflops" in peaks else "fallback"}
+            case["modes"][mode] = entry
+        m = case["modes"]
+        case["split_bf16_vs_fp32_cuda_cores"] = m["fp32_cuda_cores"]["ms_per_cc_s"] / m["split_bf16"]["ms_per_cc_s"]
+        case["fp16_vs_fp32_cuda_cores"] = m["fp32_cuda_cores"]["ms_per_cc_s"] / m["fp16"]["ms_per_cc_s"]
+        out[name] = case
+        del v, psr
+        torch.cuda.empty_cache()
+    return out, launches
 
 
 def main():
@@ -341,6 +454,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ref-spectra", type=int, default=400, help="reference arm: spectra per step")
+    ap.add_argument("--no-multibeam", action="store_true", help="skip the many-beam (C3/C4) section")
+    ap.add_argument("--mb-iters", type=int, default=5, help="many-beam timed runs per mode")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per beam_kernel launch from an ncu capture (profiles/)")
     args = ap.parse_args()

@@ -253,10 +253,12 @@ int vgb_gemm_batched(const void *A, const void *B, float *C, int M, int N, int K
  * the sum of the reference's 10 per-sample Stokes values.
  *
  * Precision modes: split BF16 weights (hi + lo, FP32 accumulate; within 1e-3
- * of the FP64 chain), single BF16, single FP16. Voltages are exact in all. */
+ * of the FP64 chain), single BF16, single FP16 on the tensor cores, and FP32
+ * weights on the CUDA cores. Voltages are exact in all. */
 #define VGB_MB_SPLIT_BF16 0
 #define VGB_MB_BF16 1
 #define VGB_MB_FP16 2
+#define VGB_MB_FP32 3 /* FP32 weights on the CUDA cores (no tensor cores): the plain baseline */
 #define VGB_MB_INT4 0 /* legacy 4+4-bit bytes, high nibble real (v_IDX order) */
 #define VGB_MB_INT8 1 /* int8 re, im pairs, same order */
 
@@ -294,6 +296,11 @@ int vgb_multibeam_run(vgb_multibeam *mb, const void *v, float *S, uint8_t *out, 
                       void *stream);
 /* Kernels the last vgb_multibeam_run launched. */
 int vgb_multibeam_launches(const vgb_multibeam *mb);
+/* Stage timing with CUDA events (off by default): ms[0..4] = weights,
+ * voltage conversion, autocorrelation GEMM, beam GEMM, renormalise of the
+ * last run, summed over coarse channels (waits for the run to finish). */
+int vgb_multibeam_enable_timing(vgb_multibeam *mb, int on);
+int vgb_multibeam_stage_ms(vgb_multibeam *mb, float *ms, int n);
 
 /* ---- streaming pipeline: one second of all coarse channels per step ---- */
 typedef struct vgb_pipeline vgb_pipeline;

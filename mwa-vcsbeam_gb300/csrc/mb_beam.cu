@@ -27,7 +27,8 @@
 // j in {C_QQ, C_PP, Re C_QP, Im C_QP}, st the Stokes parameter. It runs on the
 // FP16 tensor path (tc_gemm.cu): integrated coherencies of 4-bit voltages are
 // exact in FP16, those of 8-bit voltages are split into exact hi + lo halves,
-// and Q is split hi + lo with a power-of-two scale per row.
+// and Q carries a power-of-two scale per row (and, in the split mode, an FP16
+// lo half).
 //
 // The beam GEMM's epilogue reads the accumulators back with tcgen05.ld,
 // forms XX, YY, XY per sample across the four lanes that hold one beam,
@@ -53,10 +54,30 @@ constexpr int kMbN = 256;      // samples per MMA tile
 constexpr int kMbInt = 10;     // samples per integration (1 ms at 10 kHz)
 constexpr int kMbUsed = 250;   // samples of a tile that are used: 25 integrations
 constexpr int kMbNint = kMbUsed / kMbInt;
-constexpr int kMbStages = 3;
 constexpr int kMbBeamsPerTile = 32;  // 128 rows / 4
 constexpr int kMbThreads = 192;      // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr uint32_t kMbPolls = 1u << 26;
+
+// Per-row statistics for the 8-bit stage, gathered by the beam epilogues: the
+// minimum and maximum as order-preserving unsigned keys (atomicMin/Max), and
+// whether the row's first value is NaN. The reference's sequential scan
+// (form_beam.cpp:408-449) starts from the first value and compares with <, >:
+// a NaN there makes the result NaN, any other NaN is skipped; fminf/fmaxf over
+// the rest give the same extremes.
+__device__ __forceinline__ uint32_t fkey(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float fkey_inv(uint32_t k)
+{
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
+struct MbStats {
+    uint32_t *mn, *mx; // [nfine][B][nst] keys
+    uint32_t *nan0;    // [nfine][B][nst]: the row's first value is NaN
+};
 
 // ---------------------------------------------------------------------------
 // Tables
@@ -149,6 +170,10 @@ struct MbWeightArgs {
     uint16_t *Aw;         // [planes][nfine][Mrows][KA]
     __half *Aq;           // [nfine][Mq][Kq]
     float *qscale;        // [nfine][Mq]
+    float2 *W32;          // FP32 mode instead: W [nfine][Bp][2][A][2] complex
+    float *Q32;           //                    Q [nfine][Mq][4A]
+    MbStats stats;        // reset here for the run's rows
+    int B;
 };
 
 __device__ __forceinline__ float2 cmul32(float2 a, float2 b)
@@ -218,6 +243,11 @@ __global__ void __launch_bounds__(128) mb_weights_kernel(const MbWeightArgs w)
 {
     const int p = blockIdx.x, c = blockIdx.y;
     __shared__ float smax[4][4];
+    if (threadIdx.x < w.nst && p < w.B) {
+        const long long r = ((long long)c * w.B + p) * w.nst + threadIdx.x;
+        w.stats.mn[r] = 0xFFFFFFFFu;
+        w.stats.mx[r] = 0u;
+    }
     float mx[4] = {0.f, 0.f, 0.f, 0.f};
     for (int a = threadIdx.x; a < w.A; a += blockDim.x) {
         float2 J[4];
@@ -243,6 +273,30 @@ __global__ void __launch_bounds__(128) mb_weights_kernel(const MbWeightArgs w)
     }
     const double f = (double)(uint32_t)w.freq[c];
     const bool h16 = w.fp16 != 0;
+    if (w.W32) {
+        // FP32 CUDA-core mode: complex weights and unscaled Q rows
+        for (int a = threadIdx.x; a < w.A; a += blockDim.x) {
+            float2 J[4];
+            mb_jinv(w, c, p, a, J);
+            const double turns = w.dt[(long long)p * w.A + a] * f;
+            const float r = (float)(turns - rint(turns));
+            float sn, cs;
+            sincospif(2.f * r, &sn, &cs);
+            const float2 ph = make_float2(cs, sn);
+            for (int x = 0; x < 2; x++) {
+                float4 *d = reinterpret_cast<float4 *>(w.W32 + ((((long long)c * w.Bp + p) * 2 + x) * w.A + a) * 2);
+                const float2 w0 = cmul32(ph, J[2 * x]), w1 = cmul32(ph, J[2 * x + 1]);
+                *d = make_float4(w0.x, w0.y, w1.x, w1.y);
+            }
+            for (int st = 0; st < w.nst; st++) {
+                float q[4];
+                mb_qrow(J, st, q);
+                *reinterpret_cast<float4 *>(w.Q32 + ((long long)c * w.Mq + p * w.nst + st) * w.KA + 4 * a) =
+                    make_float4(q[0], q[1], q[2], q[3]);
+            }
+        }
+        return;
+    }
     for (int a = threadIdx.x; a < w.A; a += blockDim.x) {
         float2 J[4];
         mb_jinv(w, c, p, a, J);
@@ -288,14 +342,14 @@ __global__ void __launch_bounds__(128) mb_weights_kernel(const MbWeightArgs w)
             __half *row = w.Aq + ((long long)c * w.Mq + p * w.nst + st) * w.Kq;
             const uint2 H2 = make_uint2(hi[0] | ((uint32_t)hi[1] << 16), hi[2] | ((uint32_t)hi[3] << 16));
             const uint2 L2 = make_uint2(lo[0] | ((uint32_t)lo[1] << 16), lo[2] | ((uint32_t)lo[3] << 16));
-            // 4-bit voltages: [Q_hi | Q_lo] against [C]; 8-bit: [Q_hi | Q_hi | Q_lo] against [C_hi | C_lo]
+            // 4-bit voltages: [Q_hi (| Q_lo)] against [C]; 8-bit: [Q_hi | Q_hi (| Q_lo)] against [C_hi | C_lo]
             *reinterpret_cast<uint2 *>(row + 4 * a) = H2;
+            int k = w.KA;
             if (w.int8) {
-                *reinterpret_cast<uint2 *>(row + w.KA + 4 * a) = H2;
-                *reinterpret_cast<uint2 *>(row + 2 * w.KA + 4 * a) = L2;
-            } else {
-                *reinterpret_cast<uint2 *>(row + w.KA + 4 * a) = L2;
+                *reinterpret_cast<uint2 *>(row + k + 4 * a) = H2;
+                k += w.KA;
             }
+            if (w.planes == 2) *reinterpret_cast<uint2 *>(row + k + 4 * a) = L2;
         }
     }
 }
@@ -316,23 +370,35 @@ struct MbConvArgs {
 
 __device__ __forceinline__ int nib4(uint32_t x) { return ((int)(x << 28)) >> 28; }
 
+// One block per (integration, channel): the 10 voltage rows (2A inputs each)
+// are staged in shared memory with 16-byte loads, then each thread gathers its
+// tiles' (Q, P) inputs through polQ/polP.
 __global__ void __launch_bounds__(128) mb_convert_kernel(const MbConvArgs g)
 {
+    extern __shared__ uint4 conv_smem[];
+    uint8_t *rows = reinterpret_cast<uint8_t *>(conv_smem);
     const int t = blockIdx.x, c = blockIdx.y;
     const bool h16 = g.fp16 != 0;
+    const int rowbytes = g.ni * (g.int8 ? 2 : 1); // a multiple of 32 (nant % 16 == 0)
+    for (int k = 0; k < kMbInt; k++) {
+        const uint4 *src = reinterpret_cast<const uint4 *>(g.v + ((long long)(t * kMbInt + k) * g.nfine + c) * rowbytes);
+        for (int e = threadIdx.x; e < rowbytes / 16; e += blockDim.x)
+            conv_smem[(k * rowbytes) / 16 + e] = src[e];
+    }
+    __syncthreads();
     for (int a = threadIdx.x; a < g.A; a += blockDim.x) {
         const uint32_t iq = g.polQ[a], ip = g.polP[a];
         int cqq = 0, cpp = 0, cr = 0, ci = 0;
         for (int k = 0; k < kMbInt; k++) {
             const int s = t * kMbInt + k;
-            const long long base = ((long long)s * g.nfine + c) * g.ni;
+            const uint8_t *r = rows + k * rowbytes;
             int qr, qi, pr, pi;
             if (g.int8) {
-                const char2 vq = reinterpret_cast<const char2 *>(g.v)[base + iq];
-                const char2 vp = reinterpret_cast<const char2 *>(g.v)[base + ip];
+                const char2 vq = reinterpret_cast<const char2 *>(r)[iq];
+                const char2 vp = reinterpret_cast<const char2 *>(r)[ip];
                 qr = vq.x; qi = vq.y; pr = vp.x; pi = vp.y;
             } else {
-                const uint32_t bq = g.v[base + iq], bp = g.v[base + ip];
+                const uint32_t bq = r[iq], bp = r[ip];
                 qr = nib4(bq >> 4); qi = nib4(bq); pr = nib4(bp >> 4); pi = nib4(bp);
             }
             cqq += qr * qr + qi * qi;
@@ -362,10 +428,18 @@ __global__ void __launch_bounds__(128) mb_convert_kernel(const MbConvArgs g)
 // ---------------------------------------------------------------------------
 // The beam GEMM (persistent, one CTA per SM)
 // ---------------------------------------------------------------------------
-struct MbSmem {
-    uint8_t a[kMbStages][2][128 * 128]; // weight planes: 128 rows x 64 K (bf16/fp16)
-    uint8_t b[kMbStages][kMbN * 128];   // voltages: 256 samples x 64 K
-    uint64_t full[kMbStages], empty[kMbStages];
+// One ring stage: kPlanes weight tiles (128 rows x 64 K, bf16/fp16) and the
+// voltage tile (256 samples x 64 K); 192 KB of ring either way.
+template <int kPlanes> struct MbRing {
+    static constexpr int kTileA = 128 * 128;
+    static constexpr int kTileB = kMbN * 128;
+    static constexpr int kStage = kPlanes * kTileA + kTileB;
+    static constexpr int kStages = kPlanes == 2 ? 3 : 4;
+};
+
+template <int kPlanes> struct MbSmem {
+    uint8_t ring[MbRing<kPlanes>::kStages][MbRing<kPlanes>::kStage];
+    uint64_t full[MbRing<kPlanes>::kStages], empty[MbRing<kPlanes>::kStages];
     uint64_t tfull[2], tempty[2], drain;
     uint32_t tmem;
 };
@@ -378,6 +452,7 @@ struct MbBeamArgs {
     int Mq, nint_p;
     float invw;
     float *S;             // [nfine][B][nst][nint]
+    MbStats stats;
     unsigned *status;
 };
 
@@ -385,14 +460,17 @@ template <int kPlanes, bool kF16, int kNst>
 __global__ void __launch_bounds__(kMbThreads, 1)
     mb_beam_kernel(const __grid_constant__ CUtensorMap tw, const __grid_constant__ CUtensorMap tv, const MbBeamArgs g)
 {
+    using Ring = MbRing<kPlanes>;
+    constexpr int kStages = Ring::kStages;
     extern __shared__ uint8_t mb_raw[];
-    MbSmem &sm = *reinterpret_cast<MbSmem *>((reinterpret_cast<uintptr_t>(mb_raw) + 1023) & ~uintptr_t(1023));
+    MbSmem<kPlanes> &sm =
+        *reinterpret_cast<MbSmem<kPlanes> *>((reinterpret_cast<uintptr_t>(mb_raw) + 1023) & ~uintptr_t(1023));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
         prefetch_tmap(&tw);
         prefetch_tmap(&tv);
-        for (int s = 0; s < kMbStages; s++) {
+        for (int s = 0; s < kStages; s++) {
             mbar_init(&sm.full[s], 1);
             mbar_init(&sm.empty[s], 1);
         }
@@ -426,22 +504,23 @@ __global__ void __launch_bounds__(kMbThreads, 1)
                 const int arow = c * g.Mrows + m * 128;
                 const int brow = c * g.ns + n * kMbUsed;
                 for (int kc = 0; kc < g.nk; kc++, it++) {
-                    const int s = it % kMbStages;
-                    const uint32_t r = it / kMbStages;
+                    const int s = it % kStages;
+                    const uint32_t r = it / kStages;
                     if (r > 0 && !mbar_wait_bounded(&sm.empty[s], (r - 1) & 1, kMbPolls)) {
                         atomicOr(g.status, kErrWaitTimeout);
                         ok = false;
                         break;
                     }
-                    mbar_arrive_expect_tx(&sm.full[s], kPlanes * 128 * 128 + kMbN * 128);
-                    tma_load_2d(sm.a[s][0], &tw, kc * 64, arow, &sm.full[s]);
-                    if (kPlanes == 2) tma_load_2d(sm.a[s][1], &tw, kc * 64, arow + g.nfine * g.Mrows, &sm.full[s]);
-                    tma_load_2d(sm.b[s], &tv, kc * 64, brow, &sm.full[s]);
+                    uint8_t *st = sm.ring[s];
+                    mbar_arrive_expect_tx(&sm.full[s], Ring::kStage);
+                    tma_load_2d(st, &tw, kc * 64, arow, &sm.full[s]);
+                    if (kPlanes == 2) tma_load_2d(st + Ring::kTileA, &tw, kc * 64, arow + g.nfine * g.Mrows, &sm.full[s]);
+                    tma_load_2d(st + kPlanes * Ring::kTileA, &tv, kc * 64, brow, &sm.full[s]);
                 }
             }
             // every load issued must have landed before the CTA leaves
-            for (uint32_t k = (it > kMbStages ? it - kMbStages : 0); k < it; k++)
-                mbar_wait_bounded(&sm.full[k % kMbStages], (k / kMbStages) & 1, kMbPolls);
+            for (uint32_t k = (it > kStages ? it - kStages : 0); k < it; k++)
+                mbar_wait_bounded(&sm.full[k % kStages], (k / kStages) & 1, kMbPolls);
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -459,16 +538,17 @@ __global__ void __launch_bounds__(kMbThreads, 1)
                 tc_fence_after();
                 const uint32_t d = tmem + buf * kMbN;
                 for (int kc = 0; kc < g.nk; kc++, it++) {
-                    const int s = it % kMbStages;
-                    if (!mbar_wait_bounded(&sm.full[s], (it / kMbStages) & 1, kMbPolls)) {
+                    const int s = it % kStages;
+                    if (!mbar_wait_bounded(&sm.full[s], (it / kStages) & 1, kMbPolls)) {
                         atomicOr(g.status, kErrWaitTimeout);
                         ok = false;
                         break;
                     }
                     tc_fence_after();
-                    const uint64_t a0 = sdesc_sw128(smem_u32(sm.a[s][0]));
-                    const uint64_t a1 = sdesc_sw128(smem_u32(sm.a[s][1]));
-                    const uint64_t bd = sdesc_sw128(smem_u32(sm.b[s]));
+                    const uint32_t sa = smem_u32(sm.ring[s]);
+                    const uint64_t a0 = sdesc_sw128(sa);
+                    const uint64_t a1 = sdesc_sw128(sa + Ring::kTileA);
+                    const uint64_t bd = sdesc_sw128(sa + kPlanes * Ring::kTileA);
 #pragma unroll
                     for (int k = 0; k < 4; k++) {
                         tc_mma(d, sdesc_advance_k(a0, k), sdesc_advance_k(bd, k), idesc, (kc | k) != 0);
@@ -506,6 +586,7 @@ __global__ void __launch_bounds__(kMbThreads, 1)
 #pragma unroll
             for (int i = 0; i < kMbNint; i++) rv[i] = (writer && i < nv) ? g.R[rrow * g.nint_p + t0 + i] : 0.f;
             float *srow = g.S + (((long long)c * g.B + p) * kNst + st) * g.nint + t0;
+            float smin = __int_as_float(0x7f800000), smax = -__int_as_float(0x7f800000);
 
             if (!mbar_wait_bounded(&sm.tfull[buf], (tc >> 1) & 1, kMbPolls)) {
                 if (lane == 0) atomicOr(g.status, kErrWaitTimeout);
@@ -546,7 +627,13 @@ __global__ void __launch_bounds__(kMbThreads, 1)
                                 t1 += __shfl_xor_sync(0xffffffffu, t1, 2);
                                 val = t1;
                             }
-                            if (writer && ti < nv) srow[ti] = g.invw * (val - qs * rv[ti]);
+                            if (writer && ti < nv) {
+                                const float sv = g.invw * (val - qs * rv[ti]);
+                                srow[ti] = sv;
+                                smin = fminf(smin, sv);
+                                smax = fmaxf(smax, sv);
+                                if (ti == 0 && t0 == 0) g.stats.nan0[((long long)c * g.B + p) * kNst + st] = sv != sv;
+                            }
                             sq = pb = pc = 0.f;
                         }
                     }
@@ -555,6 +642,11 @@ __global__ void __launch_bounds__(kMbThreads, 1)
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&sm.tempty[buf]);
+            if (writer) {
+                const long long r = ((long long)c * g.B + p) * kNst + st;
+                atomicMin(&g.stats.mn[r], fkey(smin));
+                atomicMax(&g.stats.mx[r], fkey(smax));
+            }
         }
     }
     __syncwarp();
@@ -562,6 +654,191 @@ __global__ void __launch_bounds__(kMbThreads, 1)
     __syncthreads();
     tc_fence_after();
     if (warp == 0) tmem_dealloc(tmem, 512);
+}
+
+
+// ---------------------------------------------------------------------------
+// The plain FP32 CUDA-core beamformer: the same contraction, detection,
+// integration and autocorrelation removal with FP32 weights and FP32 FMAs
+// (no tensor cores). It is the baseline the tensor-core modes are measured
+// and checked against.
+// ---------------------------------------------------------------------------
+constexpr int kSimtBeams = 32;   // beams per CTA
+constexpr int kSimtSamp = 160;   // samples per CTA (16 integrations)
+constexpr int kSimtK = 16;       // tiles per K chunk (32 complex inputs)
+constexpr int kSimtRow = 33;     // padded smem row (float2)
+
+struct MbSimtArgs {
+    const float2 *W;      // [nfine][Bp][2][A][2]
+    const uint16_t *V;    // [nfine][ns][4A] bf16 (exact voltages)
+    const float *R;       // [nfine][Mq][nint_p]
+    int A, Bp, B, ns, nint, nint_p, Mq;
+    float invw;
+    float *S;             // [nfine][B][nst][nint]
+    MbStats stats;
+};
+
+// Thread: beams {bg, bg + 8} of its warp's 16 (x and y rows each) x one
+// integration of 10 samples; a warp covers 16 beams x 4 integrations.
+template <int kNst>
+__global__ void __launch_bounds__(256, 1) mb_simt_beam_kernel(const MbSimtArgs g)
+{
+    extern __shared__ float2 simt_smem[];
+    float2(*Ws)[kSimtRow] = reinterpret_cast<float2(*)[kSimtRow]>(simt_smem); // [2*beams][..]: row 2 * beam + x
+    float2(*Vs)[kSimtRow] = reinterpret_cast<float2(*)[kSimtRow]>(simt_smem + 2 * kSimtBeams * kSimtRow); // [samples]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int bg = lane & 7, ig = lane >> 3;
+    const int wb = warp & 1, ws = warp >> 1;
+    const int c = blockIdx.z;
+    const int p0 = blockIdx.y * kSimtBeams;
+    const int s0 = blockIdx.x * kSimtSamp;
+    const int lb[2] = {wb * 16 + bg, wb * 16 + bg + 8};   // local beams
+    const int ls = ws * 40 + ig * 10;                    // local first sample
+
+    float2 acc[2][2][10];
+#pragma unroll
+    for (int b = 0; b < 2; b++)
+#pragma unroll
+        for (int x = 0; x < 2; x++)
+#pragma unroll
+            for (int i = 0; i < 10; i++) acc[b][x][i] = make_float2(0.f, 0.f);
+
+    for (int a0 = 0; a0 < g.A; a0 += kSimtK) {
+        __syncthreads();
+        // weights: 64 rows x 32 complex, rows contiguous in global memory
+        for (int e = threadIdx.x; e < 2 * kSimtBeams * 2 * kSimtK; e += blockDim.x) {
+            const int r = e / (2 * kSimtK), k = e % (2 * kSimtK);
+            const int pb = r >> 1, x = r & 1;
+            Ws[r][k] = g.W[((((long long)c * g.Bp + p0 + pb) * 2 + x) * g.A + a0) * 2 + k];
+        }
+        // voltages: 160 samples x 32 complex (bf16 re, im pairs)
+        for (int e = threadIdx.x; e < kSimtSamp * 2 * kSimtK; e += blockDim.x) {
+            const int sl = e / (2 * kSimtK), k = e % (2 * kSimtK);
+            const int s = s0 + sl;
+            float2 v = make_float2(0.f, 0.f);
+            if (s < g.ns) {
+                const uint32_t u =
+                    *reinterpret_cast<const uint32_t *>(g.V + ((long long)c * g.ns + s) * (4 * g.A) + 4 * a0 + 2 * k);
+                v = make_float2(__uint_as_float(u << 16), __uint_as_float(u & 0xFFFF0000u));
+            }
+            Vs[sl][k] = v;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int k = 0; k < 2 * kSimtK; k++) {
+            float2 wv[2][2];
+#pragma unroll
+            for (int b = 0; b < 2; b++)
+#pragma unroll
+                for (int x = 0; x < 2; x++) wv[b][x] = Ws[2 * lb[b] + x][k];
+#pragma unroll
+            for (int i = 0; i < 10; i++) {
+                const float2 v = Vs[ls + i][k];
+#pragma unroll
+                for (int b = 0; b < 2; b++)
+#pragma unroll
+                    for (int x = 0; x < 2; x++) {
+                        acc[b][x][i].x = fmaf(wv[b][x].x, v.x, acc[b][x][i].x);
+                        acc[b][x][i].x = fmaf(-wv[b][x].y, v.y, acc[b][x][i].x);
+                        acc[b][x][i].y = fmaf(wv[b][x].x, v.y, acc[b][x][i].y);
+                        acc[b][x][i].y = fmaf(wv[b][x].y, v.x, acc[b][x][i].y);
+                    }
+            }
+        }
+    }
+    const int t = (s0 + ls) / kMbInt;
+    const bool tval = t < g.nint;
+#pragma unroll
+    for (int b = 0; b < 2; b++) {
+        const int p = p0 + lb[b];
+        float xx = 0.f, yy = 0.f, re = 0.f, im = 0.f;
+#pragma unroll
+        for (int i = 0; i < 10; i++) {
+            const float2 ex = acc[b][0][i], ey = acc[b][1][i];
+            xx = fmaf(ex.x, ex.x, fmaf(ex.y, ex.y, xx));
+            yy = fmaf(ey.x, ey.x, fmaf(ey.y, ey.y, yy));
+            re = fmaf(ex.x, ey.x, fmaf(ex.y, ey.y, re));
+            im = fmaf(ex.y, ey.x, fmaf(-ex.x, ey.y, im));
+        }
+        const float val[4] = {xx + yy, xx - yy, 2.f * re, -2.f * im};
+#pragma unroll
+        for (int st = 0; st < kNst; st++) {
+            const long long row = ((long long)c * g.B + p) * kNst + st;
+            float mn = __int_as_float(0x7f800000), mx = -__int_as_float(0x7f800000);
+            if (p < g.B && tval) {
+                const float r = g.R[((long long)c * g.Mq + p * kNst + st) * g.nint_p + t];
+                const float sv = g.invw * (val[st] - r);
+                g.S[row * g.nint + t] = sv;
+                if (t == 0) g.stats.nan0[row] = sv != sv;
+                mn = sv;
+                mx = sv;
+            }
+            // the four lanes of a beam group (different integrations) share a row
+            mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, 8));
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 8));
+            mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, 16));
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
+            if (ig == 0 && p < g.B) {
+                atomicMin(&g.stats.mn[row], fkey(mn));
+                atomicMax(&g.stats.mx[row], fkey(mx));
+            }
+        }
+    }
+}
+
+// R[c][row][t] = sum_k Q[c][row][k] Cint[c][t][k] in FP32 (64 x 64 tiles,
+// 4 x 4 per thread). The coherencies are read back from their exact FP16
+// halves.
+struct MbSimtAutoArgs {
+    const float *Q;       // [nfine][Mq][4A]
+    const __half *C;      // [nfine][nint_p][Kb]
+    int KA, Kb, Mq, nint, nint_p, int8;
+    float *R;             // [nfine][Mq][nint_p]
+};
+
+__global__ void __launch_bounds__(256) mb_simt_auto_kernel(const MbSimtAutoArgs g)
+{
+    __shared__ float Qs[16][65], Cs[16][65];
+    const int c = blockIdx.z;
+    const int r0 = blockIdx.y * 64, t0 = blockIdx.x * 64;
+    const int tr = threadIdx.x >> 4, tt = threadIdx.x & 15;
+    float acc[4][4] = {};
+    for (int k0 = 0; k0 < g.KA; k0 += 16) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < 64 * 16; e += 256) {
+            const int i = e >> 4, k = e & 15;
+            Qs[k][i] = g.Q[((long long)c * g.Mq + r0 + i) * g.KA + k0 + k];
+            const int t = t0 + i;
+            float cv = 0.f;
+            if (t < g.nint) {
+                const __half *row = g.C + ((long long)c * g.nint_p + t) * g.Kb;
+                cv = __half2float(row[k0 + k]);
+                if (g.int8) cv += __half2float(row[g.KA + k0 + k]);
+            }
+            Cs[k][i] = cv;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            float q[4], cv[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                q[i] = Qs[k][tr + 16 * i];
+                cv[i] = Cs[k][tt + 16 * i];
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[i][j] = fmaf(q[i], cv[j], acc[i][j]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int t = t0 + tt + 16 * j;
+            if (t < g.nint_p) g.R[((long long)c * g.Mq + r0 + tr + 16 * i) * g.nint_p + t] = acc[i][j];
+        }
 }
 
 // ---------------------------------------------------------------------------
@@ -575,57 +852,84 @@ struct MbRenormArgs {
     uint8_t *out;
     long long out_p, out_s, out_st;
     float *offsets, *scales; // [(p * nst + st) * nfine + c]
+    MbStats stats;
 };
 
+constexpr int kRnT = 128; // integrations per transpose chunk
+
+// Block: (32 channels, one beam and Stokes parameter). The row extremes come
+// from the beam epilogue (MbStats); one pass then quantises 128 integrations
+// at a time, packs four channels' bytes into a word, transposes in shared
+// memory and writes 16-byte runs of channels.
 __global__ void __launch_bounds__(256) mb_renorm_kernel(const MbRenormArgs a)
 {
     __shared__ float s_off[32], s_scl[32];
-    __shared__ uint8_t tileu[32][33];
+    __shared__ uint32_t tile[kRnT][9];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int c0 = blockIdx.x * 32;
     const int st = blockIdx.y % a.nst, p = blockIdx.y / a.nst;
-    for (int k = 0; k < 4; k++) {
-        const int cs = wid + 8 * k, c = c0 + cs;
-        if (c >= a.nfine) continue;
-        const float *row = a.S + (((long long)c * a.B + p) * a.nst + st) * a.nint;
-        const float s0 = row[0];
-        float mn = s0, mx = s0;
-        for (int t = lane; t < a.nint; t += 32) {
-            const float v = row[t];
-            mn = (v < mn ? v : mn);
-            mx = (v > mx ? v : mx);
+    if (threadIdx.x < 32) {
+        const int c = c0 + threadIdx.x;
+        float mn = 0.f, mx = 0.f;
+        if (c < a.nfine) {
+            const long long r = ((long long)c * a.B + p) * a.nst + st;
+            if (a.stats.nan0[r]) {
+                mn = mx = __int_as_float(0x7fffffff);
+            } else {
+                mn = fkey_inv(a.stats.mn[r]);
+                mx = fkey_inv(a.stats.mx[r]);
+            }
         }
-        for (int o = 16; o; o >>= 1) {
-            const float v0 = __shfl_xor_sync(0xffffffffu, mn, o), v1 = __shfl_xor_sync(0xffffffffu, mx, o);
-            mn = (v0 < mn ? v0 : mn);
-            mx = (v1 > mx ? v1 : mx);
-        }
-        if (lane == 0) {
-            const float scale = (float)((double)(mx - mn) / 256.0);
-            s_off[cs] = mn;
-            s_scl[cs] = scale;
+        const float scale = (float)((double)(mx - mn) / 256.0);
+        s_off[threadIdx.x] = mn;
+        s_scl[threadIdx.x] = scale;
+        if (c < a.nfine) {
             const long long si = ((long long)p * a.nst + st) * a.nfine + c;
             a.scales[si] = scale;
             a.offsets[si] = mn;
         }
     }
     __syncthreads();
-    for (int t0 = 0; t0 < a.nint; t0 += 32) {
-        for (int k = 0; k < 4; k++) {
-            const int cs = wid + 8 * k, c = c0 + cs, t = t0 + lane;
-            uint8_t u = 0;
-            if (c < a.nfine && t < a.nint) {
-                const float v = (a.S[(((long long)c * a.B + p) * a.nst + st) * a.nint + t] - s_off[cs]) / s_scl[cs];
-                u = sat_u8((double)v + 0.5);
-            }
-            tileu[lane][cs] = u;
+    // warp w: channels 4w .. 4w+3 of the block
+    const float *rows[4];
+    float off[4], scl[4], rcp[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int c = c0 + 4 * wid + k;
+        rows[k] = a.S + (((long long)(c < a.nfine ? c : c0) * a.B + p) * a.nst + st) * a.nint;
+        off[k] = s_off[4 * wid + k];
+        scl[k] = s_scl[4 * wid + k];
+        rcp[k] = 1.f / scl[k];
+    }
+    const bool wide = ((a.out_s | a.out_st | a.out_p) & 15) == 0 &&
+                      (reinterpret_cast<uintptr_t>(a.out) & 15) == 0 && c0 + 32 <= a.nfine;
+    for (int t0 = 0; t0 < a.nint; t0 += kRnT) {
+        float e[4][4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int t = t0 + lane + 32 * j;
+#pragma unroll
+            for (int k = 0; k < 4; k++) e[j][k] = t < a.nint ? rows[k][t] : 0.f;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            uint32_t w = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) w |= (uint32_t)quant_u8(e[j][k], off[k], scl[k], rcp[k]) << (8 * k);
+            tile[lane + 32 * j][wid] = w;
         }
         __syncthreads();
-        const int t = t0 + (threadIdx.x >> 3), cg = (threadIdx.x & 7) * 4;
+        const int tl = threadIdx.x >> 1, h = threadIdx.x & 1, t = t0 + tl;
         if (t < a.nint) {
-            uint8_t *o = a.out + p * a.out_p + (long long)t * a.out_s + st * a.out_st + c0 + cg;
-            for (int k = 0; k < 4; k++)
-                if (c0 + cg + k < a.nfine) o[k] = tileu[threadIdx.x >> 3][cg + k];
+            uint8_t *o = a.out + p * a.out_p + (long long)t * a.out_s + st * a.out_st + c0 + 16 * h;
+            const uint4 v = make_uint4(tile[tl][4 * h], tile[tl][4 * h + 1], tile[tl][4 * h + 2], tile[tl][4 * h + 3]);
+            if (wide) {
+                *reinterpret_cast<uint4 *>(o) = v;
+            } else {
+                const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+                for (int q = 0; q < 16; q++)
+                    if (c0 + 16 * h + q < a.nfine) o[q] = (uint8_t)(w4[q >> 2] >> (8 * (q & 3)));
+            }
         }
         __syncthreads();
     }
@@ -648,10 +952,15 @@ struct vgb_multibeam {
     uint16_t *d_Aw = nullptr, *d_V = nullptr;
     __half *d_Aq = nullptr, *d_C = nullptr;
     float *d_qscale = nullptr, *d_R = nullptr, *d_S = nullptr;
+    float2 *d_W32 = nullptr; // FP32 mode weights
+    float *d_Q32 = nullptr;
+    uint32_t *d_stats = nullptr; // min keys, max keys, first-is-NaN: 3 x [nfine][B][nst]
+    bool simt = false;
     CUtensorMap tmW, tmV;
     bool have_geometry = false, have_jones = false;
     int nsm = 0;
     int last_launches = 0; // kernels the last run launched
+    cudaEvent_t *ev = nullptr; // timing: 6 events per coarse channel (stage boundaries)
 };
 
 namespace {
@@ -668,8 +977,14 @@ template <typename T> int mb_alloc(T **p, size_t n, const char *what)
 
 void mb_free(vgb_multibeam *mb)
 {
+    if (mb->ev) {
+        for (int i = 0; i < 6 * mb->cfg.ncc; i++)
+            if (mb->ev[i]) cudaEventDestroy(mb->ev[i]);
+        delete[] mb->ev;
+        mb->ev = nullptr;
+    }
     void *ptrs[] = {mb->d_dt, mb->d_Binv, mb->d_H, mb->d_Dinv, mb->d_G, mb->d_freq, mb->d_polQ, mb->d_polP,
-                    mb->d_Aw, mb->d_V, mb->d_Aq, mb->d_C, mb->d_qscale, mb->d_R, mb->d_S};
+                    mb->d_Aw, mb->d_V, mb->d_Aq, mb->d_C, mb->d_qscale, mb->d_R, mb->d_S, mb->d_W32, mb->d_Q32, mb->d_stats};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -677,7 +992,7 @@ void mb_free(vgb_multibeam *mb)
 template <int kPlanes, bool kF16, int kNst> int mb_launch_beam(vgb_multibeam *mb, const MbBeamArgs &a, cudaStream_t st)
 {
     auto kern = mb_beam_kernel<kPlanes, kF16, kNst>;
-    const int smem = (int)sizeof(MbSmem) + 1024;
+    const int smem = (int)sizeof(MbSmem<kPlanes>) + 1024;
     int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
                         "cudaFuncSetAttribute(mb_beam_kernel)");
     if (rc) return rc;
@@ -695,13 +1010,15 @@ extern "C" int vgb_multibeam_create(const vgb_multibeam_config *cfg, vgb_multibe
     const vgb_multibeam_config &c = *cfg;
     if (c.ncc <= 0 || c.nfine <= 0 || c.nfine > 4096)
         return set_error(VGB_ERR_INVALID, "multibeam: ncc and nfine must be positive (nfine <= 4096)");
-    if (c.nant <= 0 || c.nant % 16)
-        return set_error(VGB_ERR_INVALID, "multibeam: nant must be a positive multiple of 16 (got %d)", c.nant);
+    if (c.nant <= 0 || c.nant % 16 || c.nant > 2048)
+        return set_error(VGB_ERR_INVALID, "multibeam: nant must be a positive multiple of 16, at most 2048 (got %d)",
+                         c.nant);
     if (c.npointing <= 0) return set_error(VGB_ERR_INVALID, "multibeam: npointing must be positive");
     if (c.nsamples <= 0 || c.nsamples % kMbInt)
         return set_error(VGB_ERR_INVALID, "multibeam: nsamples must be a positive multiple of %d", kMbInt);
     if (c.nstokes != 1 && c.nstokes != 4) return set_error(VGB_ERR_INVALID, "multibeam: nstokes must be 1 or 4");
-    if (c.precision != VGB_MB_SPLIT_BF16 && c.precision != VGB_MB_BF16 && c.precision != VGB_MB_FP16)
+    if (c.precision != VGB_MB_SPLIT_BF16 && c.precision != VGB_MB_BF16 && c.precision != VGB_MB_FP16 &&
+        c.precision != VGB_MB_FP32)
         return set_error(VGB_ERR_UNSUPPORTED, "multibeam: unknown precision %d", c.precision);
     if (c.input != VGB_MB_INT4 && c.input != VGB_MB_INT8)
         return set_error(VGB_ERR_UNSUPPORTED, "multibeam: unknown input format %d", c.input);
@@ -716,12 +1033,15 @@ extern "C" int vgb_multibeam_create(const vgb_multibeam_config *cfg, vgb_multibe
     mb->KA = 4 * c.nant;
     mb->nk = mb->KA / 64;
     mb->int8 = c.input == VGB_MB_INT8;
+    mb->planes = c.precision == VGB_MB_SPLIT_BF16 ? 2 : 1;
+    // autocorrelation GEMM operands: [Q_hi (| Q_lo)] x [C] for 4-bit voltages,
+    // [Q_hi | Q_hi (| Q_lo)] x [C_hi | C_lo] for 8-bit (Q_lo only in the split mode)
     mb->Kb = mb->int8 ? 8 * c.nant : 4 * c.nant;
-    mb->Kq = mb->int8 ? 12 * c.nant : 8 * c.nant;
+    mb->Kq = (mb->int8 ? 8 * c.nant : 4 * c.nant) + (mb->planes == 2 ? 4 * c.nant : 0);
     mb->nint = c.nsamples / kMbInt;
     mb->nint_p = (mb->nint + 127) / 128 * 128;
-    mb->planes = c.precision == VGB_MB_SPLIT_BF16 ? 2 : 1;
     mb->fp16 = c.precision == VGB_MB_FP16;
+    mb->simt = c.precision == VGB_MB_FP32;
     mb->ntn = (c.nsamples + kMbUsed - 1) / kMbUsed;
     int dev = 0;
     cudaGetDevice(&dev);
@@ -738,17 +1058,21 @@ extern "C" int vgb_multibeam_create(const vgb_multibeam_config *cfg, vgb_multibe
     if (!rc) rc = mb_alloc(&mb->d_freq, (size_t)c.ncc * nf, "frequencies");
     if (!rc) rc = mb_alloc(&mb->d_polQ, A, "polQ");
     if (!rc) rc = mb_alloc(&mb->d_polP, A, "polP");
-    if (!rc) rc = mb_alloc(&mb->d_Aw, (size_t)mb->planes * nf * mb->Mrows * mb->KA, "weights");
+    if (!rc && !mb->simt) rc = mb_alloc(&mb->d_Aw, (size_t)mb->planes * nf * mb->Mrows * mb->KA, "weights");
+    if (!rc && mb->simt) rc = mb_alloc(&mb->d_W32, nf * mb->Bp * 2 * A * 2, "FP32 weights");
+    if (!rc && mb->simt) rc = mb_alloc(&mb->d_Q32, nf * mb->Mq * mb->KA, "FP32 autocorrelation weights");
+    if (!rc && mb->simt) rc = check_cuda(cudaMemset(mb->d_Q32, 0, nf * mb->Mq * mb->KA * sizeof(float)), "cudaMemset");
     if (!rc) rc = mb_alloc(&mb->d_V, nf * c.nsamples * mb->KA, "voltages");
     if (!rc) rc = mb_alloc(&mb->d_Aq, nf * mb->Mq * mb->Kq, "autocorrelation weights");
     if (!rc) rc = mb_alloc(&mb->d_C, nf * mb->nint_p * mb->Kb, "coherencies");
     if (!rc) rc = mb_alloc(&mb->d_qscale, nf * mb->Mq, "row scales");
     if (!rc) rc = mb_alloc(&mb->d_R, nf * mb->Mq * mb->nint_p, "autocorrelation terms");
     if (!rc) rc = mb_alloc(&mb->d_S, nf * c.npointing * c.nstokes * mb->nint, "Stokes");
+    if (!rc) rc = mb_alloc(&mb->d_stats, 3 * nf * c.npointing * c.nstokes, "row statistics");
     if (!rc)
         rc = check_cuda(cudaMemset(mb->d_Aq, 0, nf * mb->Mq * mb->Kq * sizeof(__half)), "cudaMemset");
     if (!rc) rc = check_cuda(cudaMemset(mb->d_C, 0, nf * mb->nint_p * mb->Kb * sizeof(__half)), "cudaMemset");
-    if (!rc)
+    if (!rc && !mb->simt)
         rc = make_tmap_bf16(&mb->tmW, mb->d_Aw, (uint64_t)mb->planes * nf * mb->Mrows, mb->KA, (uint64_t)mb->KA * 2,
                             128, mb->fp16);
     if (!rc)
@@ -826,6 +1150,7 @@ extern "C" int vgb_multibeam_run(vgb_multibeam *mb, const void *v, float *S, uin
                                  float *scales, void *stream)
 {
     if (!mb || !v) return set_error(VGB_ERR_INVALID, "multibeam_run: NULL argument");
+    if (reinterpret_cast<uintptr_t>(v) & 15) return set_error(VGB_ERR_INVALID, "multibeam_run: v must be 16-byte aligned");
     if (!mb->have_geometry || !mb->have_jones)
         return set_error(VGB_ERR_STATE, "multibeam_run: set_geometry and set_jones must come first");
     if (out && (!offsets || !scales))
@@ -837,10 +1162,16 @@ extern "C" int vgb_multibeam_run(vgb_multibeam *mb, const void *v, float *S, uin
     const int A = c.nant, nf = c.nfine, ns = c.nsamples;
     const long long vbytes_cc = (long long)ns * nf * 2 * A * (mb->int8 ? 2 : 1);
     const long long s_cc = (long long)nf * c.npointing * c.nstokes * mb->nint;
+    const long long nrow = (long long)nf * c.npointing * c.nstokes;
+    const MbStats stats{mb->d_stats, mb->d_stats + nrow, mb->d_stats + 2 * nrow};
     int rc = VGB_SUCCESS;
     mb->last_launches = 0;
+    auto mark = [&](int cc, int i) {
+        if (mb->ev && !rc) rc = check_cuda(cudaEventRecord(mb->ev[6 * cc + i], st), "cudaEventRecord");
+    };
     for (int cc = 0; cc < c.ncc && !rc; cc++) {
         mb->last_launches += out ? 5 : 4;
+        mark(cc, 0);
         MbWeightArgs w{};
         w.dt = mb->d_dt;
         w.Binv = mb->d_Binv + 2ll * cc * mb->Bp * A;
@@ -862,8 +1193,13 @@ extern "C" int vgb_multibeam_run(vgb_multibeam *mb, const void *v, float *S, uin
         w.Aw = mb->d_Aw;
         w.Aq = mb->d_Aq;
         w.qscale = mb->d_qscale;
+        w.W32 = mb->d_W32;
+        w.Q32 = mb->d_Q32;
+        w.stats = stats;
+        w.B = c.npointing;
         mb_weights_kernel<<<dim3(mb->Bp, nf), 128, 0, st>>>(w);
         if ((rc = check_launch("mb_weights_kernel"))) break;
+        mark(cc, 1);
 
         MbConvArgs g{};
         g.v = static_cast<const uint8_t *>(v) + cc * vbytes_cc;
@@ -880,11 +1216,55 @@ extern "C" int vgb_multibeam_run(vgb_multibeam *mb, const void *v, float *S, uin
         g.polP = mb->d_polP;
         g.V = mb->d_V;
         g.C = mb->d_C;
-        mb_convert_kernel<<<dim3(mb->nint, nf), 128, 0, st>>>(g);
+        const int conv_smem = kMbInt * 2 * A * (mb->int8 ? 2 : 1);
+        if ((rc = check_cuda(cudaFuncSetAttribute(mb_convert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  conv_smem),
+                             "cudaFuncSetAttribute(mb_convert_kernel)")))
+            break;
+        mb_convert_kernel<<<dim3(mb->nint, nf), 128, conv_smem, st>>>(g);
         if ((rc = check_launch("mb_convert_kernel"))) break;
+        mark(cc, 2);
 
+        if (mb->simt) {
+            MbSimtAutoArgs q{};
+            q.Q = mb->d_Q32;
+            q.C = mb->d_C;
+            q.KA = mb->KA;
+            q.Kb = mb->Kb;
+            q.Mq = mb->Mq;
+            q.nint = mb->nint;
+            q.nint_p = mb->nint_p;
+            q.int8 = mb->int8;
+            q.R = mb->d_R;
+            mb_simt_auto_kernel<<<dim3(mb->nint_p / 64, mb->Mq / 64, nf), 256, 0, st>>>(q);
+            if ((rc = check_launch("mb_simt_auto_kernel"))) break;
+            mark(cc, 3);
+            MbSimtArgs b{};
+            b.W = mb->d_W32;
+            b.V = mb->d_V;
+            b.R = mb->d_R;
+            b.A = A;
+            b.Bp = mb->Bp;
+            b.B = c.npointing;
+            b.ns = ns;
+            b.nint = mb->nint;
+            b.nint_p = mb->nint_p;
+            b.Mq = mb->Mq;
+            b.invw = c.invw;
+            b.S = S ? S + cc * s_cc : mb->d_S;
+            b.stats = stats;
+            const dim3 grid((ns + kSimtSamp - 1) / kSimtSamp, mb->Bp / kSimtBeams, nf);
+            const int smem = (2 * kSimtBeams + kSimtSamp) * kSimtRow * (int)sizeof(float2);
+            auto kern = c.nstokes == 4 ? mb_simt_beam_kernel<4> : mb_simt_beam_kernel<1>;
+            if ((rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                                 "cudaFuncSetAttribute(mb_simt_beam_kernel)")))
+                break;
+            kern<<<grid, 256, smem, st>>>(b);
+            if ((rc = check_launch("mb_simt_beam_kernel"))) break;
+        } else {
         // autocorrelation terms R = Q C^T per channel (FP16 tensor path)
         if ((rc = gemm_batched(mb->d_Aq, mb->d_C, mb->d_R, mb->Mq, mb->nint_p, mb->Kq, nf, true, st, mb->Kb))) break;
+        mark(cc, 3);
 
         MbBeamArgs b{};
         b.nfine = nf;
@@ -902,6 +1282,7 @@ extern "C" int vgb_multibeam_run(vgb_multibeam *mb, const void *v, float *S, uin
         b.nint_p = mb->nint_p;
         b.invw = c.invw;
         b.S = S ? S + cc * s_cc : mb->d_S;
+        b.stats = stats;
         b.status = status;
         if (mb->planes == 2)
             rc = c.nstokes == 4 ? mb_launch_beam<2, false, 4>(mb, b, st) : mb_launch_beam<2, false, 1>(mb, b, st);
@@ -910,10 +1291,13 @@ extern "C" int vgb_multibeam_run(vgb_multibeam *mb, const void *v, float *S, uin
         else
             rc = c.nstokes == 4 ? mb_launch_beam<1, false, 4>(mb, b, st) : mb_launch_beam<1, false, 1>(mb, b, st);
         if (rc) break;
+        }
 
+        mark(cc, 4);
         if (out) {
             MbRenormArgs r{};
-            r.S = b.S;
+            r.S = S ? S + cc * s_cc : mb->d_S;
+            r.stats = stats;
             r.nfine = nf;
             r.B = c.npointing;
             r.nst = c.nstokes;
@@ -929,8 +1313,47 @@ extern "C" int vgb_multibeam_run(vgb_multibeam *mb, const void *v, float *S, uin
             mb_renorm_kernel<<<dim3((nf + 31) / 32, c.npointing * c.nstokes), 256, 0, st>>>(r);
             rc = check_launch("mb_renorm_kernel");
         }
+        mark(cc, 5);
     }
     return rc;
+}
+
+extern "C" int vgb_multibeam_enable_timing(vgb_multibeam *mb, int on)
+{
+    if (!mb) return set_error(VGB_ERR_INVALID, "multibeam_enable_timing: NULL handle");
+    if (on && !mb->ev) {
+        mb->ev = new cudaEvent_t[6 * mb->cfg.ncc]();
+        for (int i = 0; i < 6 * mb->cfg.ncc; i++)
+            if (cudaEventCreate(&mb->ev[i]) != cudaSuccess) {
+                cudaGetLastError();
+                return set_error(VGB_ERR_CUDA, "multibeam_enable_timing: cudaEventCreate failed");
+            }
+    } else if (!on && mb->ev) {
+        for (int i = 0; i < 6 * mb->cfg.ncc; i++)
+            if (mb->ev[i]) cudaEventDestroy(mb->ev[i]);
+        delete[] mb->ev;
+        mb->ev = nullptr;
+    }
+    return VGB_SUCCESS;
+}
+
+extern "C" int vgb_multibeam_stage_ms(vgb_multibeam *mb, float *ms, int n)
+{
+    if (!mb || !ms || n < 5) return set_error(VGB_ERR_INVALID, "multibeam_stage_ms: need 5 slots");
+    if (!mb->ev) return set_error(VGB_ERR_STATE, "multibeam_stage_ms: timing is off");
+    for (int i = 0; i < 5; i++) ms[i] = 0.f;
+    for (int cc = 0; cc < mb->cfg.ncc; cc++) {
+        int rc = check_cuda(cudaEventSynchronize(mb->ev[6 * cc + 5]), "cudaEventSynchronize");
+        if (rc) return rc;
+        for (int i = 0; i < 5; i++) {
+            float t = 0.f;
+            if ((rc = check_cuda(cudaEventElapsedTime(&t, mb->ev[6 * cc + i], mb->ev[6 * cc + i + 1]),
+                                 "cudaEventElapsedTime")))
+                return rc;
+            ms[i] += t;
+        }
+    }
+    return VGB_SUCCESS;
 }
 
 extern "C" int vgb_multibeam_launches(const vgb_multibeam *mb)

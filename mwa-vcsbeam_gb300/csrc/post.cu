@@ -166,10 +166,8 @@ __global__ void __launch_bounds__(256) renorm_kernel(const RenormArgs a)
     const float offset = mn;
     if (live) {
         uint8_t *o = a.out + cc * a.out_cc + p * a.out_p + st * a.out_st + c;
-        for (int s = wid; s < a.nstep; s += 8) {
-            const float v = (S[s * sstride] - offset) / scale;
-            o[s * a.out_s] = sat_u8((double)v + 0.5);
-        }
+        const float rcp = 1.f / scale;
+        for (int s = wid; s < a.nstep; s += 8) o[s * a.out_s] = quant_u8(S[s * sstride], offset, scale, rcp);
         if (wid == 0) {
             const long long si = cc * a.stat_cc + ((long long)p * a.nstokes + st) * a.nchan + c;
             a.scales[si] = scale;

@@ -113,6 +113,42 @@ __device__ __forceinline__ uint8_t sat_u8(double t)
     return (uint8_t)((unsigned)t & 0xFFu);
 }
 
+// sat_u8((double)v + 0.5) without FP64 arithmetic on the common path: for
+// |v| < 2^22 a float's spacing is at most 1/4, so v + 0.5f is exact and equal
+// to the double sum; larger magnitudes, infinities and NaN take the FP64 path.
+__device__ __forceinline__ uint8_t sat_u8_half(float v)
+{
+    if (fabsf(v) < 4194304.f) {
+        const float t = v + 0.5f;
+        return t <= 0.f ? (uint8_t)0 : (uint8_t)((unsigned)t & 0xFFu);
+    }
+    return sat_u8((double)v + 0.5);
+}
+
+// The reference's byte for one value, (uint8_t)((e - off) / scl + 0.5) with
+// the division correctly rounded, without a division on the common path.
+// With rcp = 1/scl (correctly rounded), q0 = x * rcp is within 1.5 ulp of
+// the true quotient, so for |q0| < 512 it differs from the correctly rounded
+// quotient q by less than 2^-12. The byte is floor(q + 1/2), which changes
+// only at half-integers; when q0 lies further than 2^-12 from every
+// half-integer, q lies in the same interval and the byte is q0 rounded to the
+// nearest integer (read from the low bits of q0 + 1.5 * 2^23). Otherwise, and
+// for out-of-range or non-finite values, the division itself is used.
+__device__ __forceinline__ uint8_t quant_u8(float e, float off, float scl, float rcp)
+{
+    const float x = __fsub_rn(e, off);
+    const float q0 = __fmul_rn(x, rcp);
+    if (fabsf(q0) < 512.f) {
+        const float y = __fadd_rn(q0, 12582912.f);
+        const float n = __fsub_rn(y, 12582912.f);
+        if (fabsf(__fsub_rn(q0, n)) < 0.499755859375f) { // 1/2 - 2^-12
+            const int ni = (int)(__float_as_uint(y) & 0x7FFFFFu) - 4194304;
+            return ni > 0 ? (uint8_t)(ni & 0xFF) : (uint8_t)0;
+        }
+    }
+    return sat_u8_half(x / scl);
+}
+
 // 1-D bulk copy global -> shared through the TMA unit. dst, src and bytes
 // must be multiples of 16 (callers copy whole 256-byte frames).
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)

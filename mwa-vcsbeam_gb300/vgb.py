@@ -63,7 +63,7 @@ class MultibeamConfig(ctypes.Structure):
     ]
 
 
-MB_SPLIT_BF16, MB_BF16, MB_FP16 = 0, 1, 2
+MB_SPLIT_BF16, MB_BF16, MB_FP16, MB_FP32 = 0, 1, 2, 3
 MB_INT4, MB_INT8 = 0, 1
 MB_INT = 10  # samples per integration
 
@@ -115,6 +115,8 @@ _SIGS = {
     "vgb_multibeam_set_jones": (I, [V, V, V, V, V, V, V]),
     "vgb_multibeam_run": (I, [V, V, V, V, V, V, V]),
     "vgb_multibeam_launches": (I, [V]),
+    "vgb_multibeam_enable_timing": (I, [V, I]),
+    "vgb_multibeam_stage_ms": (I, [V, V, I]),
     "vgb_gemm_batched": (I, [V, V, V, I, I, I, I, I, V]),
     "vgb_pipeline_create": (I, [ctypes.POINTER(PipelineConfig), ctypes.POINTER(V)]),
     "vgb_pipeline_destroy": (I, [V]),
@@ -334,6 +336,16 @@ class Multibeam:
 
     def launches(self) -> int:
         return lib().vgb_multibeam_launches(self.h)
+
+    def enable_timing(self, on=True):
+        check(lib().vgb_multibeam_enable_timing(self.h, int(bool(on))))
+
+    STAGES = ("weights", "convert", "autocorr_gemm", "beam_gemm", "renormalise")
+
+    def stage_ms(self) -> dict:
+        ms = (ctypes.c_float * 5)()
+        check(lib().vgb_multibeam_stage_ms(self.h, ms, 5))
+        return dict(zip(self.STAGES, [float(x) for x in ms]))
 
 
 class Pipeline:

@@ -47,6 +47,27 @@ def test_renormalise_matches_reference_kernel(vgb_mod, torch, golden):
     assert np.array_equal(u8[0], golden["rn_u8"])
 
 
+def test_renormalise_rounding_boundaries(vgb_mod, torch, oracle_mod):
+    """Values whose scaled quotient lies within a few ulps of every
+    half-integer (where the byte changes), plus the wrap at the maximum: the
+    division-free fast path must agree with the reference's divide bit for
+    bit."""
+    rng = np.random.default_rng(17)
+    nstep, nc = 4000, K
+    scale = np.float32(10.0 ** rng.uniform(-3, 3, size=nc)).astype(np.float32)
+    k = rng.integers(0, 257, size=(nstep, nc))
+    target = ((k + 0.5) * scale.astype(np.float64)).astype(np.float32)
+    bits = target.view(np.int32) + rng.integers(-4, 5, size=target.shape).astype(np.int32)
+    S = bits.view(np.float32).copy()
+    S[0] = 0.0                                          # row minimum
+    S[1] = (256.0 * scale.astype(np.float64)).astype(np.float32)   # row maximum
+    S = np.ascontiguousarray(S.reshape(1, 1, nstep, 1, nc))
+    off, sc, u8 = renorm(vgb_mod, torch, S)
+    o, s_, u = oracle_mod.renormalise(S[0])
+    assert np.array_equal(off[0], o) and np.array_equal(sc[0], s_)
+    assert np.array_equal(u8[0], u)
+
+
 def test_renormalise_spliced_layout(vgb_mod, torch, oracle_mod):
     """Two coarse channels written straight into spliced PSRFITS rows
     [s][stokes][cc*128 + c] (no gather step)."""
