@@ -354,7 +354,7 @@ MB_CASES = {
 MB_MODES = (("split_bf16", 0), ("fp16", 2), ("bf16", 1), ("fp32_cuda_cores", 3))
 
 
-def multibeam_section(torch, vgb, SY, iters: int):
+def multibeam_section(torch, vgb, SY, iters: int, cases=None, modes=None, nfine=K):
     """Each mode runs one coarse channel-second (128 fine channels x 10000
     samples) per step through vgb_multibeam_run on device-resident voltages;
     RTF counts 24 coarse channels per data-second. Stokes go to 8-bit PSRFITS
@@ -368,14 +368,16 @@ def multibeam_section(torch, vgb, SY, iters: int):
     out = {}
     launches = 0
     for name, (nant, npnt, spacing, nst, int8, desc) in MB_CASES.items():
-        nfine, ns = K, 10000
+        if cases and name not in cases:
+            continue
+        ns = 10000
         D = SY.calibration_jones(nant, nfine)
         Bj = SY.identity_beam(npnt, nant)
         e, n, h, c = SY.tile_layout(nant)
         side = int(round(np.sqrt(npnt)))
         az, za = SY.grid_pointings(side, spacing)
         unit = SY.unit_vectors(az, za)
-        freqs = SY.fine_chan_freqs_hz(SY.coarse_chan_start_hz(0))
+        freqs = SY.fine_chan_freqs_hz(SY.coarse_chan_start_hz(0))[:nfine]
         polQ = np.arange(0, 2 * nant, 2, dtype=np.int32)
         polP = polQ + 1
         to = lambda a: torch.from_numpy(np.ascontiguousarray(
@@ -392,9 +394,11 @@ def multibeam_section(torch, vgb, SY, iters: int):
         psr = torch.empty(npnt * nint * nst * nfine, dtype=torch.uint8, device="cuda")
         off = torch.empty(npnt * nst * nfine, device="cuda")
         scl = torch.empty_like(off)
-        case = {"workload": desc, "step": "one coarse channel-second (128 fine channels x 10000 samples)",
+        case = {"workload": desc, "step": f"one coarse channel-second ({nfine} fine channels x 10000 samples)",
                 "alg_tflop_per_cc_s": 32.0 * npnt * nant * ns * nfine / 1e12, "modes": {}}
         for mode, prec in MB_MODES:
+            if modes and mode not in modes:
+                continue
             mb = vgb.Multibeam(1, nfine, nant, npnt, ns, nstokes=nst, precision=prec,
                                input=vgb.MB_INT8 if int8 else vgb.MB_INT4)
             mb.set_geometry(to(unit), to(e), to(n), to(h), to(c))
@@ -433,8 +437,10 @@ def multibeam_section(torch, vgb, SY, iters: int):
                                      "peak_source": "measured" if "bf16_tflops" in peaks else "fallback"}
             case["modes"][mode] = entry
         m = case["modes"]
-        case["split_bf16_vs_fp32_cuda_cores"] = m["fp32_cuda_cores"]["ms_per_cc_s"] / m["split_bf16"]["ms_per_cc_s"]
-        case["fp16_vs_fp32_cuda_cores"] = m["fp32_cuda_cores"]["ms_per_cc_s"] / m["fp16"]["ms_per_cc_s"]
+        if "fp32_cuda_cores" in m and "split_bf16" in m:
+            case["split_bf16_vs_fp32_cuda_cores"] = m["fp32_cuda_cores"]["ms_per_cc_s"] / m["split_bf16"]["ms_per_cc_s"]
+        if "fp32_cuda_cores" in m and "fp16" in m:
+            case["fp16_vs_fp32_cuda_cores"] = m["fp32_cuda_cores"]["ms_per_cc_s"] / m["fp16"]["ms_per_cc_s"]
         out[name] = case
         del v, psr
         torch.cuda.empty_cache()
@@ -456,11 +462,27 @@ def main():
     ap.add_argument("--ref-spectra", type=int, default=400, help="reference arm: spectra per step")
     ap.add_argument("--no-multibeam", action="store_true", help="skip the many-beam (C3/C4) section")
     ap.add_argument("--mb-iters", type=int, default=5, help="many-beam timed runs per mode")
+    ap.add_argument("--mb-only", default=None, help="profiling: run only these many-beam cases (e.g. C4 or C3,C4) "
+                    "and print their JSON; no bench line")
+    ap.add_argument("--mb-modes", default=None, help="profiling: comma-separated precision modes")
+    ap.add_argument("--mb-nfine", type=int, default=K, help="profiling: fine channels per case")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per beam_kernel launch from an ncu capture (profiles/)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, local_rank, world = dist_env()
+    if args.mb_only:
+        import torch
+
+        import synthetic as SY
+        import vgb
+
+        vgb.lib()
+        sec, nl = multibeam_section(torch, vgb, SY, args.mb_iters, cases=args.mb_only.split(","),
+                                    modes=args.mb_modes.split(",") if args.mb_modes else None, nfine=args.mb_nfine)
+        sec["gpu_launches"] = nl
+        print(json.dumps(sec), flush=True)
+        return
     if args.impl == "reference":
         reference_arm(args, rank, world)
     else:

@@ -242,6 +242,46 @@ int vgb_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, v
 int vgb_gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, int batch, int fp16,
                      void *stream);
 
+/* ---- table inputs on the host: calibration solutions, filter files ----
+ * D layout: [nant][nfine][2][2] complex double (D_IDX, vcsbeam.h.in:242-251). */
+
+/* Offringa binary solution of one coarse channel (vmLoadOffringaSolution,
+ * calibration.c:426-582). ncc = coarse channels in the solution's request
+ * (mpi_size there); nchan_cal = calibration fine channels per coarse channel
+ * (the file's own count wins when it differs); each calibration channel fills
+ * nfine / nchan_cal fine channels; NaN matrices become zero. counts (nullable)
+ * receives the header's interval, antenna, channel and polarisation counts. */
+int vgb_cal_load_offringa(const char *path, int coarse_chan_idx, int ncc, int nant, int nchan_cal, int nfine,
+                          double *D, uint32_t *counts);
+
+/* RTS solution of one coarse channel (vmLoadRTSSolution, calibration.c:51-225):
+ * DIJones file, optional Bandpass file (NULL: DIJones only), D = Dd Db A^-1
+ * reversed into the (q, p) basis. cal_ant[a] = index of observation antenna
+ * a in the calibration solution (matching tile, calibration.c:165-166). */
+int vgb_cal_load_rts(const char *dijones_path, const char *bandpass_path, int nant_cal, int nchan_cal,
+                     int chan_width_hz, const int *cal_ant, int nant, int nfine, double *D);
+
+/* vmApplyCalibrationCorrections (calibration.c:747-882): rotate phases
+ * against antenna ref_ant (< 0: off), zero PQ/QP unless keep_cross_terms,
+ * multiply the first column by exp(i (slope f + offset)). */
+int vgb_cal_apply_corrections(double *D, int nant, int nfine, int ref_ant, int keep_cross_terms,
+                              double phase_slope, double phase_offset, long long chan_start_hz,
+                              int coarse_chan_width_hz);
+
+/* pq_phase_correction.txt lookup for a GPS second
+ * (parse_calibration_correction_file, calibration.c:663-745); ref_tile gets
+ * the reference tile name or "NONE". */
+int vgb_cal_pq_correction(const char *path, uint32_t gpstime, double *slope, double *offset, char *ref_tile,
+                          int ref_tile_len, int *found);
+
+/* Zero D of the listed antennas (vmSetCustomTileFlags, calibration.c:952-1013). */
+int vgb_cal_flag_tiles(double *D, int nant, int nfine, const int *ants, int nflags);
+
+/* Filter coefficients from an ASCII file, scaled (vmLoadFilter +
+ * vmScaleFilterCoeffs, filter.c:62-165). coeffs may be NULL to count. */
+int vgb_load_filter(const char *path, int nchans, double scale, double *coeffs, int max_coeffs, int *ncoeffs,
+                    int *ntaps);
+
 /* ---- many-beam beamformer on the tensor cores ----
  *
  * Replaces, for npointing > 1, the per-pointing loop of vmBeamformChunk

@@ -46,7 +46,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_v: bool = False) -> 
     os.makedirs(LIBDIR, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers += [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
-    common = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
+    common = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
               "-I", os.path.join(ROOT, "include"), "-I", CSRC]
     if ptxas_v:
         common += ["-Xptxas", "-v"]

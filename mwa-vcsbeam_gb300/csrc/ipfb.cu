@@ -24,7 +24,7 @@
 namespace vgb {
 
 constexpr int kIFT = 32;                 // frames per CTA
-constexpr int kIRows = 2 * (kIFT + kP - 1); // transforms per CTA (86)
+
 constexpr int kIRowsPad = 96;            // padded to whole warps of groups
 
 

@@ -109,6 +109,12 @@ _SIGS = {
     "vgb_beamform_mwax_psrfits_noalloc": (I, [ctypes.POINTER(Voltages), I, I, V, I, I, U, V, I, Fl, I, V, V, V,
                                               V]),
     "vgb_gemm_bf16": (I, [V, V, V, I, I, I, V]),
+    "vgb_cal_load_offringa": (I, [ctypes.c_char_p, I, I, I, I, I, V, V]),
+    "vgb_cal_load_rts": (I, [ctypes.c_char_p, ctypes.c_char_p, I, I, I, V, I, I, V]),
+    "vgb_cal_apply_corrections": (I, [V, I, I, I, I, ctypes.c_double, ctypes.c_double, LL, I]),
+    "vgb_cal_pq_correction": (I, [ctypes.c_char_p, ctypes.c_uint32, V, V, V, I, V]),
+    "vgb_cal_flag_tiles": (I, [V, I, I, V, I]),
+    "vgb_load_filter": (I, [ctypes.c_char_p, I, ctypes.c_double, V, I, V, V]),
     "vgb_multibeam_create": (I, [V, V]),
     "vgb_multibeam_destroy": (None, [V]),
     "vgb_multibeam_set_geometry": (I, [V, V, V, V, V, V, ctypes.c_double, V]),
@@ -295,6 +301,66 @@ def filter_fp32_exact(h: np.ndarray) -> bool:
 # --------------------------------------------------------------------------
 # pipeline
 # --------------------------------------------------------------------------
+
+# --------------------------------------------------------------------------
+# table inputs on the host (calibration solutions, filter files)
+# --------------------------------------------------------------------------
+def _enc(p):
+    return None if p is None else os.fsencode(p)
+
+
+def cal_load_offringa(path, coarse_chan_idx, ncc, nant, nchan_cal, nfine):
+    """D complex128 [nant][nfine][2][2] and the header counts."""
+    D = np.zeros((nant, nfine, 2, 2), dtype=np.complex128)
+    counts = np.zeros(4, dtype=np.uint32)
+    check(lib().vgb_cal_load_offringa(_enc(path), coarse_chan_idx, ncc, nant, nchan_cal, nfine, D.ctypes.data,
+                                      counts.ctypes.data))
+    return D, counts
+
+
+def cal_load_rts(dijones_path, bandpass_path, nant_cal, nchan_cal, chan_width_hz, cal_ant, nfine):
+    cal_ant = np.ascontiguousarray(cal_ant, dtype=np.int32)
+    D = np.zeros((cal_ant.size, nfine, 2, 2), dtype=np.complex128)
+    check(lib().vgb_cal_load_rts(_enc(dijones_path), _enc(bandpass_path), nant_cal, nchan_cal, chan_width_hz,
+                                 cal_ant.ctypes.data, cal_ant.size, nfine, D.ctypes.data))
+    return D
+
+
+def cal_apply_corrections(D, ref_ant=-1, keep_cross_terms=False, phase_slope=0.0, phase_offset=0.0,
+                          chan_start_hz=0, coarse_chan_width_hz=1280000):
+    """In place on a C-contiguous complex128 [nant][nfine][2][2] array."""
+    assert D.dtype == np.complex128 and D.flags.c_contiguous
+    check(lib().vgb_cal_apply_corrections(D.ctypes.data, D.shape[0], D.shape[1], int(ref_ant),
+                                          int(bool(keep_cross_terms)), float(phase_slope), float(phase_offset),
+                                          int(chan_start_hz), int(coarse_chan_width_hz)))
+    return D
+
+
+def cal_pq_correction(path, gpstime):
+    slope, offset = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    found = ctypes.c_int(0)
+    name = ctypes.create_string_buffer(32)
+    check(lib().vgb_cal_pq_correction(_enc(path), gpstime, ctypes.byref(slope), ctypes.byref(offset), name, 32,
+                                      ctypes.byref(found)))
+    return bool(found.value), slope.value, offset.value, name.value.decode()
+
+
+def cal_flag_tiles(D, ants):
+    ants = np.ascontiguousarray(ants, dtype=np.int32)
+    assert D.dtype == np.complex128 and D.flags.c_contiguous
+    check(lib().vgb_cal_flag_tiles(D.ctypes.data, D.shape[0], D.shape[1], ants.ctypes.data, ants.size))
+    return D
+
+
+def load_filter(path, nchans=NCHAN, scale=1.0):
+    """(coefficients float64, ntaps) from an ASCII filter file."""
+    n, t = ctypes.c_int(0), ctypes.c_int(0)
+    check(lib().vgb_load_filter(_enc(path), nchans, float(scale), None, 0, ctypes.byref(n), ctypes.byref(t)))
+    out = np.empty(n.value, dtype=np.float64)
+    check(lib().vgb_load_filter(_enc(path), nchans, float(scale), out.ctypes.data, out.size, ctypes.byref(n),
+                                ctypes.byref(t)))
+    return out, t.value
+
 
 class Multibeam:
     """Many-beam beamformer on the tensor cores (vgb_multibeam_*): tables on

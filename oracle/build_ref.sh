@@ -8,8 +8,11 @@
 #   oracle/_ref/include/vcsbeam.h   configured from include/vcsbeam.h.in
 #   oracle/_ref/ref_pfb.cubin       device code of src/pfb.cpp       (sm_103a)
 #   oracle/_ref/ref_form_beam.cubin device code of src/form_beam.cpp (sm_103a)
-#   oracle/_ref/libref_host.so      src/jones.c, src/filter.c, src/geometry.c
+#   oracle/_ref/libref_host.so      src/jones.c, src/filter.c, src/geometry.c,
+#                                   src/calibration.c
 #                                   + oracle/ref_host_shim.c (host, this machine)
+#   oracle/_ref/runtime/            RUNTIME_DIR: links to the reference's
+#                                   pfb_filter/*.dat and pq_phase_correction.txt
 #
 # The cubins travel to a GPU machine with the repository; there
 # oracle/ref_harness.cu (built by __graft_entry__.build()) loads them with the
@@ -26,11 +29,14 @@ if [ ! -f "$REF/src/pfb.cpp" ]; then
     echo "build_ref.sh: reference sources not found at $REF; nothing to build"
     exit 0
 fi
-mkdir -p "$OUT/include"
+mkdir -p "$OUT/include" "$OUT/runtime"
+for f in "$REF"/pfb_filter/*.dat "$REF/pq_phase_correction.txt"; do
+    [ -f "$f" ] && ln -sf "$f" "$OUT/runtime/$(basename "$f")"
+done
 
 # include/vcsbeam.h.in -> vcsbeam.h (the three #cmakedefine lines only)
 sed -e "s|^#cmakedefine VCSBEAM_VERSION.*|#define VCSBEAM_VERSION \"reference\"|" \
-    -e "s|^#cmakedefine RUNTIME_DIR.*|#define RUNTIME_DIR \"$REF/pfb_filter\"|" \
+    -e "s|^#cmakedefine RUNTIME_DIR.*|#define RUNTIME_DIR \"$OUT/runtime\"|" \
     -e "s|^#cmakedefine HYPERBEAM_HDF5.*|#define HYPERBEAM_HDF5 \"\"|" \
     "$REF/include/vcsbeam.h.in" > "$OUT/include/vcsbeam.h"
 
@@ -45,7 +51,7 @@ done
 
 # Host C (table builders) for CPU-side pinning of the oracle.
 gcc -O2 -fPIC -shared -D__NVCC__ -w "${INC[@]}" \
-    "$REF/src/jones.c" "$REF/src/filter.c" "$REF/src/geometry.c" \
+    "$REF/src/jones.c" "$REF/src/filter.c" "$REF/src/geometry.c" "$REF/src/calibration.c" \
     "$HERE/ref_host_shim.c" \
     -o "$OUT/libref_host.so" -L"$CUDA_HOME/lib64" -lcudart -lm &
 wait

@@ -87,6 +87,155 @@ int refhost_load_filter(char *name, int synthesis, int nchans, double scale,
     return nc;
 }
 
+/* ---- calibration.c (vmLoadOffringaSolution, vmLoadRTSSolution,
+ * vmApplyCalibrationCorrections, parse_calibration_correction_file) driven
+ * through a vcsbeam_context populated with the fields those routines read:
+ * antenna a's RF inputs are 2a ('X') and 2a+1 ('Y'), tile ids 1000 + a in the
+ * calibration metadata and 1000 + cal_ant[a] in the target observation. ---- */
+typedef struct {
+    MetafitsMetadata meta;
+    Rfinput *inputs;
+    Antenna *ants;
+    char **names;
+    CoarseChannel cc[32];
+} refh_meta;
+
+static void refh_meta_init(refh_meta *m, int nant, int nchan_cal, int chan_width_hz, const int *tile_of_ant)
+{
+    memset(m, 0, sizeof(*m));
+    m->inputs = (Rfinput *)calloc(2 * nant, sizeof(Rfinput));
+    m->ants = (Antenna *)calloc(nant, sizeof(Antenna));
+    m->names = (char **)calloc(nant, sizeof(char *));
+    for (int a = 0; a < nant; a++) {
+        m->names[a] = (char *)malloc(16);
+        snprintf(m->names[a], 16, "Tile%03d", tile_of_ant ? tile_of_ant[a] : a);
+        m->ants[a].ant = a;
+        m->ants[a].tile_name = m->names[a];
+        m->ants[a].tile_id = 1000 + (tile_of_ant ? tile_of_ant[a] : a);
+        for (int p = 0; p < 2; p++) {
+            Rfinput *r = &m->inputs[2 * a + p];
+            r->input = 2 * a + p;
+            r->ant = a;
+            r->tile_id = m->ants[a].tile_id;
+            r->tile_name = m->names[a];
+            r->pol = p ? "Y" : "X";
+        }
+    }
+    m->meta.num_ants = nant;
+    m->meta.antennas = m->ants;
+    m->meta.rf_inputs = m->inputs;
+    m->meta.num_rf_inputs = 2 * nant;
+    m->meta.num_ant_pols = 2;
+    m->meta.num_visibility_pols = 4;
+    m->meta.num_metafits_coarse_chans = 24;
+    m->meta.metafits_coarse_chans = m->cc;
+    m->meta.coarse_chan_width_hz = 1280000;
+    m->meta.num_corr_fine_chans_per_coarse = nchan_cal;
+    m->meta.corr_fine_chan_width_hz = chan_width_hz;
+    m->meta.num_volt_fine_chans_per_coarse = 128;
+}
+
+static void refh_meta_free(refh_meta *m, int nant)
+{
+    for (int a = 0; a < nant; a++) free(m->names[a]);
+    free(m->names);
+    free(m->ants);
+    free(m->inputs);
+}
+
+void refhost_load_offringa(char *path, int coarse_chan_idx, int mpi_size, int nant, int nchan_cal, int nfine,
+                           double *D)
+{
+    refh_meta cal;
+    refh_meta_init(&cal, nant, nchan_cal, 1280000 / nchan_cal, NULL);
+    vcsbeam_context vm;
+    memset(&vm, 0, sizeof(vm));
+    vm.cal.caldir = path;
+    vm.cal_coarse_chan_idxs_to_process = &coarse_chan_idx;
+    vm.cal_metadata = &cal.meta;
+    vm.mpi_size = mpi_size;
+    vm.nfine_chan = nfine;
+    vm.D = (gpuDoubleComplex *)D;
+    vmLoadOffringaSolution(&vm);
+    refh_meta_free(&cal, nant);
+}
+
+void refhost_load_rts(char *caldir, int use_bandpass, int corr_chan_number, int nant, int nchan_cal,
+                      int chan_width_hz, const int *cal_ant, int nfine, double *D)
+{
+    refh_meta cal, obs;
+    refh_meta_init(&cal, nant, nchan_cal, chan_width_hz, NULL);
+    refh_meta_init(&obs, nant, nchan_cal, chan_width_hz, cal_ant);
+    cal.cc[0].corr_chan_number = corr_chan_number;
+    vcsbeam_context vm;
+    memset(&vm, 0, sizeof(vm));
+    vm.cal.caldir = caldir;
+    vm.cal.use_bandpass = use_bandpass;
+    vm.coarse_chan_idx = 0;
+    vm.cal_metadata = &cal.meta;
+    vm.obs_metadata = &obs.meta;
+    vm.nfine_chan = nfine;
+    vm.D = (gpuDoubleComplex *)D;
+    vmLoadRTSSolution(&vm);
+    refh_meta_free(&cal, nant);
+    refh_meta_free(&obs, nant);
+}
+
+void refhost_apply_corrections(double *D, int nant, int nfine, int ref_ant, int keep_cross_terms, double slope,
+                               double offset, unsigned chan_start_hz)
+{
+    refh_meta obs;
+    refh_meta_init(&obs, nant, 128, 10000, NULL);
+    obs.cc[0].chan_start_hz = chan_start_hz;
+    char name[16] = "NONE";
+    if (ref_ant >= 0) snprintf(name, sizeof(name), "Tile%03d", ref_ant);
+    vcsbeam_context vm;
+    memset(&vm, 0, sizeof(vm));
+    vm.cal.ref_ant = name;
+    vm.cal.keep_cross_terms = keep_cross_terms;
+    vm.cal.phase_slope = slope;
+    vm.cal.phase_offset = offset;
+    vm.coarse_chan_idx = 0;
+    vm.obs_metadata = &obs.meta;
+    vm.nfine_chan = nfine;
+    vm.D = (gpuDoubleComplex *)D;
+    vmApplyCalibrationCorrections(&vm);
+    refh_meta_free(&obs, nant);
+}
+
+/* RUNTIME_DIR/pq_phase_correction.txt for one GPS second; found = the
+ * returned reference tile is not "NONE". */
+int refhost_pq_correction(unsigned gpstime, double *slope, double *offset, char *ref_tile, int len)
+{
+    calibration cal;
+    memset(&cal, 0, sizeof(cal));
+    parse_calibration_correction_file(gpstime, &cal);
+    *slope = cal.phase_slope;
+    *offset = cal.phase_offset;
+    snprintf(ref_tile, len, "%s", cal.ref_ant);
+    int found = strcmp(cal.ref_ant, "NONE") != 0;
+    free(cal.ref_ant);
+    return found;
+}
+
+/* metadata.c helpers calibration.c calls (same matching rules). */
+Rfinput *find_matching_rf_input(MetafitsMetadata *metadata, Rfinput *rfinput)
+{
+    for (uintptr_t i = 0; i < metadata->num_rf_inputs; i++)
+        if (rfinput->tile_id == metadata->rf_inputs[i].tile_id && *(rfinput->pol) == *(metadata->rf_inputs[i].pol))
+            return &(metadata->rf_inputs[i]);
+    return NULL;
+}
+Antenna *find_antenna_by_name(MetafitsMetadata *obs_metadata, char *tile_name)
+{
+    for (int i = 0; i < (int)obs_metadata->num_ants; i++)
+        if (strcmp(tile_name, obs_metadata->antennas[i].tile_name) == 0) return &(obs_metadata->antennas[i]);
+    return NULL;
+}
+void logger_timed_message(logger *log, const char *message) { (void)log; (void)message; }
+void logger_message(logger *log, const char *message) { (void)log; (void)message; }
+void vmSetNumNotFlaggedRFInputs(vcsbeam_context *vm) { (void)vm; }
+
 /* The reference host code names these; the harness never reaches them. */
 static void refhost_unreachable(const char *what)
 {

@@ -92,6 +92,9 @@ typedef struct MetafitsMetadata {
     uint32_t coarse_chan_width_hz;
     uint32_t num_delays;
     uint32_t *delays;
+    size_t num_corr_fine_chans_per_coarse;
+    uint32_t corr_fine_chan_width_hz;
+    size_t num_volt_fine_chans_per_coarse;
 } MetafitsMetadata;
 
 typedef struct VoltageMetadata {
