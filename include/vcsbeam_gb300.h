@@ -282,6 +282,64 @@ int vgb_cal_flag_tiles(double *D, int nant, int nfine, const int *ants, int nfla
 int vgb_load_filter(const char *path, int nchans, double scale, double *coeffs, int max_coeffs, int *ncoeffs,
                     int *ntaps);
 
+/* ---- primary beam (vmCalcB, primary_beam.c:79-191) ----
+ * B [nfreq][npointing][ntile][2][2] complex double = J P on the device, FP64:
+ * J the analytic MWA tile model (4 x 4 dipoles over a ground plane with the
+ * tile beamformer delays; the reference's FEE model is not available to this
+ * build), P the parallactic-angle rotation at `latitude` (primary_beam.c:
+ * 436-456) when pa_correction != 0. az, za [npointing] radians; freq_hz
+ * [nfreq]; delays [ntile][16] (0..31, 32 = dead dipole). All device pointers. */
+int vgb_primary_beam(const double *az, const double *za, int npointing, const double *freq_hz, int nfreq,
+                     const uint32_t *delays, int ntile, double latitude, int pa_correction, void *B, void *stream);
+/* Index of a live/dead dipole pattern (amps[16], 0 = dead) among the 138
+ * cached configurations of primary_beam.c:355-414; -1 for more than two (but
+ * not all) dead dipoles; -2 on a NULL argument. */
+int vgb_hash_dipole_config(const double *amps);
+
+/* ---- learned primary-beam surrogate ----
+ * An MLP (6 inputs: sin az, cos az, za, frequency, a learned 2-d embedding of
+ * the delay set; 4 hidden layers of 256, GELU; 8 outputs: re/im of the 2x2
+ * Jones matrix) with BF16 weights and FP32 accumulation on the tensor cores,
+ * trained on the device by the library's own forward/backward/Adam kernels on
+ * Jones matrices of the plain model (vgb_primary_beam without the
+ * parallactic rotation). After validation, queries in sky cells whose error
+ * exceeded the tolerance (and tiles whose delays are not a trained set) are
+ * answered by the plain model. No reference counterpart: it replaces the
+ * beam-model calls of vmCalcB (primary_beam.c:79-191). */
+typedef struct vgb_surrogate vgb_surrogate;
+/* batch: training / inference rows per GEMM pass, a multiple of 512. */
+int vgb_surrogate_create(int nsets, int batch, unsigned long long seed, vgb_surrogate **out);
+void vgb_surrogate_destroy(vgb_surrogate *s);
+int vgb_surrogate_param_count(const vgb_surrogate *s);
+/* FP32 master parameters, host buffers of vgb_surrogate_param_count floats:
+ * W0 [256][6], W1..W3 [256][256], W4 [8][256], b0..b3 [256], b4 [8],
+ * embeddings [nsets][2]. */
+int vgb_surrogate_get_params(vgb_surrogate *s, float *host, int n);
+int vgb_surrogate_set_params(vgb_surrogate *s, const float *host, int n);
+/* Training table on the device: delay_sets [nsets][16] (host), freqs_hz
+ * [nfreq] (host), ndir random directions above 10 degrees elevation. */
+int vgb_surrogate_set_training(vgb_surrogate *s, const uint32_t *delay_sets, const double *freqs_hz, int nfreq,
+                               int ndir, unsigned long long seed);
+/* Adam steps with a cosine learning-rate schedule; loss_host (nullable)
+ * receives the mean squared error of each step. */
+int vgb_surrogate_train(vgb_surrogate *s, int steps, float lr_max, float lr_min, float *loss_host);
+/* One forward/backward pass without an update on a given batch (host
+ * arrays, batch rows): feat [batch][4] (sin az, cos az, scaled za, scaled f),
+ * set [batch], target [batch][8]; returns the gradient of the mean squared
+ * error for every parameter and the loss. For checking the kernels. */
+int vgb_surrogate_gradients(vgb_surrogate *s, const float *feat_host, const int *set_host, const float *y_host,
+                            float *grad_host, float *loss_host);
+/* Validation over nval random (delay set, direction, trained frequency) queries;
+ * builds the per-cell error map used for fallback decisions. */
+int vgb_surrogate_validate(vgb_surrogate *s, long long nval, float tol, float *max_err, float *frac_cells_ok);
+/* B [nfreq][npointing][ntile][2][2] complex double, as vgb_primary_beam, from
+ * the surrogate (tile_set[t] = trained delay-set index of tile t, < 0 = none)
+ * with plain-model fallback; nfallback (host, nullable) receives the number
+ * of (frequency, pointing, tile) entries the plain model answered. */
+int vgb_surrogate_beam(vgb_surrogate *s, const double *az, const double *za, int npointing, const double *freq_hz,
+                       int nfreq, const int *tile_set, const uint32_t *delays, int ntile, double latitude,
+                       int pa_correction, void *B, unsigned *nfallback, void *stream);
+
 /* ---- many-beam beamformer on the tensor cores ----
  *
  * Replaces, for npointing > 1, the per-pointing loop of vmBeamformChunk

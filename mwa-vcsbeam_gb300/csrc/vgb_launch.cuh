@@ -91,6 +91,18 @@ int launch_round_staged(int *data, long long n, int fpga, cudaStream_t st);
 int launch_fft_staged(float2 *rows, long long nrows, cudaStream_t st);
 int launch_hist_gather(const char2 *cur, long long cur_block, long long cc_cur, int ninputs, int nblocks, int ncc,
                        char2 *hist, long long cc_hist, cudaStream_t st);
+struct PbArgs { // primary-beam model evaluation
+    const double *az, *za;       // [npointing] radians
+    int npointing;
+    const double *freq;          // [nfreq] Hz
+    int nfreq;
+    const uint32_t *delays;      // [ntile][16]
+    int ntile;
+    double lat;                  // radians
+    int pa;                      // apply the parallactic-angle rotation
+    double2 *B;                  // [nfreq][npointing][ntile][4]
+};
+int launch_beam_model(const PbArgs &a, cudaStream_t st);
 int gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, int batch, bool fp16,
                  cudaStream_t st, int Kb);
 int launch_pack_staged(const float2 *ffted, int nspectra, int ninputs, const int *i_idx, unsigned flags,

@@ -115,6 +115,18 @@ _SIGS = {
     "vgb_cal_pq_correction": (I, [ctypes.c_char_p, ctypes.c_uint32, V, V, V, I, V]),
     "vgb_cal_flag_tiles": (I, [V, I, I, V, I]),
     "vgb_load_filter": (I, [ctypes.c_char_p, I, ctypes.c_double, V, I, V, V]),
+    "vgb_primary_beam": (I, [V, V, I, V, I, V, I, ctypes.c_double, I, V, V]),
+    "vgb_hash_dipole_config": (I, [V]),
+    "vgb_surrogate_create": (I, [I, I, ctypes.c_ulonglong, V]),
+    "vgb_surrogate_destroy": (None, [V]),
+    "vgb_surrogate_param_count": (I, [V]),
+    "vgb_surrogate_get_params": (I, [V, V, I]),
+    "vgb_surrogate_set_params": (I, [V, V, I]),
+    "vgb_surrogate_set_training": (I, [V, V, V, I, I, ctypes.c_ulonglong]),
+    "vgb_surrogate_train": (I, [V, I, Fl, Fl, V]),
+    "vgb_surrogate_gradients": (I, [V, V, V, V, V, V]),
+    "vgb_surrogate_validate": (I, [V, LL, Fl, V, V]),
+    "vgb_surrogate_beam": (I, [V, V, V, I, V, I, V, V, I, ctypes.c_double, I, V, V, V]),
     "vgb_multibeam_create": (I, [V, V]),
     "vgb_multibeam_destroy": (None, [V]),
     "vgb_multibeam_set_geometry": (I, [V, V, V, V, V, V, ctypes.c_double, V]),
@@ -360,6 +372,86 @@ def load_filter(path, nchans=NCHAN, scale=1.0):
     check(lib().vgb_load_filter(_enc(path), nchans, float(scale), out.ctypes.data, out.size, ctypes.byref(n),
                                 ctypes.byref(t)))
     return out, t.value
+
+
+MWA_LATITUDE_RADIANS = -0.4660608448386394
+
+
+def primary_beam(az, za, freq_hz, delays, B, pa_correction=True, latitude=MWA_LATITUDE_RADIANS, stream=None):
+    """B [nfreq][npointing][ntile][2][2] complex (float64 device tensor view)."""
+    check(lib().vgb_primary_beam(ptr(az), ptr(za), int(az.numel()), ptr(freq_hz), int(freq_hz.numel()),
+                                 ptr(delays), int(delays.numel() // 16), float(latitude), int(bool(pa_correction)),
+                                 ptr(B), stream_ptr(stream)))
+
+
+def hash_dipole_config(amps) -> int:
+    a = np.ascontiguousarray(amps, dtype=np.float64)
+    return lib().vgb_hash_dipole_config(a.ctypes.data)
+
+
+class Surrogate:
+    """The learned primary-beam surrogate (vgb_surrogate_*)."""
+
+    def __init__(self, nsets, batch=8192, seed=1):
+        h = V()
+        check(lib().vgb_surrogate_create(nsets, batch, seed, ctypes.byref(h)))
+        self.h = h
+        self.nsets = nsets
+        self.batch = batch
+        self.nparams = lib().vgb_surrogate_param_count(h)
+
+    def close(self):
+        if self.h:
+            lib().vgb_surrogate_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.nparams, dtype=np.float32)
+        check(lib().vgb_surrogate_get_params(self.h, out.ctypes.data, out.size))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        check(lib().vgb_surrogate_set_params(self.h, p.ctypes.data, p.size))
+
+    def set_training(self, delay_sets, freqs_hz, ndir, seed=7):
+        d = np.ascontiguousarray(delay_sets, dtype=np.uint32)
+        f = np.ascontiguousarray(freqs_hz, dtype=np.float64)
+        check(lib().vgb_surrogate_set_training(self.h, d.ctypes.data, f.ctypes.data, f.size, ndir, seed))
+
+    def train(self, steps, lr_max=1e-3, lr_min=1e-5, want_loss=True):
+        loss = np.zeros(max(steps, 1), dtype=np.float32) if want_loss else None
+        check(lib().vgb_surrogate_train(self.h, steps, lr_max, lr_min, None if loss is None else loss.ctypes.data))
+        return loss
+
+    def gradients(self, feat, sets, y):
+        feat = np.ascontiguousarray(feat, dtype=np.float32)
+        sets = np.ascontiguousarray(sets, dtype=np.int32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        g = np.empty(self.nparams, dtype=np.float32)
+        loss = ctypes.c_float(0.0)
+        check(lib().vgb_surrogate_gradients(self.h, feat.ctypes.data, sets.ctypes.data, y.ctypes.data, g.ctypes.data,
+                                            ctypes.byref(loss)))
+        return g, loss.value
+
+    def validate(self, nval, tol=1e-3):
+        mx, frac = ctypes.c_float(0.0), ctypes.c_float(0.0)
+        check(lib().vgb_surrogate_validate(self.h, nval, tol, ctypes.byref(mx), ctypes.byref(frac)))
+        return mx.value, frac.value
+
+    def beam(self, az, za, freq_hz, tile_set, delays, B, pa_correction=True, latitude=MWA_LATITUDE_RADIANS,
+             stream=None):
+        nfb = ctypes.c_uint(0)
+        check(lib().vgb_surrogate_beam(self.h, ptr(az), ptr(za), int(az.numel()), ptr(freq_hz), int(freq_hz.numel()),
+                                       ptr(tile_set), ptr(delays), int(tile_set.numel()), float(latitude),
+                                       int(bool(pa_correction)), ptr(B), ctypes.byref(nfb), stream_ptr(stream)))
+        return nfb.value
 
 
 class Multibeam:

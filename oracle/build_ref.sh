@@ -9,7 +9,7 @@
 #   oracle/_ref/ref_pfb.cubin       device code of src/pfb.cpp       (sm_103a)
 #   oracle/_ref/ref_form_beam.cubin device code of src/form_beam.cpp (sm_103a)
 #   oracle/_ref/libref_host.so      src/jones.c, src/filter.c, src/geometry.c,
-#                                   src/calibration.c
+#                                   src/calibration.c, src/primary_beam.c
 #                                   + oracle/ref_host_shim.c (host, this machine)
 #   oracle/_ref/runtime/            RUNTIME_DIR: links to the reference's
 #                                   pfb_filter/*.dat and pq_phase_correction.txt
@@ -52,6 +52,7 @@ done
 # Host C (table builders) for CPU-side pinning of the oracle.
 gcc -O2 -fPIC -shared -D__NVCC__ -w "${INC[@]}" \
     "$REF/src/jones.c" "$REF/src/filter.c" "$REF/src/geometry.c" "$REF/src/calibration.c" \
+    "$REF/src/primary_beam.c" \
     "$HERE/ref_host_shim.c" \
     -o "$OUT/libref_host.so" -L"$CUDA_HOME/lib64" -lcudart -lm &
 wait

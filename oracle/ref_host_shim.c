@@ -244,7 +244,20 @@ static void refhost_unreachable(const char *what)
 }
 void logger_start_stopwatch(logger *log, const char *n, bool p) { (void)log; (void)n; (void)p; }
 void logger_stop_stopwatch(logger *log, const char *n) { (void)log; (void)n; }
-void vmCalcB(vcsbeam_context *vm, beam_geom *bg) { (void)vm; (void)bg; refhost_unreachable("vmCalcB"); }
+int32_t new_fee_beam(const char *f, FEEBeam **b) { (void)f; (void)b; refhost_unreachable("new_fee_beam"); return 1; }
+void free_fee_beam(FEEBeam *b) { (void)b; }
+int32_t calc_jones(FEEBeam *b, double az, double za, uint32_t f, const uint32_t *d, const double *a, uint32_t n,
+                   uint8_t z, const double *lat, uint8_t iau, double *j)
+{ (void)b; (void)az; (void)za; (void)f; (void)d; (void)a; (void)n; (void)z; (void)lat; (void)iau; (void)j;
+  refhost_unreachable("calc_jones"); return 1; }
+int hb_last_error_length(void) { return 1; }
+int hb_last_error_message(char *buffer, int length) { if (length > 0) buffer[0] = 0; return 0; }
+void palDh2e(double az, double el, double phi, double *ha, double *dec)
+{ (void)az; (void)el; (void)phi; (void)ha; (void)dec; refhost_unreachable("palDh2e"); }
+double palPa(double ha, double dec, double phi) { (void)ha; (void)dec; (void)phi; refhost_unreachable("palPa"); return 0.0; }
+
+/* primary_beam.c's dead-dipole hash, for parity of vgb_hash_dipole_config */
+int refhost_hash_dipole_config(double *amps) { return hash_dipole_config(amps); }
 void palMap(double rm, double dm, double pr, double pd, double px, double rv,
             double eq, double date, double *ra, double *da)
 { (void)rm; (void)dm; (void)pr; (void)pd; (void)px; (void)rv; (void)eq; (void)date; (void)ra; (void)da; refhost_unreachable("palMap"); }

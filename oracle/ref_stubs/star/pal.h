@@ -12,4 +12,6 @@ double palGmst(double ut1);
 void palDtf2r(int ihour, int imin, double sec, double *rad, int *j);
 void palDaf2r(int ideg, int iamin, double asec, double *rad, int *j);
 void palCaldj(int iy, int im, int id, double *djm, int *j);
+void palDh2e(double az, double el, double phi, double *ha, double *dec);
+double palPa(double ha, double dec, double phi);
 #endif

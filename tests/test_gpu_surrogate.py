@@ -1,0 +1,88 @@
+"""The beam surrogate's own training kernels and its fallback logic.
+
+* Gradients of one forward/backward pass against the FP64 oracle
+  (oracle/mlp.py) on the same BF16-rounded weights: loss within 1e-5,
+  every layer's gradient within 1e-3 (norm-wise relative).
+* A short training run on the plain model reduces the loss 10x, validation
+  builds the cell map (at a tolerance a 600-step network meets in part of
+  the sky), and vgb_surrogate_beam agrees with vgb_primary_beam: within the
+  validation tolerance (x2 for points the validation did not sample) where
+  the network answered, exactly where the plain model did (the untrained
+  tile, the cells over tolerance).
+"""
+import numpy as np
+import pytest
+
+import mlp as M
+import synthetic as SY
+from helpers import dev, host, torch_cuda
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def vgb_mod():
+    torch_cuda()
+    import vgb
+
+    vgb.lib()
+    return vgb
+
+
+def test_gradients_match_oracle(vgb_mod):
+    nsets, B = 4, 1024
+    s = vgb_mod.Surrogate(nsets, batch=B, seed=3)
+    rng = np.random.default_rng(4)
+    az = rng.uniform(0, 2 * np.pi, B)
+    feat = np.stack([np.sin(az), np.cos(az), rng.uniform(-1, 0.8, B), rng.uniform(-1, 1, B)], 1).astype(np.float32)
+    sets = rng.integers(0, nsets, B).astype(np.int32)
+    y = (0.3 * rng.standard_normal((B, 8))).astype(np.float32)
+    p = s.params()
+    g, loss = s.gradients(feat, sets, y)
+    loss_ref, g_ref, _ = M.forward_backward(p, nsets, feat.astype(np.float64), sets, y.astype(np.float64))
+    assert abs(loss - loss_ref) <= 1e-5 * loss_ref
+    off, _ = M.layout(nsets)
+    for name, (o, shape) in off.items():
+        n = int(np.prod(shape))
+        a, b = g[o:o + n], g_ref[o:o + n]
+        err = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+        assert err < 1e-3, (name, err)
+    s.close()
+
+
+def test_training_validation_and_fallback(vgb_mod):
+    torch = torch_cuda()
+    nsets = 4
+    delays = SY.tile_delay_sets(nsets, seed=5)
+    freqs = np.linspace(100e6, 200e6, 4)
+    s = vgb_mod.Surrogate(nsets, batch=4096, seed=2)
+    s.set_training(delays, freqs, ndir=8192)
+    loss = s.train(600, lr_max=2e-3, lr_min=1e-4)
+    assert np.all(np.isfinite(loss))
+    assert loss[-50:].mean() < 0.1 * loss[:20].mean()
+    tol = 0.25
+    mx, frac = s.validate(200_000, tol=tol)
+    print("loss", loss[:3], loss[-3:], "max validation error", mx, "cells within", tol, frac)
+    assert frac > 0.0
+    # queries: pointings x the training frequencies x tiles of two trained sets and one untrained
+    rng = np.random.default_rng(6)
+    npnt = 64
+    az = rng.uniform(0, 2 * np.pi, npnt)
+    za = np.arccos(rng.uniform(np.cos(np.radians(75)), 1, npnt))
+    tdelays = np.concatenate([delays[[0, 2]], rng.integers(0, 32, (1, 16))]).astype(np.uint32)
+    tile_set = np.array([0, 2, -1], dtype=np.int32)
+    shape = (freqs.size, npnt, 3, 2, 2)
+    Bs = torch.zeros(int(np.prod(shape)) * 2, dtype=torch.float64, device="cuda")
+    Bp = torch.zeros_like(Bs)
+    nfb = s.beam(dev(az), dev(za), dev(freqs), dev(tile_set), dev(tdelays), Bs)
+    vgb_mod.primary_beam(dev(az), dev(za), dev(freqs), dev(tdelays), Bp)
+    torch.cuda.synchronize()
+    got = host(Bs).view(np.complex128).reshape(shape)
+    ref = host(Bp).view(np.complex128).reshape(shape)
+    assert nfb >= freqs.size * npnt            # every query of the untrained tile fell back
+    assert np.array_equal(got[:, :, 2], ref[:, :, 2])
+    err = np.abs(got[:, :, :2] - ref[:, :, :2]).reshape(freqs.size, npnt, 2, -1).max(-1)
+    exact = err == 0
+    assert np.all(err[~exact] <= 2 * tol)      # network answers (rotated by P, a unitary)
+    assert (~exact).any()                      # ... and there are some
+    s.close()
