@@ -334,6 +334,8 @@ def gb300_arm(args, rank, local_rank, world):
     if mb_section is not None:
         mb_section["gpu_launches"] = mb_launches
         line["multibeam"] = mb_section
+    if rank == 0 and not args.no_surrogate:
+        line["surrogate"] = surrogate_section(torch, vgb, SY, args.sur_steps)
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_line(args.cpu_seconds)
     if rank == 0:
@@ -354,7 +356,7 @@ MB_CASES = {
 MB_MODES = (("split_bf16", 0), ("fp16", 2), ("bf16", 1), ("fp32_cuda_cores", 3))
 
 
-def multibeam_section(torch, vgb, SY, iters: int, cases=None, modes=None, nfine=K):
+def multibeam_section(torch, vgb, SY, iters: int, cases=None, modes=None, nfine=K, stream_iters=3):
     """Each mode runs one coarse channel-second (128 fine channels x 10000
     samples) per step through vgb_multibeam_run on device-resident voltages;
     RTF counts 24 coarse channels per data-second. Stokes go to 8-bit PSRFITS
@@ -436,6 +438,40 @@ def multibeam_section(torch, vgb, SY, iters: int, cases=None, modes=None, nfine=
                                      "mma_issued_tflops": mma_tf, "mma_frac": mma_tf / peak_tf,
                                      "peak_source": "measured" if "bf16_tflops" in peaks else "fallback"}
             case["modes"][mode] = entry
+        # end to end: 4 coarse channel-seconds per call from pinned host memory
+        # through vgb_multibeam_run_host (uploads, compute and downloads overlap)
+        if name == "C4" and stream_iters > 0:
+            ncs = 4
+            for mode, prec in MB_MODES:
+                if prec == 3 or (modes and mode not in modes):
+                    continue
+                mb = vgb.Multibeam(ncs, nfine, nant, npnt, ns, nstokes=nst, precision=prec,
+                                   input=vgb.MB_INT8 if int8 else vgb.MB_INT4)
+                mb.set_geometry(to(unit), to(e), to(n), to(h), to(c))
+                rep = lambda a: np.ascontiguousarray(np.stack([a] * ncs))
+                mb.set_jones(to(rep(D)), to(rep(Bj)), to(np.concatenate([freqs] * ncs)), to(polQ), to(polP))
+                vh = torch.empty(ncs * nbytes, dtype=torch.uint8).pin_memory()
+                vh.view(ncs, nbytes).copy_(v.cpu().view(torch.uint8).expand(ncs, nbytes))
+                oh = torch.empty(ncs * npnt * nint * nst * nfine, dtype=torch.uint8).pin_memory()
+                offh = torch.empty(ncs * npnt * nst * nfine, dtype=torch.float32).pin_memory()
+                sclh = torch.empty_like(offh).pin_memory()
+                st = torch.cuda.current_stream()
+                mb.run_host(vh, oh, offh, sclh, stream=st)
+                st.synchronize()
+                t0 = time.perf_counter()
+                for _ in range(stream_iters):
+                    mb.run_host(vh, oh, offh, sclh, stream=st)
+                    launches += mb.launches()
+                st.synchronize()
+                dt = time.perf_counter() - t0
+                mb.close()
+                ccs = ncs * stream_iters
+                case["modes"][mode]["e2e"] = {
+                    "value": ccs / dt / NCC, "unit": UNIT, "ms_per_cc_s": 1e3 * dt / ccs,
+                    "h2d_bytes_per_cc_s": nbytes, "d2h_bytes_per_cc_s": int(oh.numel() + 8 * offh.numel()) // ncs,
+                    "path": f"vgb_multibeam_run_host, {ncs} coarse channel-seconds per call from pinned host memory, "
+                            f"{stream_iters} calls timed (wall clock), products back to pinned host memory"}
+                del vh, oh, offh, sclh
         m = case["modes"]
         if "fp32_cuda_cores" in m and "split_bf16" in m:
             case["split_bf16_vs_fp32_cuda_cores"] = m["fp32_cuda_cores"]["ms_per_cc_s"] / m["split_bf16"]["ms_per_cc_s"]
@@ -445,6 +481,65 @@ def multibeam_section(torch, vgb, SY, iters: int, cases=None, modes=None, nfine=
         del v, psr
         torch.cuda.empty_cache()
     return out, launches
+
+
+# --------------------------------------------------------------------------
+# learned primary-beam surrogate (the beam model's stand-in for many beams)
+# --------------------------------------------------------------------------
+def surrogate_section(torch, vgb, SY, steps: int):
+    """Train the surrogate on the plain model (16 delay sets x 24 frequencies
+    in 80-300 MHz x 65,536 directions above 10 deg elevation), validate it,
+    and time B for 1024 beams x 128 tiles x 24 frequencies from the
+    surrogate (with fallback) and from the plain model on the device."""
+    nsets, nfreq = 16, 24
+    delays = SY.tile_delay_sets(nsets, seed=11)
+    freqs = np.linspace(80e6, 300e6, nfreq)
+    s = vgb.Surrogate(nsets, batch=8192, seed=1)
+    s.set_training(delays, freqs, ndir=65536)
+    t0 = time.perf_counter()
+    loss = s.train(steps, lr_max=2e-3, lr_min=1e-4)
+    train_s = time.perf_counter() - t0
+    val = {}
+    for tol in (3e-2, 1e-2, 1e-3):
+        mx, frac = s.validate(2_000_000, tol=tol)
+        val[f"{tol:g}"] = {"cells_within": frac, "max_jones_error": mx}
+    rng = np.random.default_rng(0)
+    npnt, ntile = 1024, 128
+    az = torch.tensor(rng.uniform(0, 2 * np.pi, npnt), device="cuda")
+    za = torch.tensor(np.arccos(rng.uniform(np.cos(np.radians(60)), 1, npnt)), device="cuda")
+    f = torch.tensor(freqs, device="cuda")
+    tset = rng.integers(0, nsets, ntile)
+    ts = torch.tensor(tset, dtype=torch.int32, device="cuda")
+    td = torch.tensor(delays[tset].astype(np.int32), device="cuda")
+    Bs = torch.empty(nfreq * npnt * ntile * 8, dtype=torch.float64, device="cuda")
+    Bp = torch.empty_like(Bs)
+
+    def timed(fn, n=5):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            r = fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) / n, r
+
+    out = {"workload": "MLP 6 -> 4 x 256 GELU -> 8, BF16 weights, FP32 accumulate; trained on the analytic tile "
+                       "model (16 delay sets x 24 frequencies 80-300 MHz x 65,536 directions above 10 deg); "
+                       "queries: 1024 beams x 128 tiles x 24 frequencies",
+           "train_steps": steps, "train_s": train_s, "ms_per_train_step": 1e3 * train_s / max(steps, 1),
+           "final_loss": float(loss[-100:].mean()), "validation": val}
+    for tol in (1e-3, 3e-2):
+        s.validate(2_000_000, tol=tol)
+        ms_s, nfb = timed(lambda: s.beam(az, za, f, ts, td, Bs))
+        ms_p, _ = timed(lambda: vgb.primary_beam(az, za, f, td, Bp))
+        err = (Bs - Bp).abs().max().item()
+        out[f"inference_tol_{tol:g}"] = {"surrogate_ms": ms_s, "plain_model_device_ms": ms_p,
+                                         "fallback_fraction": nfb / (nfreq * npnt * ntile),
+                                         "max_abs_B_difference": err}
+    s.close()
+    return out
 
 
 def main():
@@ -461,6 +556,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ref-spectra", type=int, default=400, help="reference arm: spectra per step")
     ap.add_argument("--no-multibeam", action="store_true", help="skip the many-beam (C3/C4) section")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the beam-surrogate section")
+    ap.add_argument("--sur-steps", type=int, default=24000, help="surrogate training steps")
     ap.add_argument("--mb-iters", type=int, default=5, help="many-beam timed runs per mode")
     ap.add_argument("--mb-only", default=None, help="profiling: run only these many-beam cases (e.g. C4 or C3,C4) "
                     "and print their JSON; no bench line")

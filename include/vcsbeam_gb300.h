@@ -392,6 +392,15 @@ int vgb_multibeam_set_jones(vgb_multibeam *mb, const double *D, const double *B,
  * scales [ncc][npointing][nstokes][nfine]. */
 int vgb_multibeam_run(vgb_multibeam *mb, const void *v, float *S, uint8_t *out, float *offsets, float *scales,
                       void *stream);
+/* The same from pinned host memory, double-buffered: v_host [ncc][nsamples]
+ * [nfine][2*nant] voltages are uploaded one coarse channel ahead of the
+ * compute and each channel's PSRFITS bytes, offsets and scales (same layouts
+ * as vgb_multibeam_run) are downloaded while the next one computes. Returns
+ * once enqueued; `stream` completes after every product is on the host
+ * (replaces the synchronous vmPushChunk / vmPullS pattern, metadata.c:
+ * 913-923, form_beam.cpp:632-644). */
+int vgb_multibeam_run_host(vgb_multibeam *mb, const void *v_host, uint8_t *out_host, float *off_host,
+                           float *scl_host, void *stream);
 /* Kernels the last vgb_multibeam_run launched. */
 int vgb_multibeam_launches(const vgb_multibeam *mb);
 /* Stage timing with CUDA events (off by default): ms[0..4] = weights,

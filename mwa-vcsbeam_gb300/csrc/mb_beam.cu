@@ -961,6 +961,12 @@ struct vgb_multibeam {
     int nsm = 0;
     int last_launches = 0; // kernels the last run launched
     cudaEvent_t *ev = nullptr; // timing: 6 events per coarse channel (stage boundaries)
+    // host streaming (vgb_multibeam_run_host): two device slots of one
+    // coarse channel-second each, upload and download streams
+    uint8_t *d_vin[2] = {nullptr, nullptr}, *d_out[2] = {nullptr, nullptr};
+    float *d_off[2] = {nullptr, nullptr}, *d_scl[2] = {nullptr, nullptr};
+    cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
+    cudaEvent_t ev_h2d[2] = {}, ev_comp[2] = {}, ev_d2h[2] = {};
 };
 
 namespace {
@@ -977,6 +983,14 @@ template <typename T> int mb_alloc(T **p, size_t n, const char *what)
 
 void mb_free(vgb_multibeam *mb)
 {
+    for (int b = 0; b < 2; b++) {
+        for (void *p : {(void *)mb->d_vin[b], (void *)mb->d_out[b], (void *)mb->d_off[b], (void *)mb->d_scl[b]})
+            if (p) cudaFree(p);
+        for (cudaEvent_t e : {mb->ev_h2d[b], mb->ev_comp[b], mb->ev_d2h[b]})
+            if (e) cudaEventDestroy(e);
+    }
+    if (mb->s_h2d) cudaStreamDestroy(mb->s_h2d);
+    if (mb->s_d2h) cudaStreamDestroy(mb->s_d2h);
     if (mb->ev) {
         for (int i = 0; i < 6 * mb->cfg.ncc; i++)
             if (mb->ev[i]) cudaEventDestroy(mb->ev[i]);
@@ -1146,6 +1160,169 @@ extern "C" int vgb_multibeam_set_jones(vgb_multibeam *mb, const double *D, const
     return rc;
 }
 
+namespace {
+
+// One coarse channel-second: weights, voltage conversion, autocorrelation
+// GEMM, beam GEMM and (when out_cc is set) the 8-bit stage, on stream st.
+int mb_run_cc(vgb_multibeam *mb, int cc, const uint8_t *v_cc, float *S_cc, uint8_t *out_cc, float *off_cc,
+              float *scl_cc, cudaStream_t st, unsigned *status)
+{
+    const vgb_multibeam_config &c = mb->cfg;
+    const int A = c.nant, nf = c.nfine, ns = c.nsamples;
+    const long long nrow = (long long)nf * c.npointing * c.nstokes;
+    const MbStats stats{mb->d_stats, mb->d_stats + nrow, mb->d_stats + 2 * nrow};
+    int rc = VGB_SUCCESS;
+    auto mark = [&](int cc_, int i) {
+        if (mb->ev && !rc) rc = check_cuda(cudaEventRecord(mb->ev[6 * cc_ + i], st), "cudaEventRecord");
+    };
+    mb->last_launches += out_cc ? 5 : 4;
+    mark(cc, 0);
+    MbWeightArgs w{};
+    w.dt = mb->d_dt;
+    w.Binv = mb->d_Binv + 2ll * cc * mb->Bp * A;
+    w.H = mb->d_H + (long long)cc * mb->Bp * A;
+    w.Dinv = mb->d_Dinv + 2ll * cc * nf * A;
+    w.G = mb->d_G + (long long)cc * nf * A;
+    w.freq = mb->d_freq + (long long)cc * nf;
+    w.A = A;
+    w.Bp = mb->Bp;
+    w.nfine = nf;
+    w.nst = c.nstokes;
+    w.planes = mb->planes;
+    w.fp16 = mb->fp16;
+    w.int8 = mb->int8;
+    w.Mrows = mb->Mrows;
+    w.Mq = mb->Mq;
+    w.KA = mb->KA;
+    w.Kq = mb->Kq;
+    w.Aw = mb->d_Aw;
+    w.Aq = mb->d_Aq;
+    w.qscale = mb->d_qscale;
+    w.W32 = mb->d_W32;
+    w.Q32 = mb->d_Q32;
+    w.stats = stats;
+    w.B = c.npointing;
+    mb_weights_kernel<<<dim3(mb->Bp, nf), 128, 0, st>>>(w);
+    if ((rc = check_launch("mb_weights_kernel"))) return rc;
+    mark(cc, 1);
+
+    MbConvArgs g{};
+    g.v = v_cc;
+    g.int8 = mb->int8;
+    g.fp16 = mb->fp16;
+    g.ns = ns;
+    g.nfine = nf;
+    g.ni = 2 * A;
+    g.A = A;
+    g.nint = mb->nint;
+    g.nint_p = mb->nint_p;
+    g.Kb = mb->Kb;
+    g.polQ = mb->d_polQ;
+    g.polP = mb->d_polP;
+    g.V = mb->d_V;
+    g.C = mb->d_C;
+    const int conv_smem = kMbInt * 2 * A * (mb->int8 ? 2 : 1);
+    if ((rc = check_cuda(cudaFuncSetAttribute(mb_convert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              conv_smem),
+                         "cudaFuncSetAttribute(mb_convert_kernel)")))
+        return rc;
+    mb_convert_kernel<<<dim3(mb->nint, nf), 128, conv_smem, st>>>(g);
+    if ((rc = check_launch("mb_convert_kernel"))) return rc;
+    mark(cc, 2);
+
+    if (mb->simt) {
+        MbSimtAutoArgs q{};
+        q.Q = mb->d_Q32;
+        q.C = mb->d_C;
+        q.KA = mb->KA;
+        q.Kb = mb->Kb;
+        q.Mq = mb->Mq;
+        q.nint = mb->nint;
+        q.nint_p = mb->nint_p;
+        q.int8 = mb->int8;
+        q.R = mb->d_R;
+        mb_simt_auto_kernel<<<dim3(mb->nint_p / 64, mb->Mq / 64, nf), 256, 0, st>>>(q);
+        if ((rc = check_launch("mb_simt_auto_kernel"))) return rc;
+        mark(cc, 3);
+        MbSimtArgs b{};
+        b.W = mb->d_W32;
+        b.V = mb->d_V;
+        b.R = mb->d_R;
+        b.A = A;
+        b.Bp = mb->Bp;
+        b.B = c.npointing;
+        b.ns = ns;
+        b.nint = mb->nint;
+        b.nint_p = mb->nint_p;
+        b.Mq = mb->Mq;
+        b.invw = c.invw;
+        b.S = S_cc ? S_cc : mb->d_S;
+        b.stats = stats;
+        const dim3 grid((ns + kSimtSamp - 1) / kSimtSamp, mb->Bp / kSimtBeams, nf);
+        const int smem = (2 * kSimtBeams + kSimtSamp) * kSimtRow * (int)sizeof(float2);
+        auto kern = c.nstokes == 4 ? mb_simt_beam_kernel<4> : mb_simt_beam_kernel<1>;
+        if ((rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                             "cudaFuncSetAttribute(mb_simt_beam_kernel)")))
+            return rc;
+        kern<<<grid, 256, smem, st>>>(b);
+        if ((rc = check_launch("mb_simt_beam_kernel"))) return rc;
+    } else {
+    // autocorrelation terms R = Q C^T per channel (FP16 tensor path)
+    if ((rc = gemm_batched(mb->d_Aq, mb->d_C, mb->d_R, mb->Mq, mb->nint_p, mb->Kq, nf, true, st, mb->Kb))) return rc;
+    mark(cc, 3);
+
+    MbBeamArgs b{};
+    b.nfine = nf;
+    b.ns = ns;
+    b.nint = mb->nint;
+    b.B = c.npointing;
+    b.Mrows = mb->Mrows;
+    b.mtiles = mb->mtiles;
+    b.ntn = mb->ntn;
+    b.nk = mb->nk;
+    b.total = (long long)nf * mb->ntn * mb->mtiles;
+    b.R = mb->d_R;
+    b.qscale = mb->d_qscale;
+    b.Mq = mb->Mq;
+    b.nint_p = mb->nint_p;
+    b.invw = c.invw;
+    b.S = S_cc ? S_cc : mb->d_S;
+    b.stats = stats;
+    b.status = status;
+    if (mb->planes == 2)
+        rc = c.nstokes == 4 ? mb_launch_beam<2, false, 4>(mb, b, st) : mb_launch_beam<2, false, 1>(mb, b, st);
+    else if (mb->fp16)
+        rc = c.nstokes == 4 ? mb_launch_beam<1, true, 4>(mb, b, st) : mb_launch_beam<1, true, 1>(mb, b, st);
+    else
+        rc = c.nstokes == 4 ? mb_launch_beam<1, false, 4>(mb, b, st) : mb_launch_beam<1, false, 1>(mb, b, st);
+    if (rc) return rc;
+    }
+
+    mark(cc, 4);
+    if (out_cc) {
+        MbRenormArgs r{};
+        r.S = S_cc ? S_cc : mb->d_S;
+        r.stats = stats;
+        r.nfine = nf;
+        r.B = c.npointing;
+        r.nst = c.nstokes;
+        r.nint = mb->nint;
+        const long long out_st = nf, out_s = (long long)c.nstokes * nf, out_p = out_s * mb->nint;
+        r.out = out_cc;
+        r.out_p = out_p;
+        r.out_s = out_s;
+        r.out_st = out_st;
+        r.offsets = off_cc;
+        r.scales = scl_cc;
+        mb_renorm_kernel<<<dim3((nf + 31) / 32, c.npointing * c.nstokes), 256, 0, st>>>(r);
+        rc = check_launch("mb_renorm_kernel");
+    }
+    mark(cc, 5);
+    return rc;
+}
+
+} // namespace
+
 extern "C" int vgb_multibeam_run(vgb_multibeam *mb, const void *v, float *S, uint8_t *out, float *offsets,
                                  float *scales, void *stream)
 {
@@ -1159,162 +1336,91 @@ extern "C" int vgb_multibeam_run(vgb_multibeam *mb, const void *v, float *S, uin
     if (!status) return set_error(VGB_ERR_CUDA, "device status word unavailable");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const vgb_multibeam_config &c = mb->cfg;
-    const int A = c.nant, nf = c.nfine, ns = c.nsamples;
-    const long long vbytes_cc = (long long)ns * nf * 2 * A * (mb->int8 ? 2 : 1);
-    const long long s_cc = (long long)nf * c.npointing * c.nstokes * mb->nint;
-    const long long nrow = (long long)nf * c.npointing * c.nstokes;
-    const MbStats stats{mb->d_stats, mb->d_stats + nrow, mb->d_stats + 2 * nrow};
+    const long long vbytes_cc = (long long)c.nsamples * c.nfine * 2 * c.nant * (mb->int8 ? 2 : 1);
+    const long long s_cc = (long long)c.nfine * c.npointing * c.nstokes * mb->nint;
+    const long long out_cc = (long long)c.npointing * mb->nint * c.nstokes * c.nfine;
+    const long long stat_cc = (long long)c.npointing * c.nstokes * c.nfine;
     int rc = VGB_SUCCESS;
     mb->last_launches = 0;
-    auto mark = [&](int cc, int i) {
-        if (mb->ev && !rc) rc = check_cuda(cudaEventRecord(mb->ev[6 * cc + i], st), "cudaEventRecord");
-    };
-    for (int cc = 0; cc < c.ncc && !rc; cc++) {
-        mb->last_launches += out ? 5 : 4;
-        mark(cc, 0);
-        MbWeightArgs w{};
-        w.dt = mb->d_dt;
-        w.Binv = mb->d_Binv + 2ll * cc * mb->Bp * A;
-        w.H = mb->d_H + (long long)cc * mb->Bp * A;
-        w.Dinv = mb->d_Dinv + 2ll * cc * nf * A;
-        w.G = mb->d_G + (long long)cc * nf * A;
-        w.freq = mb->d_freq + (long long)cc * nf;
-        w.A = A;
-        w.Bp = mb->Bp;
-        w.nfine = nf;
-        w.nst = c.nstokes;
-        w.planes = mb->planes;
-        w.fp16 = mb->fp16;
-        w.int8 = mb->int8;
-        w.Mrows = mb->Mrows;
-        w.Mq = mb->Mq;
-        w.KA = mb->KA;
-        w.Kq = mb->Kq;
-        w.Aw = mb->d_Aw;
-        w.Aq = mb->d_Aq;
-        w.qscale = mb->d_qscale;
-        w.W32 = mb->d_W32;
-        w.Q32 = mb->d_Q32;
-        w.stats = stats;
-        w.B = c.npointing;
-        mb_weights_kernel<<<dim3(mb->Bp, nf), 128, 0, st>>>(w);
-        if ((rc = check_launch("mb_weights_kernel"))) break;
-        mark(cc, 1);
+    for (int cc = 0; cc < c.ncc && !rc; cc++)
+        rc = mb_run_cc(mb, cc, static_cast<const uint8_t *>(v) + cc * vbytes_cc, S ? S + cc * s_cc : nullptr,
+                       out ? out + cc * out_cc : nullptr, out ? offsets + cc * stat_cc : nullptr,
+                       out ? scales + cc * stat_cc : nullptr, st, status);
+    return rc;
+}
 
-        MbConvArgs g{};
-        g.v = static_cast<const uint8_t *>(v) + cc * vbytes_cc;
-        g.int8 = mb->int8;
-        g.fp16 = mb->fp16;
-        g.ns = ns;
-        g.nfine = nf;
-        g.ni = 2 * A;
-        g.A = A;
-        g.nint = mb->nint;
-        g.nint_p = mb->nint_p;
-        g.Kb = mb->Kb;
-        g.polQ = mb->d_polQ;
-        g.polP = mb->d_polP;
-        g.V = mb->d_V;
-        g.C = mb->d_C;
-        const int conv_smem = kMbInt * 2 * A * (mb->int8 ? 2 : 1);
-        if ((rc = check_cuda(cudaFuncSetAttribute(mb_convert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  conv_smem),
-                             "cudaFuncSetAttribute(mb_convert_kernel)")))
-            break;
-        mb_convert_kernel<<<dim3(mb->nint, nf), 128, conv_smem, st>>>(g);
-        if ((rc = check_launch("mb_convert_kernel"))) break;
-        mark(cc, 2);
-
-        if (mb->simt) {
-            MbSimtAutoArgs q{};
-            q.Q = mb->d_Q32;
-            q.C = mb->d_C;
-            q.KA = mb->KA;
-            q.Kb = mb->Kb;
-            q.Mq = mb->Mq;
-            q.nint = mb->nint;
-            q.nint_p = mb->nint_p;
-            q.int8 = mb->int8;
-            q.R = mb->d_R;
-            mb_simt_auto_kernel<<<dim3(mb->nint_p / 64, mb->Mq / 64, nf), 256, 0, st>>>(q);
-            if ((rc = check_launch("mb_simt_auto_kernel"))) break;
-            mark(cc, 3);
-            MbSimtArgs b{};
-            b.W = mb->d_W32;
-            b.V = mb->d_V;
-            b.R = mb->d_R;
-            b.A = A;
-            b.Bp = mb->Bp;
-            b.B = c.npointing;
-            b.ns = ns;
-            b.nint = mb->nint;
-            b.nint_p = mb->nint_p;
-            b.Mq = mb->Mq;
-            b.invw = c.invw;
-            b.S = S ? S + cc * s_cc : mb->d_S;
-            b.stats = stats;
-            const dim3 grid((ns + kSimtSamp - 1) / kSimtSamp, mb->Bp / kSimtBeams, nf);
-            const int smem = (2 * kSimtBeams + kSimtSamp) * kSimtRow * (int)sizeof(float2);
-            auto kern = c.nstokes == 4 ? mb_simt_beam_kernel<4> : mb_simt_beam_kernel<1>;
-            if ((rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
-                                 "cudaFuncSetAttribute(mb_simt_beam_kernel)")))
-                break;
-            kern<<<grid, 256, smem, st>>>(b);
-            if ((rc = check_launch("mb_simt_beam_kernel"))) break;
-        } else {
-        // autocorrelation terms R = Q C^T per channel (FP16 tensor path)
-        if ((rc = gemm_batched(mb->d_Aq, mb->d_C, mb->d_R, mb->Mq, mb->nint_p, mb->Kq, nf, true, st, mb->Kb))) break;
-        mark(cc, 3);
-
-        MbBeamArgs b{};
-        b.nfine = nf;
-        b.ns = ns;
-        b.nint = mb->nint;
-        b.B = c.npointing;
-        b.Mrows = mb->Mrows;
-        b.mtiles = mb->mtiles;
-        b.ntn = mb->ntn;
-        b.nk = mb->nk;
-        b.total = (long long)nf * mb->ntn * mb->mtiles;
-        b.R = mb->d_R;
-        b.qscale = mb->d_qscale;
-        b.Mq = mb->Mq;
-        b.nint_p = mb->nint_p;
-        b.invw = c.invw;
-        b.S = S ? S + cc * s_cc : mb->d_S;
-        b.stats = stats;
-        b.status = status;
-        if (mb->planes == 2)
-            rc = c.nstokes == 4 ? mb_launch_beam<2, false, 4>(mb, b, st) : mb_launch_beam<2, false, 1>(mb, b, st);
-        else if (mb->fp16)
-            rc = c.nstokes == 4 ? mb_launch_beam<1, true, 4>(mb, b, st) : mb_launch_beam<1, true, 1>(mb, b, st);
-        else
-            rc = c.nstokes == 4 ? mb_launch_beam<1, false, 4>(mb, b, st) : mb_launch_beam<1, false, 1>(mb, b, st);
-        if (rc) break;
+extern "C" int vgb_multibeam_run_host(vgb_multibeam *mb, const void *v_host, uint8_t *out_host, float *off_host,
+                                      float *scl_host, void *stream)
+{
+    if (!mb || !v_host || !out_host || !off_host || !scl_host)
+        return set_error(VGB_ERR_INVALID, "multibeam_run_host: NULL argument");
+    if (!mb->have_geometry || !mb->have_jones)
+        return set_error(VGB_ERR_STATE, "multibeam_run_host: set_geometry and set_jones must come first");
+    unsigned *status = status_word();
+    if (!status) return set_error(VGB_ERR_CUDA, "device status word unavailable");
+    const vgb_multibeam_config &c = mb->cfg;
+    const size_t vbytes = (size_t)c.nsamples * c.nfine * 2 * c.nant * (mb->int8 ? 2 : 1);
+    const size_t obytes = (size_t)c.npointing * mb->nint * c.nstokes * c.nfine;
+    const size_t sbytes = (size_t)c.npointing * c.nstokes * c.nfine * sizeof(float);
+    int rc = VGB_SUCCESS;
+    if (!mb->s_h2d) {
+        for (int b = 0; b < 2 && !rc; b++) {
+            rc = mb_alloc(&mb->d_vin[b], vbytes, "streamed voltages");
+            if (!rc) rc = mb_alloc(&mb->d_out[b], obytes, "streamed PSRFITS bytes");
+            if (!rc) rc = mb_alloc(&mb->d_off[b], sbytes / sizeof(float), "streamed offsets");
+            if (!rc) rc = mb_alloc(&mb->d_scl[b], sbytes / sizeof(float), "streamed scales");
+            for (cudaEvent_t *e : {&mb->ev_h2d[b], &mb->ev_comp[b], &mb->ev_d2h[b]})
+                if (!rc) rc = check_cuda(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
         }
-
-        mark(cc, 4);
-        if (out) {
-            MbRenormArgs r{};
-            r.S = S ? S + cc * s_cc : mb->d_S;
-            r.stats = stats;
-            r.nfine = nf;
-            r.B = c.npointing;
-            r.nst = c.nstokes;
-            r.nint = mb->nint;
-            const long long out_st = nf, out_s = (long long)c.nstokes * nf, out_p = out_s * mb->nint;
-            r.out = out + cc * out_p * c.npointing;
-            r.out_p = out_p;
-            r.out_s = out_s;
-            r.out_st = out_st;
-            const long long stat_cc = (long long)c.npointing * c.nstokes * nf;
-            r.offsets = offsets + cc * stat_cc;
-            r.scales = scales + cc * stat_cc;
-            mb_renorm_kernel<<<dim3((nf + 31) / 32, c.npointing * c.nstokes), 256, 0, st>>>(r);
-            rc = check_launch("mb_renorm_kernel");
-        }
-        mark(cc, 5);
+        if (!rc) rc = check_cuda(cudaStreamCreateWithFlags(&mb->s_h2d, cudaStreamNonBlocking), "cudaStreamCreate");
+        if (!rc) rc = check_cuda(cudaStreamCreateWithFlags(&mb->s_d2h, cudaStreamNonBlocking), "cudaStreamCreate");
+        if (rc) return rc;
     }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const uint8_t *vin = static_cast<const uint8_t *>(v_host);
+    // the caller's earlier work on st comes first
+    rc = check_cuda(cudaEventRecord(mb->ev_comp[1], st), "cudaEventRecord");
+    if (!rc) rc = check_cuda(cudaStreamWaitEvent(mb->s_h2d, mb->ev_comp[1], 0), "cudaStreamWaitEvent");
+    for (int cc = 0; cc < 2 && cc < c.ncc && !rc; cc++) {
+        rc = check_cuda(cudaMemcpyAsync(mb->d_vin[cc], vin + cc * vbytes, vbytes, cudaMemcpyHostToDevice, mb->s_h2d),
+                        "cudaMemcpyAsync(H2D)");
+        if (!rc) rc = check_cuda(cudaEventRecord(mb->ev_h2d[cc], mb->s_h2d), "cudaEventRecord");
+    }
+    mb->last_launches = 0;
+    for (int cc = 0; cc < c.ncc && !rc; cc++) {
+        const int b = cc & 1;
+        rc = check_cuda(cudaStreamWaitEvent(st, mb->ev_h2d[b], 0), "cudaStreamWaitEvent");
+        if (!rc && cc >= 2) rc = check_cuda(cudaStreamWaitEvent(st, mb->ev_d2h[b], 0), "cudaStreamWaitEvent");
+        if (!rc) rc = mb_run_cc(mb, cc, mb->d_vin[b], nullptr, mb->d_out[b], mb->d_off[b], mb->d_scl[b], st, status);
+        if (!rc) rc = check_cuda(cudaEventRecord(mb->ev_comp[b], st), "cudaEventRecord");
+        // products of this channel out ...
+        if (!rc) rc = check_cuda(cudaStreamWaitEvent(mb->s_d2h, mb->ev_comp[b], 0), "cudaStreamWaitEvent");
+        if (!rc)
+            rc = check_cuda(cudaMemcpyAsync(out_host + cc * obytes, mb->d_out[b], obytes, cudaMemcpyDeviceToHost,
+                                            mb->s_d2h),
+                            "cudaMemcpyAsync(D2H)");
+        if (!rc)
+            rc = check_cuda(cudaMemcpyAsync(off_host + cc * (sbytes / sizeof(float)), mb->d_off[b], sbytes,
+                                            cudaMemcpyDeviceToHost, mb->s_d2h),
+                            "cudaMemcpyAsync(D2H)");
+        if (!rc)
+            rc = check_cuda(cudaMemcpyAsync(scl_host + cc * (sbytes / sizeof(float)), mb->d_scl[b], sbytes,
+                                            cudaMemcpyDeviceToHost, mb->s_d2h),
+                            "cudaMemcpyAsync(D2H)");
+        if (!rc) rc = check_cuda(cudaEventRecord(mb->ev_d2h[b], mb->s_d2h), "cudaEventRecord");
+        // ... and the channel after next in, once this slot's voltages are consumed
+        if (!rc && cc + 2 < c.ncc) {
+            rc = check_cuda(cudaStreamWaitEvent(mb->s_h2d, mb->ev_comp[b], 0), "cudaStreamWaitEvent");
+            if (!rc)
+                rc = check_cuda(cudaMemcpyAsync(mb->d_vin[b], vin + (cc + 2) * vbytes, vbytes, cudaMemcpyHostToDevice,
+                                                mb->s_h2d),
+                                "cudaMemcpyAsync(H2D)");
+            if (!rc) rc = check_cuda(cudaEventRecord(mb->ev_h2d[b], mb->s_h2d), "cudaEventRecord");
+        }
+    }
+    // the caller's stream completes only after every product has landed on the host
+    for (int b = 0; b < 2 && b < c.ncc && !rc; b++)
+        rc = check_cuda(cudaStreamWaitEvent(st, mb->ev_d2h[b], 0), "cudaStreamWaitEvent");
     return rc;
 }
 

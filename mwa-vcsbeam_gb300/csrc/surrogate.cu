@@ -40,7 +40,7 @@ constexpr double kSurZaMax = 80.0 * kBmPi / 180.0;
 struct SurLayout {
     int nsets;
     long long W0, W1, W2, W3, W4, b0, b4, emb, total; // b1..b3 follow b0
-    explicit SurLayout(int ns = 0) : nsets(ns)
+    SurLayout(int ns = 0) : nsets(ns)
     {
         W0 = 0;                        // [256][6]
         W1 = W0 + kSurH * 6;           // [256][256]

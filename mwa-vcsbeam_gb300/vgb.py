@@ -132,6 +132,7 @@ _SIGS = {
     "vgb_multibeam_set_geometry": (I, [V, V, V, V, V, V, ctypes.c_double, V]),
     "vgb_multibeam_set_jones": (I, [V, V, V, V, V, V, V]),
     "vgb_multibeam_run": (I, [V, V, V, V, V, V, V]),
+    "vgb_multibeam_run_host": (I, [V, V, V, V, V, V]),
     "vgb_multibeam_launches": (I, [V]),
     "vgb_multibeam_enable_timing": (I, [V, I]),
     "vgb_multibeam_stage_ms": (I, [V, V, I]),
@@ -491,6 +492,11 @@ class Multibeam:
     def run(self, v, S=None, out=None, offsets=None, scales=None, stream=None):
         check(lib().vgb_multibeam_run(self.h, ptr(v), ptr(S), ptr(out), ptr(offsets), ptr(scales),
                                       stream_ptr(stream)))
+
+    def run_host(self, v_host, out_host, off_host, scl_host, stream=None):
+        """Pinned host tensors in, pinned host tensors out (double-buffered)."""
+        check(lib().vgb_multibeam_run_host(self.h, ptr(v_host), ptr(out_host), ptr(off_host), ptr(scl_host),
+                                           stream_ptr(stream)))
 
     def launches(self) -> int:
         return lib().vgb_multibeam_launches(self.h)
