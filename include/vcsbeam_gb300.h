@@ -231,6 +231,8 @@ int vgb_beamform_mwax_psrfits_noalloc(const vgb_voltages *v, int ncc, int nspect
  * ("K-major"). M, N multiples of 128, K a multiple of 64. The building block
  * of the many-beam beamformer; no reference counterpart (the reference has
  * no tensor-core path, form_beam.cpp:239-371 sums tiles with one thread).
+ * The CTA tile width (128 or 256 columns) is chosen per shape by timing both
+ * on the first call with that shape (an autotuner; results are identical).
  */
 int vgb_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, void *stream);
 
@@ -466,6 +468,10 @@ int vgb_pipeline_set_host_outputs(vgb_pipeline *p, uint8_t *psrfits, float *offs
 int vgb_pipeline_sync(vgb_pipeline *p);
 /* Record CUDA events around each stage of every second (off by default). */
 int vgb_pipeline_enable_timing(vgb_pipeline *p, int on);
+/* Replay each second from a CUDA graph captured on its first occurrence (per
+ * input buffer, second parity and output set); on by default, bypassed while
+ * stage timing is on. */
+int vgb_pipeline_enable_graphs(vgb_pipeline *p, int on);
 /* Milliseconds per stage of the last second: [0] fused PFB + beamformer,
  * [1] renormalise, [2] inverse PFB + VDIF, [3] history carry. Synchronises. */
 int vgb_pipeline_stage_ms(vgb_pipeline *p, float *ms, int n);

@@ -12,6 +12,10 @@
 // the device status word, frees its tensor memory and returns.
 #include <cudaTypedefs.h>
 
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "tcgen05.cuh"
 #include "vgb_launch.cuh"
 
@@ -163,6 +167,56 @@ using namespace vgb;
 
 namespace vgb {
 
+// Tile width (N of one CTA tile: 128 or 256) for a GEMM shape, chosen by
+// timing both widths on the first call with that shape (3 runs each with CUDA
+// events on the caller's stream, after one warm-up) and cached; both widths
+// give identical results (same K order per output). While a stream is being
+// captured into a graph the measured choice is used if known, else 256.
+template <class Launch>
+int gemm_tile_width(int M, int N, int K, int Kb, int batch, bool fp16, cudaStream_t st, Launch &launch)
+{
+    if (N % 256) return 128;
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int, int, int, bool>, int> cache;
+    const auto key = std::make_tuple(M, N, K, Kb, batch, fp16);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
+    }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return 256;
+    }
+    float best_ms = 0.f;
+    int best = 256;
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess) return 256;
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return 256;
+    }
+    for (int bn : {256, 128}) {
+        if (launch(bn)) break;
+        cudaEventRecord(e0, st);
+        for (int i = 0; i < 3; i++) launch(bn);
+        cudaEventRecord(e1, st);
+        float ms = 0.f;
+        if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) break;
+        if (bn == 256 || ms < best_ms) {
+            best_ms = ms;
+            best = bn;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaGetLastError();
+    std::lock_guard<std::mutex> lk(mu);
+    cache[key] = best;
+    return best;
+}
+
 // C[b] = A[b] B[b]^T for b < batch: A rows b*M.., B rows b*N.., C rows b*M.. of
 // contiguous row-major operands (bf16, or fp16 with `fp16`). B may be
 // narrower than A along K (Kb columns, a multiple of 64): column k of A meets
@@ -176,28 +230,27 @@ int gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, in
         return set_error(VGB_ERR_INVALID, "gemm: M and N must be multiples of 128 and K of 64 (got %d, %d, %d)", M, N,
                          K);
     if ((reinterpret_cast<uintptr_t>(C) & 15)) return set_error(VGB_ERR_INVALID, "gemm: C must be 16-byte aligned");
-    const int bn = (N % 256 == 0) ? 256 : 128;
-    CUtensorMap ta, tb;
-    int rc = make_tmap_bf16(&ta, A, (uint64_t)M * batch, K, (uint64_t)K * 2, 128, fp16);
-    if (rc) return rc;
-    if ((rc = make_tmap_bf16(&tb, B, (uint64_t)N * batch, Kb, (uint64_t)Kb * 2, bn, fp16))) return rc;
     unsigned *status = status_word();
     if (!status) return set_error(VGB_ERR_CUDA, "device status word unavailable");
-    dim3 grid(N / bn, M / 128, batch);
-    auto go = [&](auto kern, int smem) {
-        int r = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
-                           "cudaFuncSetAttribute(gemm)");
-        if (!r) kern<<<grid, 128, smem, st>>>(ta, tb, C, M, N, K, Kb, status);
-        return r;
+    auto launch = [&](int bn) -> int {
+        CUtensorMap ta, tb;
+        int r = make_tmap_bf16(&ta, A, (uint64_t)M * batch, K, (uint64_t)K * 2, 128, fp16);
+        if (!r) r = make_tmap_bf16(&tb, B, (uint64_t)N * batch, Kb, (uint64_t)Kb * 2, bn, fp16);
+        if (r) return r;
+        dim3 grid(N / bn, M / 128, batch);
+        auto go = [&](auto kern, int smem) {
+            int e = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                               "cudaFuncSetAttribute(gemm)");
+            if (!e) kern<<<grid, 128, smem, st>>>(ta, tb, C, M, N, K, Kb, status);
+            return e ? e : check_launch("gemm_bf16_kernel");
+        };
+        if (fp16)
+            return bn == 256 ? go(gemm_bf16_kernel<true, 256>, (int)sizeof(GemmSmem<256>) + 1024)
+                             : go(gemm_bf16_kernel<true, 128>, (int)sizeof(GemmSmem<128>) + 1024);
+        return bn == 256 ? go(gemm_bf16_kernel<false, 256>, (int)sizeof(GemmSmem<256>) + 1024)
+                         : go(gemm_bf16_kernel<false, 128>, (int)sizeof(GemmSmem<128>) + 1024);
     };
-    if (fp16)
-        rc = bn == 256 ? go(gemm_bf16_kernel<true, 256>, (int)sizeof(GemmSmem<256>) + 1024)
-                       : go(gemm_bf16_kernel<true, 128>, (int)sizeof(GemmSmem<128>) + 1024);
-    else
-        rc = bn == 256 ? go(gemm_bf16_kernel<false, 256>, (int)sizeof(GemmSmem<256>) + 1024)
-                       : go(gemm_bf16_kernel<false, 128>, (int)sizeof(GemmSmem<128>) + 1024);
-    if (rc) return rc;
-    return check_launch("gemm_bf16_kernel");
+    return launch(gemm_tile_width(M, N, K, Kb, batch, fp16, st, launch));
 }
 
 } // namespace vgb

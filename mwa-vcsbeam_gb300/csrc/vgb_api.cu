@@ -5,6 +5,8 @@
 #include <cstring>
 #include <string>
 
+#include <vector>
+
 #include "vgb_launch.cuh"
 
 namespace vgb {
@@ -358,6 +360,18 @@ struct vgb_pipeline {
     // per-stage timing
     bool timing = false;
     cudaEvent_t ev_stage[5] = {};
+    // CUDA graphs of one second, keyed by what the captured launches bake in
+    struct Graph {
+        const void *volt;
+        long long stride;
+        int parity;
+        bool first;
+        const void *hout;
+        cudaGraphExec_t exec;
+        int launches;
+    };
+    std::vector<Graph> graphs;
+    bool use_graphs = true;
 };
 
 namespace {
@@ -448,6 +462,48 @@ int pipeline_second(vgb_pipeline *p, const char2 *volt, long long cc_stride_byte
     return rc;
 }
 
+void drop_graphs(vgb_pipeline *p)
+{
+    for (auto &g : p->graphs) cudaGraphExecDestroy(g.exec);
+    p->graphs.clear();
+}
+
+// One second, replayed from a captured CUDA graph (captured on first use for
+// this input buffer, second parity and output set); eager while timing.
+int pipeline_second_graph(vgb_pipeline *p, const char2 *volt, long long cc_stride_bytes)
+{
+    if (!p->use_graphs || p->timing) return pipeline_second(p, volt, cc_stride_bytes);
+    const int parity = (int)(p->second & 1);
+    const bool first = p->second == 0;
+    const void *hout = p->h_psrfits ? (const void *)p->h_psrfits : (const void *)p->h_vdif;
+    for (auto &g : p->graphs)
+        if (g.volt == volt && g.stride == cc_stride_bytes && g.parity == parity && g.first == first && g.hout == hout) {
+            int rc = check_cuda(cudaGraphLaunch(g.exec, p->s_comp), "cudaGraphLaunch");
+            if (!rc) {
+                p->second++;
+                p->launches = g.launches;
+            }
+            return rc;
+        }
+    if (p->graphs.size() >= 8) drop_graphs(p);
+    const long long saved = p->second;
+    int rc = check_cuda(cudaStreamBeginCapture(p->s_comp, cudaStreamCaptureModeRelaxed), "cudaStreamBeginCapture");
+    if (rc) return rc;
+    rc = pipeline_second(p, volt, cc_stride_bytes);
+    cudaGraph_t graph = nullptr;
+    const int rc_end = check_cuda(cudaStreamEndCapture(p->s_comp, &graph), "cudaStreamEndCapture");
+    p->second = saved;
+    if (!rc) rc = rc_end;
+    cudaGraphExec_t exec = nullptr;
+    if (!rc) rc = check_cuda(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+    if (graph) cudaGraphDestroy(graph);
+    if (rc) return rc;
+    p->graphs.push_back({volt, cc_stride_bytes, parity, first, hout, exec, p->launches});
+    rc = check_cuda(cudaGraphLaunch(exec, p->s_comp), "cudaGraphLaunch");
+    if (!rc) p->second++;
+    return rc;
+}
+
 } // namespace
 
 extern "C" {
@@ -498,6 +554,11 @@ int vgb_pipeline_create(const vgb_pipeline_config *cfg, vgb_pipeline **out)
         vgb_pipeline_destroy(p);
         return rc;
     }
+    // resolve the device status word now, not inside a graph capture
+    if (!status_word()) {
+        vgb_pipeline_destroy(p);
+        return set_error(VGB_ERR_CUDA, "device status word unavailable");
+    }
     *out = p;
     return VGB_SUCCESS;
 }
@@ -507,6 +568,7 @@ int vgb_pipeline_destroy(vgb_pipeline *p)
     if (!p) return VGB_SUCCESS;
     if (p->s_comp) cudaStreamSynchronize(p->s_comp);
     if (p->s_copy) cudaStreamSynchronize(p->s_copy);
+    drop_graphs(p);
     void *bufs[] = {p->d_filter, p->d_coeffs, p->d_W, p->d_volt[0], p->d_volt[1], p->d_hist[0], p->d_hist[1],
                     p->d_S, p->d_e, p->d_incoh, p->d_ehist[0], p->d_ehist[1], p->d_psrfits, p->d_off, p->d_scl,
                     p->d_vdif, p->d_hdr};
@@ -562,7 +624,16 @@ int vgb_pipeline_run_device(vgb_pipeline *p, const void *d_voltages, long long c
     if (!p || !d_voltages) return set_error(VGB_ERR_INVALID, "NULL argument");
     if (cur_cc_stride < p->second_bytes && p->cfg.ncc > 1)
         return set_error(VGB_ERR_INVALID, "coarse-channel stride smaller than one second");
-    return pipeline_second(p, static_cast<const char2 *>(d_voltages), cur_cc_stride);
+    return pipeline_second_graph(p, static_cast<const char2 *>(d_voltages), cur_cc_stride);
+}
+
+int vgb_pipeline_enable_graphs(vgb_pipeline *p, int on)
+{
+    if (!p) return set_error(VGB_ERR_INVALID, "NULL pipeline");
+    int rc = check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
+    drop_graphs(p);
+    p->use_graphs = on != 0;
+    return rc;
 }
 
 int vgb_pipeline_run_host(vgb_pipeline *p, const void *h_voltages, long long cur_cc_stride)
@@ -588,7 +659,7 @@ int vgb_pipeline_run_host(vgb_pipeline *p, const void *h_voltages, long long cur
     rc = check_cuda(cudaEventRecord(p->ev_copied[b], p->s_copy), "record copied");
     rc = rc ? rc : check_cuda(cudaStreamWaitEvent(p->s_comp, p->ev_copied[b], 0), "wait copied");
     if (rc) return rc;
-    rc = pipeline_second(p, p->d_volt[b], p->second_bytes);
+    rc = pipeline_second_graph(p, p->d_volt[b], p->second_bytes);
     if (rc) return rc;
     rc = check_cuda(cudaEventRecord(p->ev_consumed[b], p->s_comp), "record consumed");
     p->host_buf ^= 1;
@@ -664,6 +735,10 @@ int vgb_pipeline_set_host_outputs(vgb_pipeline *p, uint8_t *psrfits, float *offs
 {
     if (!p) return set_error(VGB_ERR_INVALID, "NULL pipeline");
     if (vdif && !p->cfg.do_ipfb) return set_error(VGB_ERR_STATE, "pipeline was created without the IPFB");
+    // graphs captured the previous destinations
+    int rc = check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
+    if (rc) return rc;
+    drop_graphs(p);
     p->h_psrfits = psrfits;
     p->h_off = offsets;
     p->h_scl = scales;

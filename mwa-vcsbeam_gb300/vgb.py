@@ -153,6 +153,7 @@ _SIGS = {
     "vgb_pipeline_set_host_outputs": (I, [V, V, V, V, V]),
     "vgb_pipeline_sync": (I, [V]),
     "vgb_pipeline_enable_timing": (I, [V, I]),
+    "vgb_pipeline_enable_graphs": (I, [V, I]),
     "vgb_pipeline_stage_ms": (I, [V, ctypes.POINTER(Fl), I]),
 }
 
@@ -584,6 +585,9 @@ class Pipeline:
 
     def enable_timing(self, on: bool = True):
         check(lib().vgb_pipeline_enable_timing(self.h, int(on)))
+
+    def enable_graphs(self, on: bool = True):
+        check(lib().vgb_pipeline_enable_graphs(self.h, int(on)))
 
     def stage_ms(self):
         arr = (Fl * 4)()

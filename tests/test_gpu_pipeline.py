@@ -127,3 +127,28 @@ def test_pipeline_host_equals_device(vgb_mod, torch, setup):
         outs.append(res)
     for (a, b), (c, d) in zip(outs[0], outs[1]):
         assert np.array_equal(a, c) and np.array_equal(b, d)
+
+
+def test_pipeline_graph_replay_equals_eager(vgb_mod, torch, setup):
+    """Seconds replayed from captured CUDA graphs (two resident buffers,
+    alternating; the first second captured separately) give the bytes of
+    eager execution."""
+    volt, filt, syn, tabs = setup
+    invw = 1.0 / NI
+    bufs = [dev(volt[t].reshape(-1).view(np.uint8)) for t in range(2)]
+    outs = []
+    for graphs in (False, True):
+        p = make_pipeline(vgb_mod, torch, filt, syn, tabs, invw)
+        p.enable_graphs(graphs)
+        res = []
+        for t in range(4):
+            p.run_device(bufs[t % 2])
+            ps = np.empty((NS, 4, NCC * K), np.uint8)
+            vd = np.empty((NCC, NS, 544), np.uint8)
+            p.fetch(ps, None, None, vd)
+            res.append((ps, vd))
+            assert p.launch_count() == 4
+        p.close()
+        outs.append(res)
+    for (a, b), (c, d) in zip(outs[0], outs[1]):
+        assert np.array_equal(a, c) and np.array_equal(b, d)
