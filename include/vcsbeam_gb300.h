@@ -69,6 +69,11 @@ int vgb_filter_fp32_exact(const int32_t *filter, int ntaps, int nchan);
 /* Copies and clears the device status word of the current device (after
  * synchronising `stream`). Returns VGB_ERR_DEVICE if any bit was set. */
 int vgb_check_device_status(void *stream, unsigned *flags_out);
+/* Self-test of the bounded waits: one kernel waits on an mbarrier that
+ * nothing arrives on for `polls` polls, gives up and flags the device status
+ * word (VGB_ERR_DEVICE from vgb_check_device_status; the context stays
+ * usable). */
+int vgb_selftest_bounded_wait(int polls, void *stream);
 
 /*
  * Where one second of MWAX voltages lives, per coarse channel. Window frame
@@ -472,6 +477,16 @@ int vgb_pipeline_enable_timing(vgb_pipeline *p, int on);
  * input buffer, second parity and output set); on by default, bypassed while
  * stage timing is on. */
 int vgb_pipeline_enable_graphs(vgb_pipeline *p, int on);
+/* Checkpoint / resume at a second boundary: the state the next second needs
+ * (the last 12 voltage frames of each input, the last 12 beam samples of each
+ * coarse channel for the inverse PFB, the second counter) to / from a host
+ * buffer of vgb_pipeline_state_bytes bytes. A pipeline of the same
+ * configuration that loads it continues bit-identically (the reference
+ * carries the same state in its read-buffer margin and IPFB buffer,
+ * buffer.c:106-124, pfb.cpp:950-976). */
+long long vgb_pipeline_state_bytes(const vgb_pipeline *p);
+int vgb_pipeline_save_state(vgb_pipeline *p, void *host, long long bytes);
+int vgb_pipeline_load_state(vgb_pipeline *p, const void *host, long long bytes);
 /* Milliseconds per stage of the last second: [0] fused PFB + beamformer,
  * [1] renormalise, [2] inverse PFB + VDIF, [3] history carry. Synchronises. */
 int vgb_pipeline_stage_ms(vgb_pipeline *p, float *ms, int n);

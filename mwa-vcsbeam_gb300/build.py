@@ -70,7 +70,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_v: bool = False) -> 
             if r.returncode:
                 raise RuntimeError("nvcc failed: " + " ".join(cmd))
     if force or jobs or not os.path.exists(LIB):
-        link = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcuda"]
+        link = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcuda", "-ldl"]
         r = subprocess.run(link, capture_output=True, text=True)
         if r.returncode:
             raise RuntimeError("link failed:\n" + r.stdout + r.stderr)

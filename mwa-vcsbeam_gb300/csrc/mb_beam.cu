@@ -1167,6 +1167,7 @@ namespace {
 int mb_run_cc(vgb_multibeam *mb, int cc, const uint8_t *v_cc, float *S_cc, uint8_t *out_cc, float *off_cc,
               float *scl_cc, cudaStream_t st, unsigned *status)
 {
+    NvtxRange range("vgb: multibeam coarse channel");
     const vgb_multibeam_config &c = mb->cfg;
     const int A = c.nant, nf = c.nfine, ns = c.nsamples;
     const long long nrow = (long long)nf * c.npointing * c.nstokes;

@@ -111,6 +111,29 @@ int vgb_filter_fp32_exact(const int32_t *filter, int ntaps, int nchan)
     return worst * 127 < (1LL << 24) ? 1 : 0;
 }
 
+// A wait on an mbarrier that nothing arrives on, limited to `polls` polls:
+// the kernel gives up, records kErrWaitTimeout in the status word and
+// returns, as every bounded wait in the library does on expiry.
+__global__ void selftest_wait_kernel(uint32_t polls, unsigned *status)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !mbar_wait_bounded(&bar, 0, polls)) atomicOr(status, kErrWaitTimeout);
+}
+
+int vgb_selftest_bounded_wait(int polls, void *stream)
+{
+    if (polls <= 0 || polls > (1 << 24)) return set_error(VGB_ERR_INVALID, "selftest_bounded_wait: polls 1..2^24");
+    unsigned *status = status_word();
+    if (!status) return set_error(VGB_ERR_CUDA, "device status word unavailable");
+    selftest_wait_kernel<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>((uint32_t)polls, status);
+    return check_launch("selftest_wait_kernel");
+}
+
 int vgb_check_device_status(void *stream, unsigned *flags_out)
 {
     unsigned *p = status_word();
@@ -389,6 +412,7 @@ template <class T> int dalloc(T **p, size_t bytes)
 // One second of compute on s_comp with the voltages at `volt`.
 int pipeline_second(vgb_pipeline *p, const char2 *volt, long long cc_stride_bytes)
 {
+    NvtxRange range("vgb: pipeline second");
     const vgb_pipeline_config &c = p->cfg;
     const int cur = (int)(p->second & 1), nxt = cur ^ 1;
     int rc;
@@ -625,6 +649,69 @@ int vgb_pipeline_run_device(vgb_pipeline *p, const void *d_voltages, long long c
     if (cur_cc_stride < p->second_bytes && p->cfg.ncc > 1)
         return set_error(VGB_ERR_INVALID, "coarse-channel stride smaller than one second");
     return pipeline_second_graph(p, static_cast<const char2 *>(d_voltages), cur_cc_stride);
+}
+
+// Carry-over state between seconds: a header, the 12 voltage frames of each
+// input and the 12 beam samples of each coarse channel the next second reads.
+struct PipelineStateHeader {
+    uint32_t magic, version;
+    int32_t ncc, ninputs, nblocks, do_ipfb;
+    int64_t second;
+};
+constexpr uint32_t kStateMagic = 0x56474253u; // "VGBS"
+
+static long long state_hist_bytes(const vgb_pipeline *p)
+{
+    return (long long)p->cfg.ncc * p->ninputs * kHistFrames * kK * 2;
+}
+static long long state_ehist_bytes(const vgb_pipeline *p) { return (long long)sizeof(float4) * p->cfg.ncc * kHistFrames * kK; }
+
+long long vgb_pipeline_state_bytes(const vgb_pipeline *p)
+{
+    return p ? (long long)sizeof(PipelineStateHeader) + state_hist_bytes(p) + state_ehist_bytes(p) : 0;
+}
+
+int vgb_pipeline_save_state(vgb_pipeline *p, void *host, long long bytes)
+{
+    if (!p || !host) return set_error(VGB_ERR_INVALID, "pipeline_save_state: NULL argument");
+    if (bytes < vgb_pipeline_state_bytes(p)) return set_error(VGB_ERR_INVALID, "pipeline_save_state: buffer too small");
+    int rc = check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
+    if (rc) return rc;
+    PipelineStateHeader h{kStateMagic, 1, p->cfg.ncc, p->ninputs, p->cfg.nblocks, p->cfg.do_ipfb, p->second};
+    char *out = static_cast<char *>(host);
+    std::memcpy(out, &h, sizeof(h));
+    const int cur = (int)(p->second & 1);
+    rc = check_cuda(cudaMemcpy(out + sizeof(h), p->d_hist[cur], state_hist_bytes(p), cudaMemcpyDeviceToHost),
+                    "save voltage history");
+    if (!rc)
+        rc = check_cuda(cudaMemcpy(out + sizeof(h) + state_hist_bytes(p), p->d_ehist[cur], state_ehist_bytes(p),
+                                   cudaMemcpyDeviceToHost),
+                        "save beam history");
+    return rc;
+}
+
+int vgb_pipeline_load_state(vgb_pipeline *p, const void *host, long long bytes)
+{
+    if (!p || !host) return set_error(VGB_ERR_INVALID, "pipeline_load_state: NULL argument");
+    if (bytes < vgb_pipeline_state_bytes(p)) return set_error(VGB_ERR_INVALID, "pipeline_load_state: buffer too small");
+    PipelineStateHeader h;
+    std::memcpy(&h, host, sizeof(h));
+    if (h.magic != kStateMagic || h.version != 1 || h.ncc != p->cfg.ncc || h.ninputs != p->ninputs ||
+        h.nblocks != p->cfg.nblocks || h.do_ipfb != p->cfg.do_ipfb || h.second < 0)
+        return set_error(VGB_ERR_INVALID, "pipeline_load_state: state is from a different pipeline configuration");
+    int rc = check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
+    if (rc) return rc;
+    drop_graphs(p);
+    p->second = h.second;
+    const int cur = (int)(p->second & 1);
+    const char *in = static_cast<const char *>(host);
+    rc = check_cuda(cudaMemcpy(p->d_hist[cur], in + sizeof(h), state_hist_bytes(p), cudaMemcpyHostToDevice),
+                    "load voltage history");
+    if (!rc)
+        rc = check_cuda(cudaMemcpy(p->d_ehist[cur], in + sizeof(h) + state_hist_bytes(p), state_ehist_bytes(p),
+                                   cudaMemcpyHostToDevice),
+                        "load beam history");
+    return rc;
 }
 
 int vgb_pipeline_enable_graphs(vgb_pipeline *p, int on)

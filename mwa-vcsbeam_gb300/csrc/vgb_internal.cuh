@@ -13,7 +13,19 @@
 
 #include "../../include/vcsbeam_gb300.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 namespace vgb {
+
+// NVTX range for the lifetime of a scope (visible in Nsight timelines; a
+// no-op when no tool is attached).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 
 constexpr int kVSPVB = 64000;               // samples per MWAX voltage block
 constexpr int kK = 128;                     // fine channels (FFT length)

@@ -154,6 +154,10 @@ _SIGS = {
     "vgb_pipeline_sync": (I, [V]),
     "vgb_pipeline_enable_timing": (I, [V, I]),
     "vgb_pipeline_enable_graphs": (I, [V, I]),
+    "vgb_pipeline_state_bytes": (LL, [V]),
+    "vgb_pipeline_save_state": (I, [V, V, LL]),
+    "vgb_pipeline_load_state": (I, [V, V, LL]),
+    "vgb_selftest_bounded_wait": (I, [I, V]),
     "vgb_pipeline_stage_ms": (I, [V, ctypes.POINTER(Fl), I]),
 }
 
@@ -298,6 +302,11 @@ def ipfb(e, e_job_stride, hist, hist_job_stride, coeffs, nsamples, njobs, out_f=
          frame_offset=0, stream=None):
     check(lib().vgb_ipfb(ptr(e), e_job_stride, ptr(hist), hist_job_stride, ptr(coeffs), NTAPS, NCHAN, nsamples,
                          njobs, ptr(out_f), ptr(vdif), ptr(hdr), frame_offset, stream_ptr(stream)))
+
+
+def selftest_bounded_wait(polls=1000, stream=None):
+    """Make one bounded mbarrier wait expire on purpose (see the C header)."""
+    check(lib().vgb_selftest_bounded_wait(polls, stream_ptr(stream)))
 
 
 def check_device_status(stream=None) -> int:
@@ -588,6 +597,16 @@ class Pipeline:
 
     def enable_graphs(self, on: bool = True):
         check(lib().vgb_pipeline_enable_graphs(self.h, int(on)))
+
+    def save_state(self) -> np.ndarray:
+        """The carry-over state of the next second (for resume)."""
+        buf = np.empty(lib().vgb_pipeline_state_bytes(self.h), dtype=np.uint8)
+        check(lib().vgb_pipeline_save_state(self.h, buf.ctypes.data, buf.size))
+        return buf
+
+    def load_state(self, buf: np.ndarray):
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        check(lib().vgb_pipeline_load_state(self.h, buf.ctypes.data, buf.size))
 
     def stage_ms(self):
         arr = (Fl * 4)()

@@ -216,6 +216,20 @@ def test_multibeam_run_host_streams(vgb_mod, torch, oracle_mod):
     mb.close()
 
 
+def test_multibeam_all_tiles_flagged(vgb_mod, torch, oracle_mod):
+    """Every tile flagged (D = 0, as calibration.c's NaN rows become): all
+    weights vanish, Stokes are exactly 0 and the 8-bit stage gives the
+    reference's bytes for a constant row (scale 0 -> NaN quotient -> 0)."""
+    nant, npnt, nfine, ns = 16, 32, 32, 100
+    case = make_case(oracle_mod, nant, npnt, nfine, ns, seed=41)
+    case["D"][:] = 0.0
+    res = run_mb(vgb_mod, torch, case, nant, npnt, nfine, ns, 4, 0, psrfits=True)
+    assert np.all(res["S"] == 0)
+    assert np.all(res["out"] == 0) and np.all(res["scl"] == 0) and np.all(res["off"] == 0)
+    off, scl, u8 = oracle_mod.renormalise(np.ascontiguousarray(res["S"].transpose(1, 3, 2, 0)))
+    assert np.array_equal(res["out"], u8)
+
+
 def test_multibeam_rejects_bad_config(vgb_mod):
     with pytest.raises(vgb_mod.VGBError, match="multiple of 16"):
         vgb_mod.Multibeam(1, 4, 20, 8, 100)

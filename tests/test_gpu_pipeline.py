@@ -152,3 +152,38 @@ def test_pipeline_graph_replay_equals_eager(vgb_mod, torch, setup):
         outs.append(res)
     for (a, b), (c, d) in zip(outs[0], outs[1]):
         assert np.array_equal(a, c) and np.array_equal(b, d)
+
+
+def test_pipeline_checkpoint_resume(vgb_mod, torch, setup):
+    """Save the carry-over state after two seconds, load it into a new
+    pipeline and continue: seconds 3 and 4 equal those of an uninterrupted
+    run (voltage history, inverse-PFB history and the second counter)."""
+    volt, filt, syn, tabs = setup
+    invw = 1.0 / NI
+    bufs = [dev(volt[t].reshape(-1).view(np.uint8)) for t in range(2)]
+
+    def second(p, t):
+        p.run_device(bufs[t % 2])
+        ps = np.empty((NS, 4, NCC * K), np.uint8)
+        vd = np.empty((NCC, NS, 544), np.uint8)
+        p.fetch(ps, None, None, vd)
+        return ps, vd
+
+    a = make_pipeline(vgb_mod, torch, filt, syn, tabs, invw)
+    straight = [second(a, t) for t in range(4)]
+    a.close()
+    b = make_pipeline(vgb_mod, torch, filt, syn, tabs, invw)
+    for t in range(2):
+        second(b, t)
+    state = b.save_state()
+    b.close()
+    c = make_pipeline(vgb_mod, torch, filt, syn, tabs, invw)
+    c.load_state(state)
+    for t in (2, 3):
+        ps, vd = second(c, t)
+        assert np.array_equal(ps, straight[t][0]) and np.array_equal(vd, straight[t][1])
+    bad = state.copy()
+    bad[8:12] = 0                      # another ncc
+    with pytest.raises(vgb_mod.VGBError, match="different pipeline configuration"):
+        c.load_state(bad)
+    c.close()
