@@ -72,11 +72,13 @@ __device__ __forceinline__ uint32_t issue_frames(const VoltView &vv, int cc, int
     return bytes;
 }
 
-// Producer: one thread queues step `it`'s frames (and, when W is given, the
-// weight rows of its two tiles) into stage it & 1.
+// Producer: warp 0 queues step `it`'s frames (and, when W is given, the
+// weight rows of its two tiles) into stage it & 1, one input per lane (lane
+// kG the weights), so the copy set-up costs the warp about one input's worth.
 __device__ __forceinline__ void produce(FrontSmem &sm, const VoltView &vv, int cc, int it, int m0, int nspectra,
                                        const float4 *Wcc, int nant, unsigned *status)
 {
+    const int lane = threadIdx.x & 31;
     const int s = it & 1;
     const int w_end = min(m0 + kWin, nspectra + kP - 1);
     uint32_t total = 0;
@@ -87,17 +89,19 @@ __device__ __forceinline__ void produce(FrontSmem &sm, const VoltView &vv, int c
         nw = min(2, nant - 2 * it);
         total += nw * kK * 32;
     }
-    mbar_arrive_expect_tx(&sm.bar[s], total);
+    if (lane == 0) mbar_arrive_expect_tx(&sm.bar[s], total);
+    __syncwarp();
     uint32_t issued = 0;
-    for (int li = 0; li < kG; li++) {
-        const int i = it * kG + li;
-        if (i < vv.ninputs) issued += issue_frames(vv, cc, i, m0, w_end, sm.stage[s][li][0], &sm.bar[s], status);
-    }
-    if (nw > 0) {
+    if (lane < kG) {
+        const int i = it * kG + lane;
+        if (i < vv.ninputs) issued = issue_frames(vv, cc, i, m0, w_end, sm.stage[s][lane][0], &sm.bar[s], status);
+    } else if (lane == kG && nw > 0) {
         bulk_g2s(sm.wst[s][0][0], Wcc + (long long)(2 * it) * kK * 2, nw * kK * 32, &sm.bar[s]);
-        issued += nw * kK * 32;
+        issued = nw * kK * 32;
     }
-    if (issued != total) {
+#pragma unroll
+    for (int o = 4; o; o >>= 1) issued += __shfl_xor_sync(0xffffffffu, issued, o);
+    if (lane == 0 && issued != total) {
         // Some frames were outside the buffers: complete the remaining
         // transaction count so consumers are not left waiting; the status
         // word already records the error.
@@ -310,7 +314,7 @@ __global__ void __launch_bounds__(kThreads, 2) beam_kernel(const BeamArgs a)
     const int li = tid >> 6, n0 = 2 * (tid & 63);
     load_taps(a.filter, n0, hc);
     __syncthreads();
-    if (tid == 0) produce(sm, a.vv, cc, 0, m0, a.nspectra, Wcc, a.nant, a.status);
+    if (tid < 32) produce(sm, a.vv, cc, 0, m0, a.nspectra, Wcc, a.nant, a.status);
 
     // beam accumulators for (k', m = mh + 2 mi)
     const int kp = tid & (kK - 1), mh = tid >> 7;
@@ -326,7 +330,7 @@ __global__ void __launch_bounds__(kThreads, 2) beam_kernel(const BeamArgs a)
             return;
         }
         // everyone has finished step it-1, so its buffers may be refilled
-        if (tid == 0 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, Wcc, a.nant, a.status);
+        if (tid < 32 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, Wcc, a.nant, a.status);
         wola_step<kInt32, kFpga>(sm, it & 1, li, n0, hc);
         __syncthreads();
         fft_step<kDemote>(sm, tid);
@@ -401,7 +405,7 @@ __global__ void __launch_bounds__(kThreads, 2) pack_kernel(const PackArgs a)
     const int li = tid >> 6, n0 = 2 * (tid & 63);
     load_taps(a.filter, n0, hc);
     __syncthreads();
-    if (tid == 0) produce(sm, a.vv, cc, 0, m0, a.nspectra, nullptr, 0, a.status);
+    if (tid < 32) produce(sm, a.vv, cc, 0, m0, a.nspectra, nullptr, 0, a.status);
 
     const bool int4 = (a.flags & VGB_PFB_COMPLEX_INT4) != 0;
     const bool imag_first = (a.flags & VGB_PFB_IMAG_PART_FIRST) != 0;
@@ -411,7 +415,7 @@ __global__ void __launch_bounds__(kThreads, 2) pack_kernel(const PackArgs a)
             drain(sm, it);
             return;
         }
-        if (tid == 0 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, nullptr, 0, a.status);
+        if (tid < 32 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, nullptr, 0, a.status);
         wola_step<kInt32, kFpga>(sm, it & 1, li, n0, hc);
         __syncthreads();
         fft_step<kDemote>(sm, tid);
