@@ -249,6 +249,17 @@ int vgb_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, v
 int vgb_gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, int batch, int fp16,
                      void *stream);
 
+/* Tied-array array factor (calc_array_factor, geometry.c:440-467; Eq. A4 of
+ * Meyers et al. 2017) of the look direction at npix test directions, FP64 on
+ * the device: af[i] = |sum_a conj(w_a) psi_a|^2 / nant^2 with the geometric
+ * phases of vgb_phase at frequency freq_hz (cast to whole Hz as the
+ * reference does). look [3], dirs [npix][3] (E, N, H direction cosines),
+ * tile east/north/height/cable [nant], af [npix]: device pointers. The
+ * building block of the PSF tool (app/mwa_tied_array_beam_psf.c). */
+int vgb_array_factor(const double *look, const double *dirs, int npix, double freq_hz, const double *east,
+                     const double *north, const double *height, const double *cable, double href, int nant,
+                     double *af, void *stream);
+
 /* ---- table inputs on the host: calibration solutions, filter files ----
  * D layout: [nant][nfine][2][2] complex double (D_IDX, vcsbeam.h.in:242-251). */
 

@@ -47,6 +47,54 @@ __global__ void phase_kernel(const double *unit, const double *east, const doubl
     phi[idx] = make_double2(co, s);
 }
 
+// geometry.c:440-467 (calc_array_factor; Eq. A4 of Meyers et al. 2017): the
+// tied-array response of the look direction's phases w at test direction
+// psi, |sum_a conj(w_a) psi_a|^2 / nant^2. One block per test direction, the
+// phases in FP64 with the geometric-delay kernel's operation order, the sum
+// as the reference's sequential complex additions (thread 0 adds the tiles in
+// order after each thread formed its products).
+__global__ void array_factor_kernel(const double *look, const double *dirs, int npix, double freq,
+                                    const double *east, const double *north, const double *height,
+                                    const double *cable, double href, int nant, double *af)
+{
+    extern __shared__ double2 prod[];
+    const int pix = blockIdx.x;
+    if (pix >= npix) return;
+    const double f = (double)(uint32_t)freq;
+    for (int a = threadIdx.x; a < nant; a += blockDim.x) {
+        double2 ph[2];
+        for (int k = 0; k < 2; k++) {
+            const double *u = k == 0 ? look : dirs + 3 * pix;
+            const double L = cable[a] - 0.0;
+            const double w = (east[a] - 0.0) * u[0] + (north[a] - 0.0) * u[1] + (height[a] - href) * u[2];
+            const double dt = (w - L) / 299792458.0;
+            const double phase = 2.0 * 3.14159265358979323846 * dt * f;
+            double sn, cs;
+            sincos(phase, &sn, &cs);
+            ph[k] = make_double2(cs, sn);
+        }
+        // conj(w) * psi
+        prod[a] = make_double2(ph[0].x * ph[1].x + ph[0].y * ph[1].y, ph[0].x * ph[1].y - ph[0].y * ph[1].x);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double2 s = make_double2(0.0, 0.0);
+        for (int a = 0; a < nant; a++) s = make_double2(s.x + prod[a].x, s.y + prod[a].y);
+        const double m = hypot(s.x, s.y) / nant;
+        af[pix] = m * m;
+    }
+}
+
+int launch_array_factor(const double *look, const double *dirs, int npix, double freq, const double *east,
+                        const double *north, const double *height, const double *cable, double href, int nant,
+                        double *af, cudaStream_t st)
+{
+    if (npix <= 0) return VGB_SUCCESS;
+    array_factor_kernel<<<npix, 128, sizeof(double2) * nant, st>>>(look, dirs, npix, freq, east, north, height,
+                                                                    cable, href, nant, af);
+    return check_launch("array_factor_kernel");
+}
+
 // jones.c:97-157: J = inv2x2S(D[a][c] B[p][a] / ||D B||_F), zero if the norm is 0.
 __global__ void jones_kernel(const double2 *D, const double2 *B, int npointing, int nant, int nchan, double2 *J)
 {

@@ -251,6 +251,16 @@ int vgb_phase(const double *unit, const double *east, const double *north, const
                         static_cast<double2 *>(phi), S(stream));
 }
 
+int vgb_array_factor(const double *look, const double *dirs, int npix, double freq_hz, const double *east,
+                     const double *north, const double *height, const double *cable, double href, int nant, double *af,
+                     void *stream)
+{
+    if (!look || !dirs || !east || !north || !height || !cable || !af)
+        return set_error(VGB_ERR_INVALID, "array_factor: NULL argument");
+    if (npix < 0 || nant <= 0 || nant > 6000) return set_error(VGB_ERR_INVALID, "array_factor: bad sizes");
+    return launch_array_factor(look, dirs, npix, freq_hz, east, north, height, cable, href, nant, af, S(stream));
+}
+
 int vgb_jones(const void *D, const void *B, int npointing, int nant, int nchan, void *J, void *stream)
 {
     if (!D || !B || !J) return set_error(VGB_ERR_INVALID, "NULL table pointer");

@@ -103,6 +103,9 @@ struct PbArgs { // primary-beam model evaluation
     double2 *B;                  // [nfreq][npointing][ntile][4]
 };
 int launch_beam_model(const PbArgs &a, cudaStream_t st);
+int launch_array_factor(const double *look, const double *dirs, int npix, double freq, const double *east,
+                        const double *north, const double *height, const double *cable, double href, int nant,
+                        double *af, cudaStream_t st);
 int gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, int batch, bool fp16,
                  cudaStream_t st, int Kb);
 int launch_pack_staged(const float2 *ffted, int nspectra, int ninputs, const int *i_idx, unsigned flags,

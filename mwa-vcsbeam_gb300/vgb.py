@@ -127,6 +127,7 @@ _SIGS = {
     "vgb_surrogate_gradients": (I, [V, V, V, V, V, V]),
     "vgb_surrogate_validate": (I, [V, LL, Fl, V, V]),
     "vgb_surrogate_beam": (I, [V, V, V, I, V, I, V, V, I, ctypes.c_double, I, V, V, V]),
+    "vgb_array_factor": (I, [V, V, I, ctypes.c_double, V, V, V, V, ctypes.c_double, I, V, V]),
     "vgb_multibeam_create": (I, [V, V]),
     "vgb_multibeam_destroy": (None, [V]),
     "vgb_multibeam_set_geometry": (I, [V, V, V, V, V, V, ctypes.c_double, V]),
@@ -393,6 +394,13 @@ def primary_beam(az, za, freq_hz, delays, B, pa_correction=True, latitude=MWA_LA
     check(lib().vgb_primary_beam(ptr(az), ptr(za), int(az.numel()), ptr(freq_hz), int(freq_hz.numel()),
                                  ptr(delays), int(delays.numel() // 16), float(latitude), int(bool(pa_correction)),
                                  ptr(B), stream_ptr(stream)))
+
+
+def array_factor(look, dirs, freq_hz, east, north, height, cable, out, href=377.827, stream=None):
+    """Tied-array array factor of `look` at each of `dirs` (device tensors)."""
+    check(lib().vgb_array_factor(ptr(look), ptr(dirs), int(dirs.numel() // 3), float(freq_hz), ptr(east), ptr(north),
+                                 ptr(height), ptr(cable), float(href), int(east.numel()), ptr(out),
+                                 stream_ptr(stream)))
 
 
 def hash_dipole_config(amps) -> int:

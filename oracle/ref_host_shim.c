@@ -87,6 +87,44 @@ int refhost_load_filter(char *name, int synthesis, int nchans, double scale,
     return nc;
 }
 
+/* geometry.c:440-467 calc_array_factor between a look direction and each of
+ * npix test directions (Eq. A4 of Meyers et al. 2017). */
+void refhost_array_factor(const double *look, const double *dirs, int npix, uint32_t freq_hz, int nant,
+                          const double *east, const double *north, const double *height, const double *cable,
+                          double *af)
+{
+    MetafitsMetadata md;
+    memset(&md, 0, sizeof(md));
+    Rfinput *rf = (Rfinput *)calloc(2 * nant, sizeof(Rfinput));
+    static char X[] = "X", Y[] = "Y";
+    for (int a = 0; a < nant; a++)
+        for (int p = 0; p < 2; p++) {
+            Rfinput *r = &rf[2 * a + p];
+            r->ant = a;
+            r->pol = p ? Y : X;
+            r->east_m = east[a];
+            r->north_m = north[a];
+            r->height_m = height[a];
+            r->electrical_length_m = cable[a];
+        }
+    md.rf_inputs = rf;
+    md.num_rf_inputs = 2 * nant;
+    md.num_ants = nant;
+    beam_geom b1, b2;
+    memset(&b1, 0, sizeof(b1));
+    b1.unit_E = look[0];
+    b1.unit_N = look[1];
+    b1.unit_H = look[2];
+    for (int i = 0; i < npix; i++) {
+        memset(&b2, 0, sizeof(b2));
+        b2.unit_E = dirs[3 * i];
+        b2.unit_N = dirs[3 * i + 1];
+        b2.unit_H = dirs[3 * i + 2];
+        af[i] = calc_array_factor(&md, freq_hz, &b1, &b2);
+    }
+    free(rf);
+}
+
 /* ---- calibration.c (vmLoadOffringaSolution, vmLoadRTSSolution,
  * vmApplyCalibrationCorrections, parse_calibration_correction_file) driven
  * through a vcsbeam_context populated with the fields those routines read:

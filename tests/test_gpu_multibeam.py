@@ -230,6 +230,25 @@ def test_multibeam_all_tiles_flagged(vgb_mod, torch, oracle_mod):
     assert np.array_equal(res["out"], u8)
 
 
+def test_multibeam_against_reference_kernels(vgb_mod, torch):
+    """Five pointings of the reference's own beamformer kernels
+    (tests/golden/ref_golden_multibeam.npz), summed over each 10-sample
+    integration, against the tensor-core path built from the same D, B,
+    geometry and voltages (split BF16: within 1e-3)."""
+    import os
+
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                  "ref_golden_multibeam.npz")))
+    npnt, ns, nst, nfine = g["S"].shape[0], g["S"].shape[1], 4, g["S"].shape[3]
+    nant = g["D"].shape[0]
+    case = dict(D=g["D"], B=g["B"], unit=g["unit"], east=g["east"], north=g["north"], height=g["height"],
+                cable=g["cable"], freqs=g["freqs"], polQ=g["polQ"], polP=g["polP"], v_dev=np.ascontiguousarray(g["v"]))
+    res = run_mb(vgb_mod, torch, case, nant, npnt, nfine, ns, nst, 0, invw=float(g["invw"]))
+    ref = g["S"].astype(np.float64).reshape(npnt, ns // NINT, NINT, nst, nfine).sum(axis=2).transpose(3, 0, 2, 1)
+    errs = stokes_err(res["S"], ref)
+    assert max(errs) < 1e-3, errs
+
+
 def test_multibeam_rejects_bad_config(vgb_mod):
     with pytest.raises(vgb_mod.VGBError, match="multiple of 16"):
         vgb_mod.Multibeam(1, 4, 20, 8, 100)
