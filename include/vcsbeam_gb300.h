@@ -248,6 +248,10 @@ int vgb_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, v
  */
 int vgb_gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, int batch, int fp16,
                      void *stream);
+/* Force the GEMM kernel variant for shapes whose N is a multiple of 256 (128
+ * or 256: the plain kernel's tile width; 512: the persistent kernel), or 0 for
+ * the autotuned choice. Returns the previous setting (-1 on a bad value). */
+int vgb_gemm_variant(int v);
 
 /* Tied-array array factor (calc_array_factor, geometry.c:440-467; Eq. A4 of
  * Meyers et al. 2017) of the look direction at npix test directions, FP64 on

@@ -161,21 +161,166 @@ __global__ void __launch_bounds__(128, 1)
     if (warp == 0) tmem_dealloc(tmem, BN);
 }
 
+
+// ---------------------------------------------------------------------------
+// Persistent form: one 192-thread CTA per SM walks the (batch, n, m) tiles of
+// 128 x 256; warp 0 streams K chunks through a 4-stage TMA ring, warp 1 issues
+// the MMAs into one of two 256-column TMEM accumulators, warps 2-5 (TMEM lane
+// quarter = warp % 4) store the other one, so a tile's epilogue overlaps the
+// next tile's MMAs. Same operands, K order and results as gemm_bf16_kernel.
+// ---------------------------------------------------------------------------
+constexpr int kPStages = 4;
+struct PersistSmem {
+    uint8_t a[kPStages][kTileBytes];
+    uint8_t b[kPStages][256 * 128];
+    uint64_t full[kPStages], empty[kPStages];
+    uint64_t tfull[2], tempty[2], drain;
+    uint32_t tmem;
+};
+
+template <bool kF16>
+__global__ void __launch_bounds__(192, 1)
+    gemm_persist_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, float *C,
+                        int M, int N, int K, int Kb, int batch, unsigned *status)
+{
+    extern __shared__ uint8_t pg_raw[];
+    PersistSmem &sm =
+        *reinterpret_cast<PersistSmem *>((reinterpret_cast<uintptr_t>(pg_raw) + 1023) & ~uintptr_t(1023));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int mt = M / 128, ntile = N / 256, nk = K / 64;
+    const long long total = (long long)batch * ntile * mt;
+
+    if (threadIdx.x == 0) {
+        prefetch_tmap(&ta);
+        prefetch_tmap(&tb);
+        for (int s = 0; s < kPStages; s++) {
+            mbar_init(&sm.full[s], 1);
+            mbar_init(&sm.empty[s], 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&sm.tfull[b], 1);
+            mbar_init(&sm.tempty[b], 4);
+        }
+        mbar_init(&sm.drain, 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    if (warp == 0) {
+        tmem_alloc(&sm.tmem, 512);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = sm.tmem;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            uint32_t it = 0;
+            bool ok = true;
+            for (long long t = blockIdx.x; t < total && ok; t += gridDim.x) {
+                const int m = (int)(t % mt), n = (int)((t / mt) % ntile), b = (int)(t / ((long long)mt * ntile));
+                for (int kc = 0; kc < nk; kc++, it++) {
+                    const int s = it % kPStages;
+                    const uint32_t r = it / kPStages;
+                    if (r > 0 && !mbar_wait_bounded(&sm.empty[s], (r - 1) & 1, kWaitPolls)) {
+                        atomicOr(status, kErrWaitTimeout);
+                        ok = false;
+                        break;
+                    }
+                    mbar_arrive_expect_tx(&sm.full[s], kTileBytes + 256 * 128);
+                    tma_load_2d(sm.a[s], &ta, kc * 64, b * M + m * 128, &sm.full[s]);
+                    tma_load_2d(sm.b[s], &tb, (kc * 64) % Kb, b * N + n * 256, &sm.full[s]);
+                }
+            }
+            for (uint32_t k = (it > kPStages ? it - kPStages : 0); k < it; k++)
+                mbar_wait_bounded(&sm.full[k % kPStages], (k / kPStages) & 1, kWaitPolls);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16_f32(256, false, kF16);
+            uint32_t it = 0, tc = 0;
+            bool ok = true;
+            for (long long t = blockIdx.x; t < total && ok; t += gridDim.x, tc++) {
+                const int buf = tc & 1;
+                const uint32_t u = tc >> 1;
+                if (u > 0 && !mbar_wait_bounded(&sm.tempty[buf], (u - 1) & 1, kWaitPolls)) {
+                    atomicOr(status, kErrWaitTimeout);
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d = tmem + buf * 256;
+                for (int kc = 0; kc < nk; kc++, it++) {
+                    const int s = it % kPStages;
+                    if (!mbar_wait_bounded(&sm.full[s], (it / kPStages) & 1, kWaitPolls)) {
+                        atomicOr(status, kErrWaitTimeout);
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint64_t ad = sdesc_sw128(smem_u32(sm.a[s])), bd = sdesc_sw128(smem_u32(sm.b[s]));
+#pragma unroll
+                    for (int k = 0; k < 4; k++)
+                        tc_mma(d, sdesc_advance_k(ad, k), sdesc_advance_k(bd, k), idesc, (kc | k) != 0);
+                    tc_commit(&sm.empty[s]);
+                }
+                if (ok) tc_commit(&sm.tfull[buf]);
+            }
+            tc_commit(&sm.drain);
+            mbar_wait_bounded(&sm.drain, 0, kWaitPolls);
+        }
+    } else {
+        const int q4 = warp & 3;
+        uint32_t tc = 0;
+        for (long long t = blockIdx.x; t < total; t += gridDim.x, tc++) {
+            const int buf = tc & 1;
+            const int m = (int)(t % mt), n = (int)((t / mt) % ntile), b = (int)(t / ((long long)mt * ntile));
+            if (!mbar_wait_bounded(&sm.tfull[buf], (tc >> 1) & 1, kWaitPolls)) {
+                if (lane == 0) atomicOr(status, kErrWaitTimeout);
+                break;
+            }
+            tc_fence_after();
+            const int row = m * 128 + q4 * 32 + lane;
+            float *out = C + ((long long)b * M + row) * N + n * 256;
+#pragma unroll 1
+            for (int c = 0; c < 8; c++) {
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(q4 * 32) << 16) + buf * 256 + c * 32, v);
+                float4 *o = reinterpret_cast<float4 *>(out + c * 32);
+#pragma unroll
+                for (int j = 0; j < 8; j++) o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&sm.tempty[buf]);
+        }
+    }
+    __syncwarp();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 512);
+}
+
 } // namespace vgb
 
 using namespace vgb;
 
 namespace vgb {
 
-// Tile width (N of one CTA tile: 128 or 256) for a GEMM shape, chosen by
-// timing both widths on the first call with that shape (3 runs each with CUDA
-// events on the caller's stream, after one warm-up) and cached; both widths
-// give identical results (same K order per output). While a stream is being
+// Kernel variant for a GEMM shape: the plain kernel with 128- or 256-wide
+// tiles, or the persistent kernel (256-wide tiles, overlapped epilogue),
+// chosen by timing each on the first call with that shape (3 runs each with
+// CUDA events on the caller's stream, after one warm-up) and cached; all give
+// identical results (same K order per output). While a stream is being
 // captured into a graph the measured choice is used if known, else 256.
+static int g_gemm_variant = 0; // 0: autotuned; else forced (128, 256, 512)
+
 template <class Launch>
 int gemm_tile_width(int M, int N, int K, int Kb, int batch, bool fp16, cudaStream_t st, Launch &launch)
 {
     if (N % 256) return 128;
+    if (g_gemm_variant) return g_gemm_variant;
     static std::mutex mu;
     static std::map<std::tuple<int, int, int, int, int, bool>, int> cache;
     const auto key = std::make_tuple(M, N, K, Kb, batch, fp16);
@@ -197,7 +342,7 @@ int gemm_tile_width(int M, int N, int K, int Kb, int batch, bool fp16, cudaStrea
         cudaEventDestroy(e0);
         return 256;
     }
-    for (int bn : {256, 128}) {
+    for (int bn : {256, 128, 512}) {
         if (launch(bn)) break;
         cudaEventRecord(e0, st);
         for (int i = 0; i < 3; i++) launch(bn);
@@ -233,10 +378,28 @@ int gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, in
     unsigned *status = status_word();
     if (!status) return set_error(VGB_ERR_CUDA, "device status word unavailable");
     auto launch = [&](int bn) -> int {
+        // bn: 128 or 256 = the plain kernel's tile width; 512 = the persistent kernel (256-wide tiles)
         CUtensorMap ta, tb;
         int r = make_tmap_bf16(&ta, A, (uint64_t)M * batch, K, (uint64_t)K * 2, 128, fp16);
-        if (!r) r = make_tmap_bf16(&tb, B, (uint64_t)N * batch, Kb, (uint64_t)Kb * 2, bn, fp16);
+        if (!r) r = make_tmap_bf16(&tb, B, (uint64_t)N * batch, Kb, (uint64_t)Kb * 2, bn == 128 ? 128 : 256, fp16);
         if (r) return r;
+        if (bn == 512) {
+            static int nsm = 0;
+            if (!nsm) {
+                int dev = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+                if (nsm <= 0) nsm = 1;
+            }
+            const long long tiles = (long long)batch * (N / 256) * (M / 128);
+            const int grid = (int)(tiles < nsm ? tiles : nsm);
+            const int smem = (int)sizeof(PersistSmem) + 1024;
+            auto kern = fp16 ? gemm_persist_kernel<true> : gemm_persist_kernel<false>;
+            int e = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                               "cudaFuncSetAttribute(gemm_persist)");
+            if (!e) kern<<<grid, 192, smem, st>>>(ta, tb, C, M, N, K, Kb, batch, status);
+            return e ? e : check_launch("gemm_persist_kernel");
+        }
         dim3 grid(N / bn, M / 128, batch);
         auto go = [&](auto kern, int smem) {
             int e = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
@@ -258,6 +421,15 @@ int gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, in
 extern "C" int vgb_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, void *stream)
 {
     return gemm_batched(A, B, C, M, N, K, 1, false, static_cast<cudaStream_t>(stream), K);
+}
+
+extern "C" int vgb_gemm_variant(int v)
+{
+    if (v != 0 && v != 128 && v != 256 && v != 512)
+        return set_error(VGB_ERR_INVALID, "gemm_variant: 0 (autotuned), 128, 256 or 512"), -1;
+    const int prev = g_gemm_variant;
+    g_gemm_variant = v;
+    return prev;
 }
 
 extern "C" int vgb_gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, int batch, int fp16,

@@ -138,6 +138,7 @@ _SIGS = {
     "vgb_multibeam_enable_timing": (I, [V, I]),
     "vgb_multibeam_stage_ms": (I, [V, V, I]),
     "vgb_gemm_batched": (I, [V, V, V, I, I, I, I, I, V]),
+    "vgb_gemm_variant": (I, [I]),
     "vgb_pipeline_create": (I, [ctypes.POINTER(PipelineConfig), ctypes.POINTER(V)]),
     "vgb_pipeline_destroy": (I, [V]),
     "vgb_pipeline_set_filters": (I, [V, V, V]),
@@ -241,6 +242,14 @@ def beamform_mwax_psrfits_noalloc(v: Voltages, ncc, nspectra, filt, flags, W, na
 def gemm_bf16(A, B, C, M, N, K, stream=None):
     """C[M][N] = A[M][K] @ B[N][K]^T on the tensor cores (bf16 in, FP32 out)."""
     check(lib().vgb_gemm_bf16(ptr(A), ptr(B), ptr(C), M, N, K, stream_ptr(stream)))
+
+
+def gemm_variant(v: int) -> int:
+    """Force a GEMM kernel variant (0 autotuned, 128, 256, 512 persistent)."""
+    prev = lib().vgb_gemm_variant(v)
+    if prev < 0:
+        raise VGBError(lib().vgb_last_error().decode())
+    return prev
 
 
 def gemm_batched(A, B, C, M, N, K, batch, fp16=False, stream=None):

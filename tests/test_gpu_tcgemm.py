@@ -44,6 +44,33 @@ def test_gemm_batched(fp16):
     assert err < 1e-5, err
 
 
+@pytest.mark.parametrize("variant", [128, 256, 512])
+def test_gemm_variants_identical(variant):
+    """Every kernel variant the autotuner chooses between (plain 128- and
+    256-wide tiles, persistent 256-wide) gives the same bits."""
+    torch = torch_cuda()
+    import vgb
+
+    M, N, K, nb = 384, 512, 320, 3
+    g = torch.Generator(device="cuda").manual_seed(5)
+    A = torch.randn(nb, M, K, device="cuda", generator=g).to(torch.float16)
+    B = torch.randn(nb, N, K, device="cuda", generator=g).to(torch.float16)
+    C0 = torch.full((nb, M, N), float("nan"), device="cuda")
+    C1 = torch.full((nb, M, N), float("nan"), device="cuda")
+    prev = vgb.gemm_variant(128)
+    try:
+        vgb.gemm_batched(A, B, C0, M, N, K, nb, True)
+        vgb.gemm_variant(variant)
+        vgb.gemm_batched(A, B, C1, M, N, K, nb, True)
+    finally:
+        vgb.gemm_variant(prev)
+    torch.cuda.synchronize()
+    assert vgb.check_device_status() == 0
+    assert torch.equal(C0, C1)
+    ref = A.float() @ B.float().transpose(1, 2)
+    assert (C1 - ref).abs().max().item() <= 1e-5 * ref.abs().max().item()
+
+
 def test_gemm_rejects_bad_shapes():
     torch = torch_cuda()
     import vgb
