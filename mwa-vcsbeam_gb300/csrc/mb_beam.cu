@@ -185,19 +185,17 @@ __device__ __forceinline__ float2 cmulc32(float2 a, float2 b) // a * conj(b)
     return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
 
-// J^-1 for (channel c, beam p, tile a); zero when |D B|_F = 0 (jones.c:144-147).
-__device__ __forceinline__ void mb_jinv(const MbWeightArgs &w, int c, int p, int a, float2 (&J)[4])
+// J^-1 from the beam's (B^-1, Gram of B) and the channel's (D^-1, Gram of D);
+// zero when |D B|_F = 0 (jones.c:144-147).
+__device__ __forceinline__ void mb_jinv_from(const float4 h, const float4 g, const float4 b0, const float4 b1,
+                                             const float4 d0, const float4 d1, float2 (&J)[4])
 {
-    const long long pa = (long long)p * w.A + a, ca = (long long)c * w.A + a;
-    const float4 h = w.H[pa], g = w.G[ca];
     const float tr = g.x * h.x + g.y * h.y + 2.f * (g.z * h.z + g.w * h.w);
     if (!(tr > 0.f)) {
         J[0] = J[1] = J[2] = J[3] = make_float2(0.f, 0.f);
         return;
     }
     const float n = sqrtf(tr);
-    const float4 b0 = w.Binv[2 * pa], b1 = w.Binv[2 * pa + 1];
-    const float4 d0 = w.Dinv[2 * ca], d1 = w.Dinv[2 * ca + 1];
     const float2 b[4] = {make_float2(b0.x, b0.y), make_float2(b0.z, b0.w), make_float2(b1.x, b1.y),
                          make_float2(b1.z, b1.w)};
     const float2 d[4] = {make_float2(d0.x, d0.y), make_float2(d0.z, d0.w), make_float2(d1.x, d1.y),
@@ -210,6 +208,13 @@ __device__ __forceinline__ void mb_jinv(const MbWeightArgs &w, int c, int p, int
             const float2 u = cmul32(b[2 * r + 1], d[2 + col]);
             J[2 * r + col] = make_float2(n * (t.x + u.x), n * (t.y + u.y));
         }
+}
+
+// J^-1 for (channel c, beam p, tile a).
+__device__ __forceinline__ void mb_jinv(const MbWeightArgs &w, int c, int p, int a, float2 (&J)[4])
+{
+    const long long pa = (long long)p * w.A + a, ca = (long long)c * w.A + a;
+    mb_jinv_from(w.H[pa], w.G[ca], w.Binv[2 * pa], w.Binv[2 * pa + 1], w.Dinv[2 * ca], w.Dinv[2 * ca + 1], J);
 }
 
 // Autocorrelation coefficients of Stokes st over (C_QQ, C_PP, Re C_QP, Im C_QP).
@@ -239,50 +244,98 @@ __device__ __forceinline__ float from_bits(uint16_t b, bool fp16)
 // One block per (beam, channel); the threads step over tiles. Pass 1 finds the
 // largest |Q| of each Stokes row (its power-of-two scale), pass 2 writes the
 // embedded weights (hi, lo planes) and the scaled, split Q rows.
-__global__ void __launch_bounds__(128) mb_weights_kernel(const MbWeightArgs w)
+constexpr int kMbWeightThreads = 128;
+constexpr int kMbPairMaxTiles = 512; // arrays the pair kernel covers (2 tiles per thread, 256 threads)
+constexpr int kMbWeightBeams = 8;    // beams per block in the pair kernel
+
+// Phase (cos, sin) of tile a for beam p at frequency f: turns dt * f in FP64,
+// wrapped to [-1/2, 1/2], then sin/cos in FP32.
+__device__ __forceinline__ float2 mb_phase(const MbWeightArgs &w, int p, int a, double f)
 {
-    const int p = blockIdx.x, c = blockIdx.y;
-    __shared__ float smax[4][4];
-    if (threadIdx.x < w.nst && p < w.B) {
-        const long long r = ((long long)c * w.B + p) * w.nst + threadIdx.x;
-        w.stats.mn[r] = 0xFFFFFFFFu;
-        w.stats.mx[r] = 0u;
+    const double turns = w.dt[(long long)p * w.A + a] * f;
+    const float r = (float)(turns - rint(turns));
+    float sn, cs;
+    sincospif(2.f * r, &sn, &cs);
+    return make_float2(cs, sn);
+}
+
+// The embedded real rows (x, rho) of W = phase J^-1: four values per tile,
+// split into a hi part and the remainder (lo) in the GEMM's 16-bit type.
+__device__ __forceinline__ void mb_weight_halves(const float2 ph, const float2 (&J)[4], int x, int rho, bool h16,
+                                                 uint2 &hi2, uint2 &lo2)
+{
+    float val[4];
+    for (int q = 0; q < 2; q++) {
+        const float2 v = cmul32(ph, J[2 * x + q]);
+        val[2 * q + 0] = rho == 0 ? v.x : v.y;
+        val[2 * q + 1] = rho == 0 ? -v.y : v.x;
     }
-    float mx[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int a = threadIdx.x; a < w.A; a += blockDim.x) {
-        float2 J[4];
-        mb_jinv(w, c, p, a, J);
-        for (int st = 0; st < w.nst; st++) {
-            float q[4];
-            mb_qrow(J, st, q);
-            for (int j = 0; j < 4; j++) mx[st] = fmaxf(mx[st], fabsf(q[j]));
-        }
+    uint16_t hi[4], lo[4];
+    for (int j = 0; j < 4; j++) {
+        hi[j] = to_bits(val[j], h16);
+        lo[j] = to_bits(val[j] - from_bits(hi[j], h16), h16);
     }
+    hi2 = make_uint2(hi[0] | ((uint32_t)hi[1] << 16), hi[2] | ((uint32_t)hi[3] << 16));
+    lo2 = make_uint2(lo[0] | ((uint32_t)lo[1] << 16), lo[2] | ((uint32_t)lo[3] << 16));
+}
+
+// Q row values scaled by inv_scale, split into FP16 hi and lo.
+__device__ __forceinline__ void mb_q_halves(const float (&q)[4], float inv_scale, uint2 &hi2, uint2 &lo2)
+{
+    uint16_t hi[4], lo[4];
+    for (int j = 0; j < 4; j++) {
+        const float s = q[j] * inv_scale;
+        const __half h = __float2half_rn(s);
+        hi[j] = __half_as_ushort(h);
+        lo[j] = __half_as_ushort(__float2half_rn(s - __half2float(h)));
+    }
+    hi2 = make_uint2(hi[0] | ((uint32_t)hi[1] << 16), hi[2] | ((uint32_t)hi[3] << 16));
+    lo2 = make_uint2(lo[0] | ((uint32_t)lo[1] << 16), lo[2] | ((uint32_t)lo[3] << 16));
+}
+
+// Power-of-two scale of each Stokes row of Q from the block's per-warp maxima.
+__device__ __forceinline__ void mb_q_scales(const MbWeightArgs &w, int c, int p, float (&mx)[4],
+                                            float (&smax)[8][4], float (&inv_scale)[4])
+{
     for (int st = 0; st < 4; st++) {
         for (int o = 16; o; o >>= 1) mx[st] = fmaxf(mx[st], __shfl_xor_sync(0xffffffffu, mx[st], o));
         if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5][st] = mx[st];
     }
     __syncthreads();
-    float inv_scale[4];
     for (int st = 0; st < 4; st++) {
-        const float m = fmaxf(fmaxf(smax[0][st], smax[1][st]), fmaxf(smax[2][st], smax[3][st]));
+        float m = 0.f;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) m = fmaxf(m, smax[k][st]);
         int e = 0;
         if (m > 0.f && isfinite(m)) frexpf(m, &e); // m = f 2^e, f in [0.5, 1)
         inv_scale[st] = ldexpf(1.f, -e);
         if (threadIdx.x == 0 && st < w.nst) w.qscale[(long long)c * w.Mq + p * w.nst + st] = ldexpf(1.f, e);
     }
+}
+
+__device__ __forceinline__ void mb_reset_stats(const MbWeightArgs &w, int c, int p)
+{
+    if ((int)threadIdx.x < w.nst && p < w.B) {
+        const long long r = ((long long)c * w.B + p) * w.nst + threadIdx.x;
+        w.stats.mn[r] = 0xFFFFFFFFu;
+        w.stats.mx[r] = 0u;
+    }
+}
+
+// Any array size: one block per (beam, channel), threads stepping over tiles.
+// The first pass finds each Stokes row's largest |Q| (its power-of-two scale),
+// the second forms J^-1 again and writes the weight and Q rows. Also the FP32
+// CUDA-core mode's complex weights and unscaled Q rows.
+__global__ void __launch_bounds__(kMbWeightThreads) mb_weights_kernel(const MbWeightArgs w)
+{
+    const int p = blockIdx.x, c = blockIdx.y;
+    __shared__ float smax[8][4];
+    mb_reset_stats(w, c, p);
     const double f = (double)(uint32_t)w.freq[c];
-    const bool h16 = w.fp16 != 0;
     if (w.W32) {
-        // FP32 CUDA-core mode: complex weights and unscaled Q rows
         for (int a = threadIdx.x; a < w.A; a += blockDim.x) {
             float2 J[4];
             mb_jinv(w, c, p, a, J);
-            const double turns = w.dt[(long long)p * w.A + a] * f;
-            const float r = (float)(turns - rint(turns));
-            float sn, cs;
-            sincospif(2.f * r, &sn, &cs);
-            const float2 ph = make_float2(cs, sn);
+            const float2 ph = mb_phase(w, p, a, f);
             for (int x = 0; x < 2; x++) {
                 float4 *d = reinterpret_cast<float4 *>(w.W32 + ((((long long)c * w.Bp + p) * 2 + x) * w.A + a) * 2);
                 const float2 w0 = cmul32(ph, J[2 * x]), w1 = cmul32(ph, J[2 * x + 1]);
@@ -297,60 +350,128 @@ __global__ void __launch_bounds__(128) mb_weights_kernel(const MbWeightArgs w)
         }
         return;
     }
+    float mx[4] = {0.f, 0.f, 0.f, 0.f};
     for (int a = threadIdx.x; a < w.A; a += blockDim.x) {
         float2 J[4];
         mb_jinv(w, c, p, a, J);
-        // phase turns dt * f in FP64, wrapped to [-1/2, 1/2], then sin/cos in FP32
-        const double turns = w.dt[(long long)p * w.A + a] * f;
-        const float r = (float)(turns - rint(turns));
-        float sn, cs;
-        sincospif(2.f * r, &sn, &cs);
-        const float2 ph = make_float2(cs, sn);
-        float2 W[4];
-        for (int i = 0; i < 4; i++) W[i] = cmul32(ph, J[i]);
+        for (int st = 0; st < w.nst; st++) {
+            float q[4];
+            mb_qrow(J, st, q);
+            for (int j = 0; j < 4; j++) mx[st] = fmaxf(mx[st], fabsf(q[j]));
+        }
+    }
+    float inv_scale[4];
+    mb_q_scales(w, c, p, mx, smax, inv_scale);
+    const bool h16 = w.fp16 != 0;
+    for (int a = threadIdx.x; a < w.A; a += blockDim.x) {
+        float2 J[4];
+        mb_jinv(w, c, p, a, J);
+        const float2 ph = mb_phase(w, p, a, f);
         for (int x = 0; x < 2; x++)
             for (int rho = 0; rho < 2; rho++) {
-                float val[4];
-                for (int q = 0; q < 2; q++) {
-                    const float2 v = W[2 * x + q];
-                    val[2 * q + 0] = rho == 0 ? v.x : v.y;
-                    val[2 * q + 1] = rho == 0 ? -v.y : v.x;
-                }
-                uint16_t hi[4], lo[4];
-                for (int j = 0; j < 4; j++) {
-                    hi[j] = to_bits(val[j], h16);
-                    lo[j] = to_bits(val[j] - from_bits(hi[j], h16), h16);
-                }
+                uint2 hi, lo;
+                mb_weight_halves(ph, J, x, rho, h16, hi, lo);
                 const long long row = (long long)c * w.Mrows + 4 * p + 2 * x + rho;
-                uint2 *d0 = reinterpret_cast<uint2 *>(w.Aw + row * w.KA + 4 * a);
-                *d0 = make_uint2(hi[0] | ((uint32_t)hi[1] << 16), hi[2] | ((uint32_t)hi[3] << 16));
-                if (w.planes == 2) {
-                    uint2 *d1 = reinterpret_cast<uint2 *>(w.Aw + ((long long)w.nfine * w.Mrows + row) * w.KA + 4 * a);
-                    *d1 = make_uint2(lo[0] | ((uint32_t)lo[1] << 16), lo[2] | ((uint32_t)lo[3] << 16));
-                }
+                *reinterpret_cast<uint2 *>(w.Aw + row * w.KA + 4 * a) = hi;
+                if (w.planes == 2)
+                    *reinterpret_cast<uint2 *>(w.Aw + ((long long)w.nfine * w.Mrows + row) * w.KA + 4 * a) = lo;
             }
         for (int st = 0; st < w.nst; st++) {
             float q[4];
             mb_qrow(J, st, q);
-            uint16_t hi[4], lo[4];
-            for (int j = 0; j < 4; j++) {
-                const float s = q[j] * inv_scale[st];
-                const __half h = __float2half_rn(s);
-                hi[j] = __half_as_ushort(h);
-                lo[j] = __half_as_ushort(__float2half_rn(s - __half2float(h)));
-            }
-            __half *row = w.Aq + ((long long)c * w.Mq + p * w.nst + st) * w.Kq;
-            const uint2 H2 = make_uint2(hi[0] | ((uint32_t)hi[1] << 16), hi[2] | ((uint32_t)hi[3] << 16));
-            const uint2 L2 = make_uint2(lo[0] | ((uint32_t)lo[1] << 16), lo[2] | ((uint32_t)lo[3] << 16));
+            uint2 hi, lo;
+            mb_q_halves(q, inv_scale[st], hi, lo);
             // 4-bit voltages: [Q_hi (| Q_lo)] against [C]; 8-bit: [Q_hi | Q_hi (| Q_lo)] against [C_hi | C_lo]
-            *reinterpret_cast<uint2 *>(row + 4 * a) = H2;
+            __half *qrow = w.Aq + ((long long)c * w.Mq + p * w.nst + st) * w.Kq;
+            *reinterpret_cast<uint2 *>(qrow + 4 * a) = hi;
             int k = w.KA;
             if (w.int8) {
-                *reinterpret_cast<uint2 *>(row + k + 4 * a) = H2;
+                *reinterpret_cast<uint2 *>(qrow + k + 4 * a) = hi;
                 k += w.KA;
             }
-            if (w.planes == 2) *reinterpret_cast<uint2 *>(row + k + 4 * a) = L2;
+            if (w.planes == 2) *reinterpret_cast<uint2 *>(qrow + k + 4 * a) = lo;
         }
+    }
+}
+
+// Up to 512 tiles: one block per (channel, kMbWeightBeams beams), thread t owning
+// tiles 2t and 2t+1. The channel's D^-1 and its Gram terms stay in registers
+// across the block's beams, each J^-1 is formed once (and held while the
+// block finds the Q rows' scales), and every row is written with 16-byte
+// stores covering both tiles.
+__global__ void __launch_bounds__(256, 3) mb_weights_pair_kernel(const MbWeightArgs w)
+{
+    __shared__ float smax[8][4];
+    const int c = blockIdx.y;
+    const int a0 = 2 * threadIdx.x;
+    const bool live = a0 < w.A;
+    float4 dv[2][2], gv[2];
+    for (int u = 0; u < 2; u++) {
+        const long long ca = (long long)c * w.A + (live ? a0 + u : 0);
+        dv[u][0] = w.Dinv[2 * ca];
+        dv[u][1] = w.Dinv[2 * ca + 1];
+        gv[u] = w.G[ca];
+    }
+    const double f = (double)(uint32_t)w.freq[c];
+    const bool h16 = w.fp16 != 0;
+    const int p_end = min(w.Bp, ((int)blockIdx.x + 1) * kMbWeightBeams);
+    for (int p = blockIdx.x * kMbWeightBeams; p < p_end; p++) {
+        mb_reset_stats(w, c, p);
+        float mx[4] = {0.f, 0.f, 0.f, 0.f};
+        float2 J[2][4];
+        if (live) {
+            float2 ph[2];
+            for (int u = 0; u < 2; u++) {
+                const long long pa = (long long)p * w.A + a0 + u;
+                mb_jinv_from(w.H[pa], gv[u], w.Binv[2 * pa], w.Binv[2 * pa + 1], dv[u][0], dv[u][1], J[u]);
+                ph[u] = mb_phase(w, p, a0 + u, f);
+            }
+            for (int x = 0; x < 2; x++)
+                for (int rho = 0; rho < 2; rho++) {
+                    uint2 hi0, lo0, hi1, lo1;
+                    mb_weight_halves(ph[0], J[0], x, rho, h16, hi0, lo0);
+                    mb_weight_halves(ph[1], J[1], x, rho, h16, hi1, lo1);
+                    const long long row = (long long)c * w.Mrows + 4 * p + 2 * x + rho;
+                    *reinterpret_cast<uint4 *>(w.Aw + row * w.KA + 4 * a0) = make_uint4(hi0.x, hi0.y, hi1.x, hi1.y);
+                    if (w.planes == 2)
+                        *reinterpret_cast<uint4 *>(w.Aw + ((long long)w.nfine * w.Mrows + row) * w.KA + 4 * a0) =
+                            make_uint4(lo0.x, lo0.y, lo1.x, lo1.y);
+                }
+#pragma unroll
+            for (int st = 0; st < 4; st++)
+                if (st < w.nst)
+#pragma unroll
+                    for (int u = 0; u < 2; u++) {
+                        float q[4];
+                        mb_qrow(J[u], st, q);
+                        for (int j = 0; j < 4; j++) mx[st] = fmaxf(mx[st], fabsf(q[j]));
+                    }
+        }
+        float inv_scale[4];
+        mb_q_scales(w, c, p, mx, smax, inv_scale);
+        if (live) {
+#pragma unroll
+            for (int st = 0; st < 4; st++)
+                if (st < w.nst) {
+                    float q0[4], q1[4];
+                    mb_qrow(J[0], st, q0);
+                    mb_qrow(J[1], st, q1);
+                    uint2 hi0, lo0, hi1, lo1;
+                    mb_q_halves(q0, inv_scale[st], hi0, lo0);
+                    mb_q_halves(q1, inv_scale[st], hi1, lo1);
+                    const uint4 H4 = make_uint4(hi0.x, hi0.y, hi1.x, hi1.y);
+                    __half *qrow = w.Aq + ((long long)c * w.Mq + p * w.nst + st) * w.Kq;
+                    *reinterpret_cast<uint4 *>(qrow + 4 * a0) = H4;
+                    int k = w.KA;
+                    if (w.int8) {
+                        *reinterpret_cast<uint4 *>(qrow + k + 4 * a0) = H4;
+                        k += w.KA;
+                    }
+                    if (w.planes == 2)
+                        *reinterpret_cast<uint4 *>(qrow + k + 4 * a0) = make_uint4(lo0.x, lo0.y, lo1.x, lo1.y);
+                }
+        }
+        __syncthreads(); // smax is reused by the next beam
     }
 }
 
@@ -1203,7 +1324,12 @@ int mb_run_cc(vgb_multibeam *mb, int cc, const uint8_t *v_cc, float *S_cc, uint8
     w.Q32 = mb->d_Q32;
     w.stats = stats;
     w.B = c.npointing;
-    mb_weights_kernel<<<dim3(mb->Bp, nf), 128, 0, st>>>(w);
+    if (A <= kMbPairMaxTiles && !mb->d_W32) {
+        const int threads = std::max(32, (A / 2 + 31) / 32 * 32);
+        mb_weights_pair_kernel<<<dim3((mb->Bp + kMbWeightBeams - 1) / kMbWeightBeams, nf), threads, 0, st>>>(w);
+    } else {
+        mb_weights_kernel<<<dim3(mb->Bp, nf), kMbWeightThreads, 0, st>>>(w);
+    }
     if ((rc = check_launch("mb_weights_kernel"))) return rc;
     mark(cc, 1);
 
