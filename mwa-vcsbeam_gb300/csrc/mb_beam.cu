@@ -485,30 +485,39 @@ struct MbConvArgs {
     int int8, fp16;
     int ns, nfine, ni, A, nint, nint_p, Kb;
     const uint32_t *polQ, *polP;
+    unsigned *status;     // kErrBadInput when polQ / polP name an input outside the row
     uint16_t *V;
     __half *C;
 };
 
 __device__ __forceinline__ int nib4(uint32_t x) { return ((int)(x << 28)) >> 28; }
 
-// One block per (integration, channel): the 10 voltage rows (2A inputs each)
-// are staged in shared memory with 16-byte loads, then each thread gathers its
-// tiles' (Q, P) inputs through polQ/polP.
+// One block per (channel, integration), channels fastest so that neighbouring
+// blocks read neighbouring bytes of each sample: the 10 voltage rows (2A
+// inputs each) are staged in shared memory with 16-byte loads, then each
+// thread gathers its tiles' (Q, P) inputs through polQ/polP.
 __global__ void __launch_bounds__(128) mb_convert_kernel(const MbConvArgs g)
 {
     extern __shared__ uint4 conv_smem[];
     uint8_t *rows = reinterpret_cast<uint8_t *>(conv_smem);
-    const int t = blockIdx.x, c = blockIdx.y;
+    const int c = blockIdx.x, t = blockIdx.y;
     const bool h16 = g.fp16 != 0;
     const int rowbytes = g.ni * (g.int8 ? 2 : 1); // a multiple of 32 (nant % 16 == 0)
-    for (int k = 0; k < kMbInt; k++) {
-        const uint4 *src = reinterpret_cast<const uint4 *>(g.v + ((long long)(t * kMbInt + k) * g.nfine + c) * rowbytes);
-        for (int e = threadIdx.x; e < rowbytes / 16; e += blockDim.x)
-            conv_smem[(k * rowbytes) / 16 + e] = src[e];
+    const int per_row = rowbytes / 16;
+    // all of the block's row loads in flight at once (asynchronous copies), one wait
+    for (int e = threadIdx.x; e < kMbInt * per_row; e += blockDim.x) {
+        const int k = e / per_row, i = e - k * per_row;
+        const uint4 *src = reinterpret_cast<const uint4 *>(g.v + ((long long)(t * kMbInt + k) * g.nfine + c) * rowbytes) + i;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(&conv_smem[e])), "l"(src) : "memory");
     }
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
     __syncthreads();
     for (int a = threadIdx.x; a < g.A; a += blockDim.x) {
         const uint32_t iq = g.polQ[a], ip = g.polP[a];
+        if (iq >= (uint32_t)g.ni || ip >= (uint32_t)g.ni) {
+            atomicOr(g.status, kErrBadInput);
+            continue;
+        }
         int cqq = 0, cpp = 0, cr = 0, ci = 0;
         for (int k = 0; k < kMbInt; k++) {
             const int s = t * kMbInt + k;
@@ -1149,8 +1158,9 @@ extern "C" int vgb_multibeam_create(const vgb_multibeam_config *cfg, vgb_multibe
         return set_error(VGB_ERR_INVALID, "multibeam: nant must be a positive multiple of 16, at most 2048 (got %d)",
                          c.nant);
     if (c.npointing <= 0) return set_error(VGB_ERR_INVALID, "multibeam: npointing must be positive");
-    if (c.nsamples <= 0 || c.nsamples % kMbInt)
-        return set_error(VGB_ERR_INVALID, "multibeam: nsamples must be a positive multiple of %d", kMbInt);
+    if (c.nsamples <= 0 || c.nsamples % kMbInt || c.nsamples / kMbInt > 65535)
+        return set_error(VGB_ERR_INVALID, "multibeam: nsamples must be a positive multiple of %d, at most %d", kMbInt,
+                         65535 * kMbInt);
     if (c.nstokes != 1 && c.nstokes != 4) return set_error(VGB_ERR_INVALID, "multibeam: nstokes must be 1 or 4");
     if (c.precision != VGB_MB_SPLIT_BF16 && c.precision != VGB_MB_BF16 && c.precision != VGB_MB_FP16 &&
         c.precision != VGB_MB_FP32)
@@ -1346,6 +1356,7 @@ int mb_run_cc(vgb_multibeam *mb, int cc, const uint8_t *v_cc, float *S_cc, uint8
     g.Kb = mb->Kb;
     g.polQ = mb->d_polQ;
     g.polP = mb->d_polP;
+    g.status = status;
     g.V = mb->d_V;
     g.C = mb->d_C;
     const int conv_smem = kMbInt * 2 * A * (mb->int8 ? 2 : 1);
@@ -1353,7 +1364,7 @@ int mb_run_cc(vgb_multibeam *mb, int cc, const uint8_t *v_cc, float *S_cc, uint8
                                               conv_smem),
                          "cudaFuncSetAttribute(mb_convert_kernel)")))
         return rc;
-    mb_convert_kernel<<<dim3(mb->nint, nf), 128, conv_smem, st>>>(g);
+    mb_convert_kernel<<<dim3(nf, mb->nint), 128, conv_smem, st>>>(g);
     if ((rc = check_launch("mb_convert_kernel"))) return rc;
     mark(cc, 2);
 

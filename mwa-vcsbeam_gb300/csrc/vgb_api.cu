@@ -150,9 +150,10 @@ int vgb_check_device_status(void *stream, unsigned *flags_out)
     }
     if (flags_out) *flags_out = h;
     if (h)
-        return set_error(VGB_ERR_DEVICE, "kernel status 0x%x%s%s", h,
+        return set_error(VGB_ERR_DEVICE, "kernel status 0x%x%s%s%s", h,
                          (h & kErrWaitTimeout) ? " (bounded wait expired)" : "",
-                         (h & kErrBadFrame) ? " (frame outside the voltage buffers)" : "");
+                         (h & kErrBadFrame) ? " (frame outside the voltage buffers)" : "",
+                         (h & kErrBadInput) ? " (polQ/polP input index outside the voltage row)" : "");
     return VGB_SUCCESS;
 }
 

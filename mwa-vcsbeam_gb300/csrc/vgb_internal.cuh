@@ -36,6 +36,7 @@ constexpr int kHistFrames = kP;             // frames of the previous second a s
 // Error flag bits a kernel may raise in the device status word.
 constexpr unsigned kErrWaitTimeout = 1u;    // a bounded mbarrier wait gave up
 constexpr unsigned kErrBadFrame = 2u;       // a frame index fell outside the described buffers
+constexpr unsigned kErrBadInput = 4u;       // an input index (polQ / polP) fell outside the voltage row
 
 // ---------------------------------------------------------------------------
 // Where the frames of one coarse channel's second live.

@@ -34,7 +34,7 @@ def vgb_mod(torch):
     return vgb
 
 
-def make_case(O, nant, npointing, nfine, ns, seed=1, int8=False, flag_tile=None, cc=0):
+def make_case(O, nant, npointing, nfine, ns, seed=1, int8=False, flag_tile=None, cc=0, natural=False):
     D = SY.calibration_jones(nant, nfine, seed=seed)
     rng = np.random.default_rng(seed + 50)  # a per-channel ripple so D^-1 differs across channels
     D = D * (1.0 + 0.05 * np.exp(2j * np.pi * rng.uniform(size=(nant, nfine, 1, 1))))
@@ -48,7 +48,8 @@ def make_case(O, nant, npointing, nfine, ns, seed=1, int8=False, flag_tile=None,
     az, za = SY.grid_pointings(side, 0.02)
     unit = np.ascontiguousarray(SY.unit_vectors(az[:npointing], za[:npointing]))
     freqs = SY.fine_chan_freqs_hz(SY.coarse_chan_start_hz(cc))[:nfine].astype(np.float64)
-    polQ, polP = pol_lists(SY.legacy_input_order(nant))
+    # the legacy order is a permutation of the inputs; natural = tile a's pols at inputs 2a, 2a + 1 (MWAX)
+    polQ, polP = pol_lists(np.arange(2 * nant) if natural else SY.legacy_input_order(nant))
     if int8:
         raw = O.gen_int8(seed + 5, ns * nfine * 2 * nant * 2, sigma_num=16).reshape(ns, nfine, 2 * nant, 2)
         v_oracle = raw[..., 0].astype(np.float64) + 1j * raw[..., 1].astype(np.float64)
@@ -134,6 +135,32 @@ def test_multibeam_stokes_i_int8_flagged(vgb_mod, torch, oracle_mod):
     res = run_mb(vgb_mod, torch, case, nant, npnt, nfine, ns, 1, 0, int8=True, invw=invw)
     errs = stokes_err(res["S"], ref)
     assert max(errs) < 1e-3, errs
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-3), (2, 4e-3), (1, 3e-2)])
+def test_multibeam_int8_natural_order(vgb_mod, torch, oracle_mod, precision, tol):
+    """8-bit voltages in every tensor precision (each expands the raw bytes
+    to its own 16-bit type inside the beam GEMM), full Stokes, with the tiles'
+    inputs in the MWAX order (consecutive weight columns)."""
+    nant, npnt, nfine, ns = 32, 40, 3, 520
+    case = make_case(oracle_mod, nant, npnt, nfine, ns, seed=21, int8=True, natural=True)
+    invw = 1.0 / (2 * nant)
+    ref = oracle_stokes(oracle_mod, case, 4, invw)
+    res = run_mb(vgb_mod, torch, case, nant, npnt, nfine, ns, 4, precision, int8=True, invw=invw)
+    errs = stokes_err(res["S"], ref)
+    assert max(errs) < tol, errs
+
+
+def test_multibeam_bad_input_index(vgb_mod, torch, oracle_mod):
+    """An input index outside the voltage row (polQ of a tile = 2 nant + 5) is
+    skipped by the kernels and reported through the device status word."""
+    nant, npnt, nfine, ns = 16, 32, 2, 100
+    case = make_case(oracle_mod, nant, npnt, nfine, ns, seed=23)
+    case["polQ"] = case["polQ"].copy()
+    case["polQ"][3] = 2 * nant + 5
+    with pytest.raises(vgb_mod.VGBError, match="input index"):
+        run_mb(vgb_mod, torch, case, nant, npnt, nfine, ns, 4, 0)
+    assert vgb_mod.check_device_status() == 0
 
 
 def test_multibeam_psrfits_bytes(vgb_mod, torch, oracle_mod):
