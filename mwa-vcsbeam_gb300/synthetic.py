@@ -126,20 +126,28 @@ def legacy_input_order(nant: int, seed: int = 3) -> np.ndarray:
     return rng.permutation(2 * nant).astype(np.int32)
 
 
-def tile_delay_sets(n: int, seed: int = 5, max_za_deg: float = 45.0) -> np.ndarray:
-    """[n][16] analogue beamformer delay settings (0..31 steps of 435 ps) of
-    tiles pointed at random directions within max_za_deg of zenith: each
-    dipole's geometric delay, quantised, offset to start at 0 (dipole i at
-    column i % 4 east, row i // 4 from north, 1.1 m pitch)."""
-    rng = np.random.default_rng(seed)
-    out = np.zeros((n, 16), dtype=np.uint32)
+def tile_delays_toward(az: float, za: float) -> np.ndarray:
+    """[16] analogue beamformer delays (0..31 steps of 435 ps) pointing a tile
+    at (az, za) in radians: each dipole's geometric delay, quantised, offset to
+    start at 0 (dipole i at column i % 4 east, row i // 4 from north, 1.1 m
+    pitch)."""
     i = np.arange(16)
     x = ((i % 4) - 1.5) * 1.1
     y = (1.5 - (i // 4)) * 1.1
+    tau = (x * np.sin(za) * np.sin(az) + y * np.sin(za) * np.cos(az)) / 299792458.0
+    d = np.round(tau / 435e-12)
+    return np.clip(d - d.min(), 0, 31).astype(np.uint32)
+
+
+def tile_delay_sets(n: int, seed: int = 5, max_za_deg: float = 45.0, return_dirs: bool = False):
+    """[n][16] delay settings of tiles pointed at random directions within
+    max_za_deg of zenith (and, with return_dirs, their [n] az, za in radians)."""
+    rng = np.random.default_rng(seed)
+    out = np.zeros((n, 16), dtype=np.uint32)
+    dirs = np.zeros((n, 2))
     for k in range(n):
         az = rng.uniform(0, 2 * np.pi)
         za = np.radians(rng.uniform(0, max_za_deg))
-        tau = (x * np.sin(za) * np.sin(az) + y * np.sin(za) * np.cos(az)) / 299792458.0
-        d = np.round(tau / 435e-12)
-        out[k] = np.clip(d - d.min(), 0, 31).astype(np.uint32)
-    return out
+        out[k] = tile_delays_toward(az, za)
+        dirs[k] = az, za
+    return (out, dirs[:, 0], dirs[:, 1]) if return_dirs else out
