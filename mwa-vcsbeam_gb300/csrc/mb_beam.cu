@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(kMbWeightThreads) mb_weights_kernel(const MbWe
 // across the block's beams, each J^-1 is formed once (and held while the
 // block finds the Q rows' scales), and every row is written with 16-byte
 // stores covering both tiles.
-__global__ void __launch_bounds__(256, 3) mb_weights_pair_kernel(const MbWeightArgs w)
+__global__ void __launch_bounds__(256, 4) mb_weights_pair_kernel(const MbWeightArgs w)
 {
     __shared__ float smax[8][4];
     const int c = blockIdx.y;
