@@ -6,7 +6,8 @@
  * code, and never exits the process. vgb_last_error() describes the last
  * failure on the calling thread. Launches are asynchronous on the given
  * stream; vgb_check_device_status() reports errors kernels raised (a bounded
- * wait that expired, a frame outside the described buffers).
+ * wait that expired, a frame outside the described buffers, an input index
+ * outside the voltage row).
  *
  * The VCSBeam library API (include/vcsbeam.h in this project, mirroring the
  * reference's include/vcsbeam.h.in) is implemented on top of these calls.
@@ -310,7 +311,9 @@ int vgb_load_filter(const char *path, int nchans, double scale, double *coeffs, 
  * tile beamformer delays; the reference's FEE model is not available to this
  * build), P the parallactic-angle rotation at `latitude` (primary_beam.c:
  * 436-456) when pa_correction != 0. az, za [npointing] radians; freq_hz
- * [nfreq]; delays [ntile][16] (0..31, 32 = dead dipole). All device pointers. */
+ * [nfreq]; delays [ntile][16] (0..31, 32 = dead dipole). All device pointers;
+ * delays and B 16-byte aligned. Tiles with identical delays share one
+ * evaluation (vmCalcB's per-configuration cache), copied to each tile. */
 int vgb_primary_beam(const double *az, const double *za, int npointing, const double *freq_hz, int nfreq,
                      const uint32_t *delays, int ntile, double latitude, int pa_correction, void *B, void *stream);
 /* Index of a live/dead dipole pattern (amps[16], 0 = dead) among the 138
@@ -357,7 +360,9 @@ int vgb_surrogate_validate(vgb_surrogate *s, long long nval, float tol, float *m
 /* B [nfreq][npointing][ntile][2][2] complex double, as vgb_primary_beam, from
  * the surrogate (tile_set[t] = trained delay-set index of tile t, < 0 = none)
  * with plain-model fallback; nfallback (host, nullable) receives the number
- * of (frequency, pointing, tile) entries the plain model answered. */
+ * of (frequency, pointing, tile) entries the plain model answered. The
+ * network runs once per (frequency, pointing) for each delay set some tile
+ * uses; tile_set is read back to the host on `stream` (the call waits for it). */
 int vgb_surrogate_beam(vgb_surrogate *s, const double *az, const double *za, int npointing, const double *freq_hz,
                        int nfreq, const int *tile_set, const uint32_t *delays, int ntile, double latitude,
                        int pa_correction, void *B, unsigned *nfallback, void *stream);

@@ -1,5 +1,7 @@
 // Primary-beam matrices B [pointing][tile][2][2] (vmCalcB,
-// primary_beam.c:79-191) on the device, FP64.
+// primary_beam.c:79-191) on the device, FP64, evaluated once per distinct
+// delay set (tiles sharing a dipole configuration share B, as vmCalcB's
+// per-configuration cache) and copied to the other tiles.
 //
 // The reference evaluates the MWA FEE model (mwa_hyperbeam's calc_jones, a
 // Rust crate reading an HDF5 table of spherical-wave coefficients) once per
@@ -29,17 +31,61 @@
 
 namespace vgb {
 
-__global__ void beam_model_kernel(const PbArgs a)
+// Distinct delay sets, as vmCalcB evaluates the beam once per distinct
+// dipole configuration (primary_beam.c:119-160): rep[t] = the first tile with
+// tile t's 16 delays, list[k] = the k-th such first tile, count = their number.
+// One block; O(ntile^2) comparisons of 16 words, early exit on the first match.
+__global__ void beam_configs_kernel(const uint32_t *delays, int ntile, int *rep, int *list, int *count)
+{
+    __shared__ int s_first[1024];
+    __shared__ int s_base;
+    if (threadIdx.x == 0) s_base = 0;
+    __syncthreads();
+    for (int t0 = 0; t0 < ntile; t0 += blockDim.x) {
+        const int t = t0 + threadIdx.x;
+        int r = t;
+        if (t < ntile) {
+            const uint4 *dt = reinterpret_cast<const uint4 *>(delays + 16 * (long long)t);
+            const uint4 a0 = dt[0], a1 = dt[1], a2 = dt[2], a3 = dt[3];
+            for (int u = 0; u < t; u++) {
+                const uint4 *du = reinterpret_cast<const uint4 *>(delays + 16 * (long long)u);
+                const uint4 b0 = du[0], b1 = du[1], b2 = du[2], b3 = du[3];
+                if (a0.x == b0.x && a0.y == b0.y && a0.z == b0.z && a0.w == b0.w && a1.x == b1.x && a1.y == b1.y &&
+                    a1.z == b1.z && a1.w == b1.w && a2.x == b2.x && a2.y == b2.y && a2.z == b2.z && a2.w == b2.w &&
+                    a3.x == b3.x && a3.y == b3.y && a3.z == b3.z && a3.w == b3.w) {
+                    r = u;
+                    break;
+                }
+            }
+            rep[t] = r;
+        }
+        s_first[threadIdx.x] = t < ntile && r == t;
+        __syncthreads();
+        if (threadIdx.x == 0) { // compact this chunk's first tiles in tile order
+            int k = s_base;
+            for (int i = 0; i < (int)blockDim.x && t0 + i < ntile; i++)
+                if (s_first[i]) list[k++] = t0 + i;
+            s_base = k;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *count = s_base;
+}
+
+// B for (frequency, pointing, the k-th distinct delay set), written at that
+// set's first tile. Threads with k >= count leave at once.
+__global__ void beam_model_kernel(const PbArgs a, const int *list, const int *count)
 {
     const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long n = (long long)a.nfreq * a.npointing * a.ntile;
-    if (idx >= n) return;
-    const int t = idx % a.ntile;
-    const int p = (idx / a.ntile) % a.npointing;
-    const int fi = idx / ((long long)a.ntile * a.npointing);
+    const long long per_k = (long long)a.nfreq * a.npointing;
+    const int k = (int)(idx / per_k);
+    if (k >= *count || k >= a.ntile) return;
+    const int p = (int)(idx % a.npointing);
+    const int fi = (int)((idx / a.npointing) % a.nfreq);
+    const int t = list[k];
     double2 J[4];
-    bm_jones(a.az[p], a.za[p], a.freq[fi], a.delays + 16 * t, J);
-    double2 *o = a.B + 4 * idx;
+    bm_jones(a.az[p], a.za[p], a.freq[fi], a.delays + 16 * (long long)t, J);
+    double2 *o = a.B + 4 * (((long long)fi * a.npointing + p) * a.ntile + t);
     if (!a.pa) {
         for (int e = 0; e < 4; e++) o[e] = J[e];
         return;
@@ -53,12 +99,44 @@ __global__ void beam_model_kernel(const PbArgs a)
     o[3] = make_double2(J[2].x * P[1] + J[3].x * P[3], J[2].y * P[1] + J[3].y * P[3]);
 }
 
+// Every other tile copies its set's matrix (32 bytes per thread, two uint4).
+__global__ void beam_expand_kernel(const PbArgs a, const int *rep)
+{
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long n = (long long)a.nfreq * a.npointing * a.ntile;
+    if (idx >= n) return;
+    const int t = (int)(idx % a.ntile);
+    const int r = rep[t];
+    if (r == t) return;
+    const uint4 *src = reinterpret_cast<const uint4 *>(a.B + 4 * (idx - t + r));
+    uint4 *dst = reinterpret_cast<uint4 *>(a.B + 4 * idx);
+    dst[0] = src[0];
+    dst[1] = src[1];
+    dst[2] = src[2];
+    dst[3] = src[3];
+}
+
 int launch_beam_model(const PbArgs &a, cudaStream_t st)
 {
     const long long n = (long long)a.nfreq * a.npointing * a.ntile;
     if (n <= 0) return VGB_SUCCESS;
-    beam_model_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(a);
-    return check_launch("beam_model_kernel");
+    int *scratch = nullptr; // rep [ntile], list [ntile], count
+    int rc = check_cuda(cudaMallocAsync(reinterpret_cast<void **>(&scratch), (2 * (size_t)a.ntile + 1) * sizeof(int), st),
+                        "cudaMallocAsync(beam configurations)");
+    if (rc) return rc;
+    int *rep = scratch, *list = scratch + a.ntile, *count = scratch + 2 * a.ntile;
+    beam_configs_kernel<<<1, 1024, 0, st>>>(a.delays, a.ntile, rep, list, count);
+    rc = check_launch("beam_configs_kernel");
+    if (!rc) {
+        beam_model_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(a, list, count);
+        rc = check_launch("beam_model_kernel");
+    }
+    if (!rc) {
+        beam_expand_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a, rep);
+        rc = check_launch("beam_expand_kernel");
+    }
+    const int rf = check_cuda(cudaFreeAsync(scratch, st), "cudaFreeAsync(beam configurations)");
+    return rc ? rc : rf;
 }
 
 } // namespace vgb
@@ -92,6 +170,8 @@ extern "C" int vgb_primary_beam(const double *az, const double *za, int npointin
 {
     if (!az || !za || !freq_hz || !delays || !B) return set_error(VGB_ERR_INVALID, "primary_beam: NULL argument");
     if (npointing <= 0 || nfreq <= 0 || ntile <= 0) return set_error(VGB_ERR_INVALID, "primary_beam: empty shape");
+    if ((reinterpret_cast<uintptr_t>(delays) | reinterpret_cast<uintptr_t>(B)) & 15)
+        return set_error(VGB_ERR_INVALID, "primary_beam: delays and B must be 16-byte aligned");
     PbArgs a{az, za, npointing, freq_hz, nfreq, delays, ntile, latitude, pa_correction, static_cast<double2 *>(B)};
     return launch_beam_model(a, static_cast<cudaStream_t>(stream));
 }

@@ -330,6 +330,7 @@ struct SurQueryArgs {
     uint64_t seed;
     float *y;               // [B][8]
     int *cell_of;           // [B] set * cells + cell
+    const int *set_list;    // queries: the delay sets evaluated (nsets of them), in row order
 };
 
 __global__ void sur_query_kernel(const SurQueryArgs a)
@@ -356,7 +357,7 @@ __global__ void sur_query_kernel(const SurQueryArgs a)
             }
             a.cell_of[i] = s * kSurNaz * kSurNza + sur_cell(az, za);
         } else {
-            s = (int)(q % a.nsets);
+            s = a.set_list[q % a.nsets];
             const int p = (int)((q / a.nsets) % a.npointing);
             const int fi = (int)(q / ((long long)a.nsets * a.npointing));
             az = a.az[p];
@@ -387,7 +388,9 @@ struct SurExpandArgs {
     int npointing, nfreq, nsets, ntile;
     const int *tile_set;      // [ntile] delay-set index, < 0: not covered
     const uint32_t *delays;   // [ntile][16]
-    const float *Jsur;        // [nfreq][npointing][nsets][8]
+    const float *Jsur;        // [nfreq][npointing][nslots][8]
+    const int *slot_of;       // [nsets] row slot of each evaluated set, -1 if not evaluated
+    int nslots;
     const unsigned *cell_err; // [nsets][cells]
     float tol;
     double lat;
@@ -404,10 +407,11 @@ __global__ void sur_expand_kernel(const SurExpandArgs a)
     const double az = a.az[p], za = a.za[p];
     const int s = a.tile_set[t];
     double2 J[4];
-    bool use = s >= 0 && s < a.nsets && za <= kSurZaMax &&
+    const int slot = s >= 0 && s < a.nsets ? a.slot_of[s] : -1;
+    bool use = slot >= 0 && za <= kSurZaMax &&
                __uint_as_float(a.cell_err[s * kSurNaz * kSurNza + sur_cell(az, za)]) <= a.tol;
     if (use) {
-        const float *o = a.Jsur + 8 * (((long long)fi * a.npointing + p) * a.nsets + s);
+        const float *o = a.Jsur + 8 * (((long long)fi * a.npointing + p) * a.nslots + slot);
         for (int e = 0; e < 4; e++) J[e] = make_double2(o[2 * e], o[2 * e + 1]);
     } else {
         bm_jones(az, za, a.freq[fi], a.delays + 16 * t, J);
@@ -451,6 +455,7 @@ struct vgb_surrogate {
     long long step = 0;
     float *Jsur = nullptr;
     long long Jsur_cap = 0;
+    int *set_map = nullptr; // queries: [nsets] evaluated sets in row order, then [nsets] slot of each set
 };
 
 namespace {
@@ -608,6 +613,7 @@ extern "C" int vgb_surrogate_create(int nsets, int batch, unsigned long long see
     s->set_of = sur_alloc<int>(s, B, rc);
     s->cell_of = sur_alloc<int>(s, B, rc);
     s->cell_err = sur_alloc<unsigned>(s, (size_t)nsets * kSurNaz * kSurNza, rc);
+    s->set_map = sur_alloc<int>(s, 2 * (size_t)nsets, rc);
     s->max_err = sur_alloc<unsigned>(s, 1, rc);
     s->nfallback = sur_alloc<unsigned>(s, 1, rc);
     if (!rc) rc = check_cuda(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -879,8 +885,23 @@ extern "C" int vgb_surrogate_beam(vgb_surrogate *s, const double *az, const doub
     if (npointing <= 0 || nfreq <= 0 || ntile <= 0) return set_error(VGB_ERR_INVALID, "surrogate_beam: empty shape");
     if (!s->validated) return set_error(VGB_ERR_STATE, "surrogate_beam: validate the network first");
     cudaStream_t caller = static_cast<cudaStream_t>(stream);
-    const long long rows = (long long)nfreq * npointing * s->nsets;
-    int rc = VGB_SUCCESS;
+    // the network runs only for the delay sets some tile uses (as vmCalcB
+    // evaluates once per distinct configuration)
+    std::vector<int> ts(ntile), list, slot(s->nsets, -1);
+    int rc = check_cuda(cudaMemcpyAsync(ts.data(), tile_set, sizeof(int) * ntile, cudaMemcpyDeviceToHost, caller),
+                        "cudaMemcpyAsync(tile_set)");
+    if (!rc) rc = check_cuda(cudaStreamSynchronize(caller), "cudaStreamSynchronize");
+    if (rc) return rc;
+    for (int t = 0; t < ntile; t++)
+        if (ts[t] >= 0 && ts[t] < s->nsets && slot[ts[t]] < 0) {
+            slot[ts[t]] = (int)list.size();
+            list.push_back(ts[t]);
+        }
+    const int nslots = (int)list.size();
+    const long long rows = (long long)nfreq * npointing * nslots;
+    std::vector<int> map(2 * s->nsets, 0);
+    for (int k = 0; k < nslots; k++) map[k] = list[k];
+    for (int k = 0; k < s->nsets; k++) map[s->nsets + k] = slot[k];
     if (rows > s->Jsur_cap) {
         if (s->Jsur) cudaFree(s->Jsur);
         s->Jsur = nullptr;
@@ -894,6 +915,9 @@ extern "C" int vgb_surrogate_beam(vgb_surrogate *s, const double *az, const doub
     rc = check_cuda(cudaEventRecord(ev, caller), "cudaEventRecord");
     if (!rc) rc = check_cuda(cudaStreamWaitEvent(s->st, ev, 0), "cudaStreamWaitEvent");
     if (!rc) rc = check_cuda(cudaMemsetAsync(s->nfallback, 0, sizeof(unsigned), s->st), "cudaMemsetAsync");
+    if (!rc)
+        rc = check_cuda(cudaMemcpyAsync(s->set_map, map.data(), sizeof(int) * map.size(), cudaMemcpyHostToDevice, s->st),
+                        "cudaMemcpyAsync(set map)");
     for (long long r0 = 0; r0 < rows && !rc; r0 += s->B) {
         SurQueryArgs q{};
         q.az = az;
@@ -901,7 +925,8 @@ extern "C" int vgb_surrogate_beam(vgb_surrogate *s, const double *az, const doub
         q.freq = freq_hz;
         q.npointing = npointing;
         q.nfreq = nfreq;
-        q.nsets = s->nsets;
+        q.nsets = nslots;
+        q.set_list = s->set_map;
         q.params = s->p;
         q.L = s->L;
         q.row0 = r0;
@@ -920,8 +945,9 @@ extern "C" int vgb_surrogate_beam(vgb_surrogate *s, const double *az, const doub
                         "cudaMemcpyAsync");
     }
     if (!rc) {
-        SurExpandArgs e{az, za, freq_hz, npointing, nfreq, s->nsets, ntile, tile_set, delays, s->Jsur, s->cell_err,
-                        s->tol, latitude, pa_correction, static_cast<double2 *>(B), s->nfallback};
+        SurExpandArgs e{az,      za,      freq_hz,    npointing,        nfreq,   s->nsets,      ntile,
+                        tile_set, delays, s->Jsur,    s->set_map + s->nsets, nslots, s->cell_err, s->tol,
+                        latitude, pa_correction, static_cast<double2 *>(B), s->nfallback};
         const long long n = (long long)nfreq * npointing * ntile;
         sur_expand_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s->st>>>(e);
         rc = check_launch("sur_expand_kernel");

@@ -90,3 +90,29 @@ def test_primary_beam_matches_oracle(vgb_mod):
         want = BM.primary_beam(az, za, freqs, delays, pa=pa)
         assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
         assert np.all(got[:, :, 4] == 0)
+
+
+@pytest.mark.gpu
+def test_primary_beam_shared_configurations(vgb_mod):
+    """Tiles sharing a delay set share B (evaluated once per distinct set and
+    copied): 1,100 tiles drawn from 5 sets (one with a dead dipole), spread
+    over more than one 1,024-tile chunk of the configuration scan."""
+    torch = torch_cuda()
+    rng = np.random.default_rng(9)
+    npnt, ntile = 12, 1100
+    az = rng.uniform(0, 2 * np.pi, npnt)
+    za = rng.uniform(0, np.radians(70), npnt)
+    freqs = np.array([120e6, 210e6])
+    sets = rng.integers(0, 32, (5, 16)).astype(np.uint32)
+    sets[3, 7] = 32
+    pick = rng.integers(0, 5, ntile)
+    pick[1050:] = 4                   # a set first seen in the second chunk
+    pick[:1050][pick[:1050] == 4] = 0
+    delays = np.ascontiguousarray(sets[pick])
+    B = torch.zeros(freqs.size * npnt * ntile * 8, dtype=torch.float64, device="cuda")
+    vgb_mod.primary_beam(dev(az), dev(za), dev(freqs), dev(delays), B)
+    torch.cuda.synchronize()
+    got = host(B).view(np.complex128).reshape(freqs.size, npnt, ntile, 2, 2)
+    want_sets = BM.primary_beam(az, za, freqs, sets)
+    want = want_sets[:, :, pick]
+    assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
