@@ -277,6 +277,14 @@ __device__ __forceinline__ void load_taps(const int *filter, int n0, int (&hc)[2
         for (int p = 0; p < kP; p++) hc[q][p] = __ldg(filter + kK * kP - kK * p - (n0 + q) - 1);
 }
 
+// The rows of input li are written by the WOLA and transformed by the FFT in
+// the same 64 threads (two warps: tid / 64 == li in both mappings), so only
+// those two warps meet between the two stages (named barrier 1 + li).
+__device__ __forceinline__ void input_barrier(int li)
+{
+    asm volatile("bar.sync %0, 64;" ::"r"(1 + li) : "memory");
+}
+
 // Wait for step `it`'s data; every thread learns whether any thread timed
 // out, so the CTA leaves together. The barrier also orders the previous
 // step's reads of the buffers before this step's writes.
@@ -332,7 +340,7 @@ __global__ void __launch_bounds__(kThreads, 2) beam_kernel(const BeamArgs a)
         // everyone has finished step it-1, so its buffers may be refilled
         if (tid < 32 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, Wcc, a.nant, a.status);
         wola_step<kInt32, kFpga>(sm, it & 1, li, n0, hc);
-        __syncthreads();
+        input_barrier(li);
         fft_step<kDemote>(sm, tid);
         __syncthreads();
 #pragma unroll
@@ -417,7 +425,7 @@ __global__ void __launch_bounds__(kThreads, 2) pack_kernel(const PackArgs a)
         }
         if (tid < 32 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, nullptr, 0, a.status);
         wola_step<kInt32, kFpga>(sm, it & 1, li, n0, hc);
-        __syncthreads();
+        input_barrier(li);
         fft_step<kDemote>(sm, tid);
         __syncthreads();
 #pragma unroll
