@@ -389,6 +389,7 @@ struct SurExpandArgs {
     const int *tile_set;      // [ntile] delay-set index, < 0: not covered
     const uint32_t *delays;   // [ntile][16]
     const float *Jsur;        // [nfreq][npointing][nslots][8]
+    double2 *Bsur;            // [nfreq][npointing][nslots][4]: Jsur (x P)
     const int *slot_of;       // [nsets] row slot of each evaluated set, -1 if not evaluated
     int nslots;
     const unsigned *cell_err; // [nsets][cells]
@@ -399,6 +400,33 @@ struct SurExpandArgs {
     unsigned *nfallback;
 };
 
+// The network's Jones matrices per (frequency, pointing, evaluated set) in
+// FP64, times the parallactic rotation when asked: B rows shared by every
+// tile of the set (one rotation per pointing and set, not per tile).
+__global__ void sur_rotate_kernel(const SurExpandArgs a, long long rows)
+{
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const int p = (int)((r / a.nslots) % a.npointing);
+    const float *o = a.Jsur + 8 * r;
+    double2 J[4];
+    for (int e = 0; e < 4; e++) J[e] = make_double2(o[2 * e], o[2 * e + 1]);
+    double2 *out = a.Bsur + 4 * r;
+    if (!a.pa) {
+        for (int e = 0; e < 4; e++) out[e] = J[e];
+        return;
+    }
+    double P[4];
+    bm_pa(a.lat, a.az[p], a.za[p], P);
+    out[0] = make_double2(J[0].x * P[0] + J[1].x * P[2], J[0].y * P[0] + J[1].y * P[2]);
+    out[1] = make_double2(J[0].x * P[1] + J[1].x * P[3], J[0].y * P[1] + J[1].y * P[3]);
+    out[2] = make_double2(J[2].x * P[0] + J[3].x * P[2], J[2].y * P[0] + J[3].y * P[2]);
+    out[3] = make_double2(J[2].x * P[1] + J[3].x * P[3], J[2].y * P[1] + J[3].y * P[3]);
+}
+
+// Per (frequency, pointing, tile): the network's B where its sky cell is
+// within tolerance and the tile's set was trained; else the plain model's B,
+// already in place (counted as fallback).
 __global__ void sur_expand_kernel(const SurExpandArgs a)
 {
     const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -406,28 +434,19 @@ __global__ void sur_expand_kernel(const SurExpandArgs a)
     const int t = idx % a.ntile, p = (idx / a.ntile) % a.npointing, fi = idx / ((long long)a.ntile * a.npointing);
     const double az = a.az[p], za = a.za[p];
     const int s = a.tile_set[t];
-    double2 J[4];
     const int slot = s >= 0 && s < a.nsets ? a.slot_of[s] : -1;
-    bool use = slot >= 0 && za <= kSurZaMax &&
-               __uint_as_float(a.cell_err[s * kSurNaz * kSurNza + sur_cell(az, za)]) <= a.tol;
-    if (use) {
-        const float *o = a.Jsur + 8 * (((long long)fi * a.npointing + p) * a.nslots + slot);
-        for (int e = 0; e < 4; e++) J[e] = make_double2(o[2 * e], o[2 * e + 1]);
-    } else {
-        bm_jones(az, za, a.freq[fi], a.delays + 16 * t, J);
+    const bool use = slot >= 0 && za <= kSurZaMax &&
+                     __uint_as_float(a.cell_err[s * kSurNaz * kSurNza + sur_cell(az, za)]) <= a.tol;
+    if (!use) {
         atomicAdd(a.nfallback, 1u);
-    }
-    double2 *out = a.B + 4 * idx;
-    if (!a.pa) {
-        for (int e = 0; e < 4; e++) out[e] = J[e];
         return;
     }
-    double P[4];
-    bm_pa(a.lat, az, za, P);
-    out[0] = make_double2(J[0].x * P[0] + J[1].x * P[2], J[0].y * P[0] + J[1].y * P[2]);
-    out[1] = make_double2(J[0].x * P[1] + J[1].x * P[3], J[0].y * P[1] + J[1].y * P[3]);
-    out[2] = make_double2(J[2].x * P[0] + J[3].x * P[2], J[2].y * P[0] + J[3].y * P[2]);
-    out[3] = make_double2(J[2].x * P[1] + J[3].x * P[3], J[2].y * P[1] + J[3].y * P[3]);
+    const uint4 *src = reinterpret_cast<const uint4 *>(a.Bsur + 4 * (((long long)fi * a.npointing + p) * a.nslots + slot));
+    uint4 *dst = reinterpret_cast<uint4 *>(a.B + 4 * idx);
+    dst[0] = src[0];
+    dst[1] = src[1];
+    dst[2] = src[2];
+    dst[3] = src[3];
 }
 
 } // namespace vgb
@@ -454,6 +473,7 @@ struct vgb_surrogate {
     bool validated = false;
     long long step = 0;
     float *Jsur = nullptr;
+    double2 *Bsur = nullptr;
     long long Jsur_cap = 0;
     int *set_map = nullptr; // queries: [nsets] evaluated sets in row order, then [nsets] slot of each set
 };
@@ -658,7 +678,7 @@ extern "C" void vgb_surrogate_destroy(vgb_surrogate *s)
     if (s->st) cudaStreamSynchronize(s->st);
     for (void *p : s->allocs) cudaFree(p);
     for (void *p : {(void *)s->tab_az, (void *)s->tab_za, (void *)s->tab_f, (void *)s->tab_Y, (void *)s->tab_delays,
-                    (void *)s->Jsur})
+                    (void *)s->Jsur, (void *)s->Bsur})
         if (p) cudaFree(p);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
@@ -884,6 +904,8 @@ extern "C" int vgb_surrogate_beam(vgb_surrogate *s, const double *az, const doub
         return set_error(VGB_ERR_INVALID, "surrogate_beam: NULL argument");
     if (npointing <= 0 || nfreq <= 0 || ntile <= 0) return set_error(VGB_ERR_INVALID, "surrogate_beam: empty shape");
     if (!s->validated) return set_error(VGB_ERR_STATE, "surrogate_beam: validate the network first");
+    if ((reinterpret_cast<uintptr_t>(delays) | reinterpret_cast<uintptr_t>(B)) & 15)
+        return set_error(VGB_ERR_INVALID, "surrogate_beam: delays and B must be 16-byte aligned");
     cudaStream_t caller = static_cast<cudaStream_t>(stream);
     // the network runs only for the delay sets some tile uses (as vmCalcB
     // evaluates once per distinct configuration)
@@ -904,7 +926,12 @@ extern "C" int vgb_surrogate_beam(vgb_surrogate *s, const double *az, const doub
     for (int k = 0; k < s->nsets; k++) map[s->nsets + k] = slot[k];
     if (rows > s->Jsur_cap) {
         if (s->Jsur) cudaFree(s->Jsur);
+        if (s->Bsur) cudaFree(s->Bsur);
         s->Jsur = nullptr;
+        s->Bsur = nullptr;
+        s->Jsur_cap = 0;
+        if ((rc = check_cuda(cudaMalloc(&s->Bsur, rows * 4 * sizeof(double2)), "cudaMalloc(surrogate B rows)")))
+            return rc;
         if ((rc = check_cuda(cudaMalloc(&s->Jsur, rows * 8 * sizeof(float)), "cudaMalloc(surrogate outputs)")))
             return rc;
         s->Jsur_cap = rows;
@@ -944,13 +971,25 @@ extern "C" int vgb_surrogate_beam(vgb_surrogate *s, const double *az, const doub
                                         s->st),
                         "cudaMemcpyAsync");
     }
+    // fallback answers: the plain model for every entry (once per distinct
+    // delay set, copied to tiles), then the network's answers overwrite it
     if (!rc) {
-        SurExpandArgs e{az,      za,      freq_hz,    npointing,        nfreq,   s->nsets,      ntile,
-                        tile_set, delays, s->Jsur,    s->set_map + s->nsets, nslots, s->cell_err, s->tol,
-                        latitude, pa_correction, static_cast<double2 *>(B), s->nfallback};
+        PbArgs pb{az, za, npointing, freq_hz, nfreq, delays, ntile, latitude, pa_correction, static_cast<double2 *>(B)};
+        rc = launch_beam_model(pb, s->st);
+    }
+    if (!rc) {
+        SurExpandArgs e{az,      za,      freq_hz,    npointing,        nfreq,   s->nsets,   ntile,
+                        tile_set, delays, s->Jsur,    s->Bsur,   s->set_map + s->nsets, nslots,
+                        s->cell_err, s->tol, latitude, pa_correction, static_cast<double2 *>(B), s->nfallback};
+        if (rows > 0) {
+            sur_rotate_kernel<<<(unsigned)((rows + 127) / 128), 128, 0, s->st>>>(e, rows);
+            rc = check_launch("sur_rotate_kernel");
+        }
         const long long n = (long long)nfreq * npointing * ntile;
-        sur_expand_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s->st>>>(e);
-        rc = check_launch("sur_expand_kernel");
+        if (!rc) {
+            sur_expand_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s->st>>>(e);
+            rc = check_launch("sur_expand_kernel");
+        }
     }
     if (!rc && nfallback)
         rc = check_cuda(cudaMemcpyAsync(nfallback, s->nfallback, sizeof(unsigned), cudaMemcpyDeviceToHost, s->st),
