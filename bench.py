@@ -44,6 +44,7 @@ NCC, NANT, NBLK, K, P = 24, 128, 20, 128, 12
 NI = 2 * NANT
 NSPEC = NBLK * 500
 SECOND_BYTES = NBLK * NI * 64000 * 2           # one coarse channel, one second
+BEAM_KERNEL_DRAM_BYTES_PER_CC = (1.322855e9 + 87.599872e6) / 2
 
 
 def out_bytes(ncc):
@@ -315,11 +316,18 @@ def gb300_arm(args, rank, local_rank, world):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     alg_bytes = ncc * SECOND_BYTES          # the voltages it must read, per launch
+    # DRAM bytes (read + write) of one launch: the ncu capture of a 2-channel
+    # launch (profiles/beam_kernel_2cc.md: 1.3229 GB read + 87.6 MB written)
+    # scaled by the channels processed, since each channel's voltages are read
+    # once and its products written once
+    traffic = args.traffic if args.traffic is not None else ncc * BEAM_KERNEL_DRAM_BYTES_PER_CC
     achieved = alg_bytes / (stage[0] / 1e3) / 1e9
     roofline = {"kernel": "beam_kernel (fused PFB + tied-array/incoherent beam + Stokes)", "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
-                "traffic": args.traffic, "alg_bytes_per_launch": alg_bytes,
+                "traffic": traffic, "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a "
+                "2-channel launch, scaled to the channels of this launch" if args.traffic is None else "--traffic",
+                "alg_bytes_per_launch": alg_bytes,
                 "stage_ms": {"pfb_beam": stage[0], "renormalise": stage[1], "ipfb_vdif": stage[2],
                              "history": stage[3]}}
 
