@@ -249,6 +249,12 @@ int vgb_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, v
  */
 int vgb_gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, int batch, int fp16,
                      void *stream);
+/* Split-operand form: C[b] = (A0[b] + A1[b]) B[b]^T where each row of A holds
+ * A0 then A1 (K elements each, 2K in all; A[b] at A + b*M*2K) and B[b] at
+ * B + b*N*K: the hi + lo product of a split operand with B read once per K
+ * step (persistent kernel). M a multiple of 128, N of 256, K of 64. */
+int vgb_gemm_batched_planes(const void *A, const void *B, float *C, int M, int N, int K, int batch, int fp16,
+                            void *stream);
 /* Force the GEMM kernel variant for shapes whose N is a multiple of 256 (128
  * or 256: the plain kernel's tile width; 512: the persistent kernel), or 0 for
  * the autotuned choice. Returns the previous setting (-1 on a bad value). */

@@ -991,7 +991,7 @@ constexpr int kRnT = 128; // integrations per transpose chunk
 // from the beam epilogue (MbStats); one pass then quantises 128 integrations
 // at a time, packs four channels' bytes into a word, transposes in shared
 // memory and writes 16-byte runs of channels.
-__global__ void __launch_bounds__(256) mb_renorm_kernel(const MbRenormArgs a)
+__global__ void __launch_bounds__(256, 4) mb_renorm_kernel(const MbRenormArgs a)
 {
     __shared__ float s_off[32], s_scl[32];
     __shared__ uint32_t tile[kRnT][9];
@@ -1406,7 +1406,12 @@ int mb_run_cc(vgb_multibeam *mb, int cc, const uint8_t *v_cc, float *S_cc, uint8
         if ((rc = check_launch("mb_simt_beam_kernel"))) return rc;
     } else {
     // autocorrelation terms R = Q C^T per channel (FP16 tensor path)
-    if ((rc = gemm_batched(mb->d_Aq, mb->d_C, mb->d_R, mb->Mq, mb->nint_p, mb->Kq, nf, true, st, mb->Kb))) return rc;
+    // 4-bit split: R = Q_hi C + Q_lo C with C read once per K step (two A planes)
+    if (!mb->int8 && mb->planes == 2 && mb->nint_p % 256 == 0)
+        rc = gemm_batched_planes(mb->d_Aq, mb->d_C, mb->d_R, mb->Mq, mb->nint_p, mb->Kb, nf, true, st);
+    else
+        rc = gemm_batched(mb->d_Aq, mb->d_C, mb->d_R, mb->Mq, mb->nint_p, mb->Kq, nf, true, st, mb->Kb);
+    if (rc) return rc;
     mark(cc, 3);
 
     MbBeamArgs b{};

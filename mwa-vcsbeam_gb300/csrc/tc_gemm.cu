@@ -170,22 +170,27 @@ __global__ void __launch_bounds__(128, 1)
 // next tile's MMAs. Same operands, K order and results as gemm_bf16_kernel.
 // ---------------------------------------------------------------------------
 constexpr int kPStages = 4;
-struct PersistSmem {
-    uint8_t a[kPStages][kTileBytes];
-    uint8_t b[kPStages][256 * 128];
-    uint64_t full[kPStages], empty[kPStages];
+// kA A planes per K step (2: the A rows hold two K-wide halves, e.g. the hi
+// and lo parts of a split operand, both multiplied by the same B tile); the
+// ring keeps 192 KB either way.
+template <int kA> struct PersistSmem {
+    static constexpr int kStages = kA == 2 ? 3 : kPStages;
+    uint8_t a[kStages][kA][kTileBytes];
+    uint8_t b[kStages][256 * 128];
+    uint64_t full[kStages], empty[kStages];
     uint64_t tfull[2], tempty[2], drain;
     uint32_t tmem;
 };
 
-template <bool kF16>
+template <bool kF16, int kA>
 __global__ void __launch_bounds__(192, 1)
     gemm_persist_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, float *C,
                         int M, int N, int K, int Kb, int batch, unsigned *status)
 {
+    constexpr int kPStages = PersistSmem<kA>::kStages;
     extern __shared__ uint8_t pg_raw[];
-    PersistSmem &sm =
-        *reinterpret_cast<PersistSmem *>((reinterpret_cast<uintptr_t>(pg_raw) + 1023) & ~uintptr_t(1023));
+    PersistSmem<kA> &sm =
+        *reinterpret_cast<PersistSmem<kA> *>((reinterpret_cast<uintptr_t>(pg_raw) + 1023) & ~uintptr_t(1023));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int mt = M / 128, ntile = N / 256, nk = K / 64;
     const long long total = (long long)batch * ntile * mt;
@@ -228,8 +233,9 @@ __global__ void __launch_bounds__(192, 1)
                         ok = false;
                         break;
                     }
-                    mbar_arrive_expect_tx(&sm.full[s], kTileBytes + 256 * 128);
-                    tma_load_2d(sm.a[s], &ta, kc * 64, b * M + m * 128, &sm.full[s]);
+                    mbar_arrive_expect_tx(&sm.full[s], kA * kTileBytes + 256 * 128);
+                    tma_load_2d(sm.a[s][0], &ta, kc * 64, b * M + m * 128, &sm.full[s]);
+                    if (kA == 2) tma_load_2d(sm.a[s][1], &ta, K + kc * 64, b * M + m * 128, &sm.full[s]);
                     tma_load_2d(sm.b[s], &tb, (kc * 64) % Kb, b * N + n * 256, &sm.full[s]);
                 }
             }
@@ -258,10 +264,13 @@ __global__ void __launch_bounds__(192, 1)
                         break;
                     }
                     tc_fence_after();
-                    const uint64_t ad = sdesc_sw128(smem_u32(sm.a[s])), bd = sdesc_sw128(smem_u32(sm.b[s]));
+                    const uint64_t ad = sdesc_sw128(smem_u32(sm.a[s][0])), bd = sdesc_sw128(smem_u32(sm.b[s]));
+                    const uint64_t ad1 = sdesc_sw128(smem_u32(sm.a[s][kA - 1]));
 #pragma unroll
-                    for (int k = 0; k < 4; k++)
+                    for (int k = 0; k < 4; k++) {
                         tc_mma(d, sdesc_advance_k(ad, k), sdesc_advance_k(bd, k), idesc, (kc | k) != 0);
+                        if (kA == 2) tc_mma(d, sdesc_advance_k(ad1, k), sdesc_advance_k(bd, k), idesc, 1);
+                    }
                     tc_commit(&sm.empty[s]);
                 }
                 if (ok) tc_commit(&sm.tfull[buf]);
@@ -393,8 +402,8 @@ int gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, in
             }
             const long long tiles = (long long)batch * (N / 256) * (M / 128);
             const int grid = (int)(tiles < nsm ? tiles : nsm);
-            const int smem = (int)sizeof(PersistSmem) + 1024;
-            auto kern = fp16 ? gemm_persist_kernel<true> : gemm_persist_kernel<false>;
+            const int smem = (int)sizeof(PersistSmem<1>) + 1024;
+            auto kern = fp16 ? gemm_persist_kernel<true, 1> : gemm_persist_kernel<false, 1>;
             int e = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
                                "cudaFuncSetAttribute(gemm_persist)");
             if (!e) kern<<<grid, 192, smem, st>>>(ta, tb, C, M, N, K, Kb, batch, status);
@@ -414,6 +423,37 @@ int gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, in
                          : go(gemm_bf16_kernel<false, 128>, (int)sizeof(GemmSmem<128>) + 1024);
     };
     return launch(gemm_tile_width(M, N, K, Kb, batch, fp16, st, launch));
+}
+
+int gemm_batched_planes(const void *A, const void *B, float *C, int M, int N, int K, int batch, bool fp16,
+                        cudaStream_t st)
+{
+    if (!A || !B || !C) return set_error(VGB_ERR_INVALID, "gemm: NULL operand");
+    if (M <= 0 || N <= 0 || K <= 0 || batch <= 0 || M % 128 || N % 256 || K % 64)
+        return set_error(VGB_ERR_INVALID, "gemm (two A planes): M must be a multiple of 128, N of 256, K of 64 "
+                                          "(got %d, %d, %d)", M, N, K);
+    if ((reinterpret_cast<uintptr_t>(C) & 15)) return set_error(VGB_ERR_INVALID, "gemm: C must be 16-byte aligned");
+    unsigned *status = status_word();
+    if (!status) return set_error(VGB_ERR_CUDA, "device status word unavailable");
+    CUtensorMap ta, tb;
+    int r = make_tmap_bf16(&ta, A, (uint64_t)M * batch, 2 * K, (uint64_t)K * 4, 128, fp16);
+    if (!r) r = make_tmap_bf16(&tb, B, (uint64_t)N * batch, K, (uint64_t)K * 2, 256, fp16);
+    if (r) return r;
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (nsm <= 0) nsm = 1;
+    }
+    const long long tiles = (long long)batch * (N / 256) * (M / 128);
+    const int grid = (int)(tiles < nsm ? tiles : nsm);
+    const int smem = (int)sizeof(PersistSmem<2>) + 1024;
+    auto kern = fp16 ? gemm_persist_kernel<true, 2> : gemm_persist_kernel<false, 2>;
+    int e = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                       "cudaFuncSetAttribute(gemm_persist, two planes)");
+    if (!e) kern<<<grid, 192, smem, st>>>(ta, tb, C, M, N, K, K, batch, status);
+    return e ? e : check_launch("gemm_persist_kernel (two A planes)");
 }
 
 } // namespace vgb
@@ -436,4 +476,10 @@ extern "C" int vgb_gemm_batched(const void *A, const void *B, float *C, int M, i
                                 void *stream)
 {
     return gemm_batched(A, B, C, M, N, K, batch, fp16 != 0, static_cast<cudaStream_t>(stream), K);
+}
+
+extern "C" int vgb_gemm_batched_planes(const void *A, const void *B, float *C, int M, int N, int K, int batch,
+                                       int fp16, void *stream)
+{
+    return gemm_batched_planes(A, B, C, M, N, K, batch, fp16 != 0, static_cast<cudaStream_t>(stream));
 }

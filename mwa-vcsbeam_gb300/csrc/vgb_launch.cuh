@@ -108,6 +108,12 @@ int launch_array_factor(const double *look, const double *dirs, int npix, double
                         double *af, cudaStream_t st);
 int gemm_batched(const void *A, const void *B, float *C, int M, int N, int K, int batch, bool fp16,
                  cudaStream_t st, int Kb);
+// C[b] = (A0[b] + A1[b]) B[b]^T where each A row holds A0 then A1 (K wide
+// each, 2K in all) and B rows are K wide: the split-operand product of the
+// K-concatenated form with B read once per K step (persistent kernel; M a
+// multiple of 128, N of 256).
+int gemm_batched_planes(const void *A, const void *B, float *C, int M, int N, int K, int batch, bool fp16,
+                        cudaStream_t st);
 int launch_pack_staged(const float2 *ffted, int nspectra, int ninputs, const int *i_idx, unsigned flags,
                        void *out, cudaStream_t st);
 

@@ -138,6 +138,7 @@ _SIGS = {
     "vgb_multibeam_enable_timing": (I, [V, I]),
     "vgb_multibeam_stage_ms": (I, [V, V, I]),
     "vgb_gemm_batched": (I, [V, V, V, I, I, I, I, I, V]),
+    "vgb_gemm_batched_planes": (I, [V, V, V, I, I, I, I, I, V]),
     "vgb_gemm_variant": (I, [I]),
     "vgb_pipeline_create": (I, [ctypes.POINTER(PipelineConfig), ctypes.POINTER(V)]),
     "vgb_pipeline_destroy": (I, [V]),
@@ -255,6 +256,12 @@ def gemm_variant(v: int) -> int:
 def gemm_batched(A, B, C, M, N, K, batch, fp16=False, stream=None):
     """C[b] = A[b] @ B[b]^T for b < batch (bf16, or fp16 operands; FP32 out)."""
     check(lib().vgb_gemm_batched(ptr(A), ptr(B), ptr(C), M, N, K, batch, int(bool(fp16)), stream_ptr(stream)))
+
+
+def gemm_batched_planes(A, B, C, M, N, K, batch, fp16=False, stream=None):
+    """C[b] = (A[b][:, :K] + A[b][:, K:]) @ B[b]^T, A rows 2K wide (split operand)."""
+    check(lib().vgb_gemm_batched_planes(ptr(A), ptr(B), ptr(C), M, N, K, batch, int(bool(fp16)),
+                                        stream_ptr(stream)))
 
 
 def fpfb(v: Voltages, ncc, nspectra, filt, i_idx, flags, out, stream=None):

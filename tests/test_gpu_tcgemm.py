@@ -44,6 +44,27 @@ def test_gemm_batched(fp16):
     assert err < 1e-5, err
 
 
+@pytest.mark.parametrize("fp16", [False, True])
+def test_gemm_batched_planes(fp16):
+    """Two A planes (hi | lo halves of each row) against one B: the same sum
+    as the K-concatenated product with B read modulo K, against FP32."""
+    torch = torch_cuda()
+    import vgb
+
+    M, N, K, nb = 384, 512, 192, 3
+    dt = torch.float16 if fp16 else torch.bfloat16
+    g = torch.Generator(device="cuda").manual_seed(21 + fp16)
+    A = torch.randn(nb, M, 2 * K, device="cuda", generator=g).to(dt)
+    B = torch.randn(nb, N, K, device="cuda", generator=g).to(dt)
+    C = torch.full((nb, M, N), float("nan"), device="cuda")
+    vgb.gemm_batched_planes(A, B, C, M, N, K, nb, fp16)
+    torch.cuda.synchronize()
+    assert vgb.check_device_status() == 0
+    ref = (A[:, :, :K].float() + A[:, :, K:].float()) @ B.float().transpose(1, 2)
+    err = (C - ref).abs().max().item() / ref.abs().max().item()
+    assert err < 1e-5, err
+
+
 @pytest.mark.parametrize("variant", [128, 256, 512])
 def test_gemm_variants_identical(variant):
     """Every kernel variant the autotuner chooses between (plain 128- and
