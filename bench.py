@@ -501,6 +501,63 @@ def multibeam_section(torch, vgb, SY, iters: int, cases=None, modes=None, nfine=
 # --------------------------------------------------------------------------
 # learned primary-beam surrogate (the beam model's stand-in for many beams)
 # --------------------------------------------------------------------------
+def beam_sweep(torch, vgb, SY, counts=(1, 4, 16, 64, 256, 1024), nant=256, nfine=K, ns=10000):
+    """Beams per coarse channel-second from 1 to 1024: the per-pointing CUDA-core
+    beamformer (vgb_beamform_legacy: Stokes at every 100 us sample, the
+    reference's own per-pointing structure) against the tensor-core path
+    (vgb_multibeam, split BF16 and FP16, Stokes integrated to 1 ms), on one
+    coarse channel-second of 4-bit legacy voltages from 256 tiles, full
+    Stokes. One timed call each after a warm-up, CUDA events."""
+    g = torch.Generator(device="cuda").manual_seed(5)
+    nb = ns * nfine * 2 * nant
+    re = torch.randn(nb, device="cuda", generator=g).mul_(2.5).round_().clamp_(-8, 7).to(torch.int32)
+    im = torch.randn(nb, device="cuda", generator=g).mul_(2.5).round_().clamp_(-8, 7).to(torch.int32)
+    v = (((re & 15) << 4) | (im & 15)).to(torch.uint8)
+    del re, im
+    polQ = torch.arange(0, 2 * nant, 2, dtype=torch.int32, device="cuda")
+    polP = polQ + 1
+    e, n, h, c = SY.tile_layout(nant)
+    to = lambda a: torch.from_numpy(np.ascontiguousarray(
+        a.view(np.float64) if a.dtype == np.complex128 else a)).cuda()
+    freqs = SY.fine_chan_freqs_hz(SY.coarse_chan_start_hz(0))[:nfine]
+    D = SY.calibration_jones(nant, nfine)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    rows = []
+    for B in counts:
+        row = {"beams": B}
+        W = torch.randn(B * nant * nfine * 8, device="cuda", generator=g)
+        S = torch.empty(B * ns * 4 * nfine, device="cuda")
+        row["cuda_cores_per_pointing_ms"] = timed(lambda: vgb.beamform_legacy(
+            v, 0, ns, nfine, nant, polQ, polP, W, B, 1.0 / (2 * nant), 4, S))
+        del W, S
+        side = int(np.ceil(np.sqrt(B)))
+        az, za = SY.grid_pointings(side, 0.02)
+        unit = SY.unit_vectors(az[:B], za[:B])
+        for mode, prec in (("split_bf16", vgb.MB_SPLIT_BF16), ("fp16", vgb.MB_FP16)):
+            mb = vgb.Multibeam(1, nfine, nant, B, ns, nstokes=4, precision=prec, input=vgb.MB_INT4)
+            mb.set_geometry(to(unit), to(e), to(n), to(h), to(c))
+            mb.set_jones(to(D), to(SY.identity_beam(B, nant)), to(freqs), polQ, polP)
+            row[f"tensor_{mode}_ms"] = timed(lambda: mb.run(v))
+            mb.close()
+        torch.cuda.empty_cache()
+        rows.append(row)
+    if vgb.check_device_status() != 0:
+        raise RuntimeError("device status raised in the beam sweep")
+    return {"workload": f"one coarse channel-second: {nant} tiles x 2 pols, 4-bit legacy voltages, {nfine} fine "
+                        f"channels x {ns} samples, full Stokes (per-pointing path at 100 us, tensor path "
+                        f"integrated to 1 ms)", "rows": rows}
+
+
 def sur_feed_beam_run(torch, vgb, SY, Bs, Bp, az, za, f_cc, ntile, nfreq, cc):
     """One coarse channel-second of the 1024-beam run (128 tiles, 4-bit
     voltages, split BF16, full Stokes) with the last tracked second's B (at
@@ -638,11 +695,22 @@ def main():
     ap.add_argument("--mb-modes", default=None, help="profiling: comma-separated precision modes")
     ap.add_argument("--mb-nfine", type=int, default=K, help="profiling: fine channels per case")
     ap.add_argument("--mb-stream-iters", type=int, default=3, help="many-beam host-streaming calls timed (0: skip)")
+    ap.add_argument("--beam-sweep", action="store_true",
+                    help="time 1..1024 beams per coarse channel-second on both beamformers and print their JSON")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per beam_kernel launch from an ncu capture (profiles/)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, local_rank, world = dist_env()
+    if args.beam_sweep:
+        import torch
+
+        import synthetic as SY
+        import vgb
+
+        vgb.lib()
+        print(json.dumps(beam_sweep(torch, vgb, SY)), flush=True)
+        return
     if args.mb_only:
         import torch
 

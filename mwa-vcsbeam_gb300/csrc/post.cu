@@ -280,12 +280,14 @@ int launch_incoh(const uint8_t *data, long long nrows, int ninput, float *incoh,
 
 // ---------------------------------------------------------------------------
 // Beamformer for legacy-layout fine voltages v[s][c][i].
-// A block covers 16 channels x 16 samples; the voltage rows are staged in
-// shared memory with a 4-byte pad so the per-antenna byte gathers of 32
-// threads fall in 32 different banks.
+// A block covers 16 channels x 4 samples = 64 voltage rows, four threads per
+// row splitting the tiles (tile = part, part + 4, ...) and combining their
+// sums with two shuffles; the 4+4-bit rows are staged in shared memory with a
+// 4-byte pad (33 KB for 256 tiles, so several blocks share an SM).
 // ---------------------------------------------------------------------------
 
-constexpr int kLS = 16, kLC = 16; // samples, channels per block
+constexpr int kLS = 4, kLC = 16; // samples, channels per block
+constexpr int kLParts = 4;       // threads per row
 
 template <bool kInt4>
 __global__ void __launch_bounds__(256) legacy_beam_kernel(const LegacyArgs a)
@@ -293,66 +295,84 @@ __global__ void __launch_bounds__(256) legacy_beam_kernel(const LegacyArgs a)
     extern __shared__ __align__(16) unsigned char lsm[];
     const int ni = 2 * a.nant;
     const int tid = threadIdx.x;
-    const int cl = tid & (kLC - 1), sl = tid >> 4;
+    const int r = tid / kLParts, part = tid % kLParts;
     const int c0 = blockIdx.x * kLC, s0 = blockIdx.y * kLS;
-    const int c = c0 + cl, s = s0 + sl;
+    const int c = c0 + r % kLC, s = s0 + r / kLC;
     const bool live = c < a.nchan && s < a.nsamples;
+    const int wpr = ni / 4 + 1;
 
-    // Stage the 4+4-bit rows (s, c) of this block, row stride ni/4 + 1 words.
-    // Complex FP64 voltages are read straight from global memory.
+    // Stage the 4+4-bit rows (s, c) of this block. Complex FP64 voltages are
+    // read straight from global memory.
     if (kInt4) {
-        const int wpr = ni / 4 + 1;
         uint32_t *rows = reinterpret_cast<uint32_t *>(lsm);
         const int nw = ni / 4;
-        for (int idx = tid; idx < kLS * kLC * nw; idx += 256) {
-            const int r = idx / nw, wdx = idx % nw;
-            const int rs = s0 + r / kLC, rc = c0 + r % kLC;
+        for (int idx = tid; idx < kLS * kLC * nw; idx += blockDim.x) {
+            const int rr = idx / nw, wdx = idx % nw;
+            const int rs = s0 + rr / kLC, rc = c0 + rr % kLC;
             uint32_t val = 0;
             if (rs < a.nsamples && rc < a.nchan)
                 val = __ldg(reinterpret_cast<const uint32_t *>(static_cast<const uint8_t *>(a.v) +
                                                                 ((long long)rs * a.nchan + rc) * ni) +
                             wdx);
-            rows[r * wpr + wdx] = val;
+            rows[rr * wpr + wdx] = val;
         }
     }
+    // the tiles' (Q, P) input pairs, checked against the row once per block
+    uint32_t *pq = reinterpret_cast<uint32_t *>(lsm + (kInt4 ? (size_t)kLS * kLC * wpr * 4 : 0));
+    for (int ant = tid; ant < a.nant; ant += blockDim.x) {
+        uint32_t iq = __ldg(a.polQ + ant), ip = __ldg(a.polP + ant);
+        if (iq >= (uint32_t)ni || ip >= (uint32_t)ni) {
+            if (blockIdx.x == 0 && blockIdx.y == 0) atomicOr(a.status, kErrBadInput);
+            iq = ip = 0;
+        }
+        pq[ant] = iq | (ip << 16);
+    }
     __syncthreads();
-    if (!live) return;
-    const int r = sl * kLC + cl;
+    const uint8_t *row8 = lsm + 4 * (r * wpr);
 
     for (int p = 0; p < a.npointing; p++) {
-        float acc[9];
+        float acc[8];
 #pragma unroll
-        for (int q = 0; q < 9; q++) acc[q] = 0.f;
-        const float4 *Wp = a.W + ((long long)p * a.nant * a.nchan + c) * 2;
-        for (int ant = 0; ant < a.nant; ant++) {
-            const uint32_t iq = __ldg(a.polQ + ant), ip = __ldg(a.polP + ant);
-            float2 vq, vp;
-            if (kInt4) {
-                const uint8_t *row = lsm + 4 * (r * (ni / 4 + 1));
-                const uint32_t bq = row[iq], bp = row[ip];
-                vq = make_float2((float)nib(bq >> 4), (float)nib(bq));
-                vp = make_float2((float)nib(bp >> 4), (float)nib(bp));
-            } else {
-                const double2 *row = static_cast<const double2 *>(a.v) + ((long long)s * a.nchan + c) * ni;
-                const double2 dq = __ldg(row + iq), dp = __ldg(row + ip);
-                vq = make_float2((float)dq.x, (float)dq.y);
-                vp = make_float2((float)dp.x, (float)dp.y);
+        for (int q = 0; q < 8; q++) acc[q] = 0.f;
+        const float4 *Wp = a.W + ((long long)p * a.nant * a.nchan + (live ? c : 0)) * 2;
+        if (live) {
+#pragma unroll 4
+            for (int ant = part; ant < a.nant; ant += kLParts) {
+                const uint32_t iqp = pq[ant], iq = iqp & 0xFFFFu, ip = iqp >> 16;
+                float2 vq, vp;
+                if (kInt4) {
+                    const uint32_t bq = row8[iq], bp = row8[ip];
+                    vq = make_float2((float)nib(bq >> 4), (float)nib(bq));
+                    vp = make_float2((float)nib(bp >> 4), (float)nib(bp));
+                } else {
+                    const double2 *row = static_cast<const double2 *>(a.v) + ((long long)s * a.nchan + c) * ni;
+                    const double2 dq = __ldg(row + iq), dp = __ldg(row + ip);
+                    vq = make_float2((float)dq.x, (float)dq.y);
+                    vp = make_float2((float)dp.x, (float)dp.y);
+                }
+                const float4 wa = __ldg(Wp + (long long)ant * a.nchan * 2);
+                const float4 wb = __ldg(Wp + (long long)ant * a.nchan * 2 + 1);
+                const float exr = wa.x * vq.x - wa.y * vq.y + wa.z * vp.x - wa.w * vp.y;
+                const float exi = wa.x * vq.y + wa.y * vq.x + wa.z * vp.y + wa.w * vp.x;
+                const float eyr = wb.x * vq.x - wb.y * vq.y + wb.z * vp.x - wb.w * vp.y;
+                const float eyi = wb.x * vq.y + wb.y * vq.x + wb.z * vp.y + wb.w * vp.x;
+                acc[0] += exr;
+                acc[1] += exi;
+                acc[2] += eyr;
+                acc[3] += eyi;
+                acc[4] = fmaf(exr, exr, fmaf(exi, exi, acc[4]));
+                acc[5] = fmaf(eyr, eyr, fmaf(eyi, eyi, acc[5]));
+                acc[6] = fmaf(exr, eyr, fmaf(exi, eyi, acc[6]));
+                acc[7] = fmaf(exi, eyr, fmaf(-exr, eyi, acc[7]));
             }
-            const float4 wa = __ldg(Wp + (long long)ant * a.nchan * 2);
-            const float4 wb = __ldg(Wp + (long long)ant * a.nchan * 2 + 1);
-            const float exr = wa.x * vq.x - wa.y * vq.y + wa.z * vp.x - wa.w * vp.y;
-            const float exi = wa.x * vq.y + wa.y * vq.x + wa.z * vp.y + wa.w * vp.x;
-            const float eyr = wb.x * vq.x - wb.y * vq.y + wb.z * vp.x - wb.w * vp.y;
-            const float eyi = wb.x * vq.y + wb.y * vq.x + wb.z * vp.y + wb.w * vp.x;
-            acc[0] += exr;
-            acc[1] += exi;
-            acc[2] += eyr;
-            acc[3] += eyi;
-            acc[4] = fmaf(exr, exr, fmaf(exi, exi, acc[4]));
-            acc[5] = fmaf(eyr, eyr, fmaf(eyi, eyi, acc[5]));
-            acc[6] = fmaf(exr, eyr, fmaf(exi, eyi, acc[6]));
-            acc[7] = fmaf(exi, eyr, fmaf(-exr, eyi, acc[7]));
         }
+        // the row's four partial sums (lanes 4k .. 4k+3 of a warp)
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], 1);
+            acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], 2);
+        }
+        if (!live || part != 0) continue;
         const float bnXX = acc[0] * acc[0] + acc[1] * acc[1] - acc[4];
         const float bnYY = acc[2] * acc[2] + acc[3] * acc[3] - acc[5];
         const float bxr = acc[0] * acc[2] + acc[1] * acc[3] - acc[6];
@@ -366,8 +386,8 @@ __global__ void __launch_bounds__(256) legacy_beam_kernel(const LegacyArgs a)
         }
         if (a.e) a.e[((long long)p * a.nsamples + s) * a.nchan + c] = make_float4(acc[0], acc[1], acc[2], acc[3]);
     }
-    if (kInt4 && a.incoh) {
-        const uint32_t *row = reinterpret_cast<const uint32_t *>(lsm) + r * (ni / 4 + 1);
+    if (kInt4 && a.incoh && live && part == 0) {
+        const uint32_t *row = reinterpret_cast<const uint32_t *>(lsm) + r * wpr;
         int accp = 0;
         for (int wdx = 0; wdx < ni / 4; wdx++) accp += power4(row[wdx]);
         a.incoh[(long long)s * a.nchan + c] = (float)accp;
@@ -380,9 +400,12 @@ int launch_legacy_beam(const LegacyArgs &a, cudaStream_t st)
     const int ni = 2 * a.nant;
     const bool int4 = a.datatype == VGB_INT4;
     if (int4 && (ni % 4) != 0) return set_error(VGB_ERR_INVALID, "legacy beamformer: 2*nant must be a multiple of 4");
-    const size_t smem = int4 ? (size_t)kLS * kLC * (ni / 4 + 1) * 4 : 16;
+    if (ni > 65535) return set_error(VGB_ERR_INVALID, "legacy beamformer: at most 65535 inputs");
+    const size_t smem = (int4 ? (size_t)kLS * kLC * (ni / 4 + 1) * 4 : 0) + (size_t)a.nant * 4;
     if (smem > 227 * 1024)
         return set_error(VGB_ERR_INVALID, "legacy beamformer: %d inputs do not fit the shared-memory tile", ni);
+    if ((a.nsamples + kLS - 1) / kLS > 65535)
+        return set_error(VGB_ERR_INVALID, "legacy beamformer: at most %d samples per call", 65535 * kLS);
     dim3 grid((a.nchan + kLC - 1) / kLC, (a.nsamples + kLS - 1) / kLS);
     if (int4) {
         int rc = check_cuda(cudaFuncSetAttribute(legacy_beam_kernel<true>,

@@ -300,6 +300,8 @@ int vgb_beamform_legacy(const void *v, int datatype, int nsamples, int nchan, in
     a.S = S_;
     a.e = static_cast<float4 *>(e);
     a.incoh = datatype == VGB_INT4 ? incoh : nullptr;
+    a.status = status_word();
+    if (!a.status) return set_error(VGB_ERR_CUDA, "device status word unavailable");
     return launch_legacy_beam(a, S(stream));
 }
 

@@ -57,6 +57,7 @@ struct LegacyArgs {
     float *S;                // [p][s][nstokes][nchan]
     float4 *e;               // [p][s][nchan] nullable
     float *incoh;            // [s][nchan] nullable (int4 only)
+    unsigned *status;        // kErrBadInput when polQ / polP name an input outside the row
 };
 
 struct IpfbArgs {

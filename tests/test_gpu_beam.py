@@ -155,6 +155,24 @@ def test_legacy_beamformer_many_pointings(vgb_mod, torch, oracle_mod):
         assert rel_err(Sg[p], Sref[p]) < 1e-5
 
 
+def test_legacy_beamformer_bad_input_index(vgb_mod, torch, oracle_mod):
+    """polQ naming an input outside the row (2 nant + 1) is reported through
+    the device status word, not read."""
+    nant, ns = 8, 16
+    v = oracle_mod.gen_int4_bytes(4, ns * K * 2 * nant).reshape(ns, K, 2 * nant)
+    polQ, polP = pol_lists(SY.legacy_input_order(nant, seed=2))
+    polQ = polQ.copy()
+    polQ[5] = 2 * nant + 1
+    J, phi = tables(nant)
+    W = weights_on_device(J, phi)
+    S = torch.empty(ns * 4 * K, dtype=torch.float32, device="cuda")
+    vgb_mod.beamform_legacy(dev(v), vgb_mod.INT4, ns, K, nant, dev(polQ), dev(polP), W, 1, 1 / 16, 4, S)
+    torch.cuda.synchronize()
+    with pytest.raises(vgb_mod.VGBError, match="input index"):
+        vgb_mod.check_device_status()
+    assert vgb_mod.check_device_status() == 0
+
+
 def test_device_tables_match_oracle(vgb_mod, torch, oracle_mod):
     nant, npnt = 24, 2
     D = SY.calibration_jones(nant, K, seed=4)
