@@ -177,7 +177,7 @@ __device__ __forceinline__ void wola_step(FrontSmem &sm, int s, int li, int n0, 
                 for (int q = 0; q < 4; q++) v[q] = (v[q] > 0 ? v[q] + 0x2000 : v[q]) >> 14;
                 b = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
             } else {
-                const float sc = 1.0f / 16384.0f;
+                const float sc = 1.0f / (16384.0f * kK); // 2^-14 and the FFT's 1/K, exact powers of two
                 b = make_float4((float)ar[m][0] * sc, (float)ai[m][0] * sc, (float)ar[m][1] * sc,
                                 (float)ai[m][1] * sc);
             }
@@ -209,7 +209,7 @@ __device__ __forceinline__ void wola_step(FrontSmem &sm, int s, int li, int n0, 
             if (kFpga) {
                 b = make_float4(fpga_round(ar[m].x), fpga_round(ai[m].x), fpga_round(ar[m].y), fpga_round(ai[m].y));
             } else {
-                const float2 sc = make_float2(1.0f / 16384.0f, 1.0f / 16384.0f);
+                const float2 sc = make_float2(1.0f / (16384.0f * kK), 1.0f / (16384.0f * kK));
                 const float2 r = __fmul2_rn(ar[m], sc), i = __fmul2_rn(ai[m], sc);
                 b = make_float4(r.x, i.x, r.y, i.y);
             }
@@ -227,7 +227,10 @@ __device__ __forceinline__ float demote4(float x)
 
 // Steps 4-5: FFT of row g = (li, m) by the 8 threads of a group, in place;
 // the row then holds the shifted, scaled, (im, re)-ordered voltages at k'.
-template <bool kDemote>
+// kScale: apply the 1/K here (after FPGA rounding); without FPGA rounding the
+// WOLA output already carries it (scaling by a power of two commutes exactly
+// with the FFT's arithmetic).
+template <bool kDemote, bool kScale>
 __device__ __forceinline__ void fft_step(FrontSmem &sm, int tid)
 {
     const int g = tid >> 3, j = tid & 7;
@@ -244,7 +247,7 @@ __device__ __forceinline__ void fft_step(FrontSmem &sm, int tid)
             const int k = 2 * j + h + 16 * k2;
             const int kp = (k + kK / 2) & (kK - 1);
             const float2 X = out[h][k2];
-            float vr = X.y * (1.0f / kK), vi = X.x * (1.0f / kK);
+            float vr = kScale ? X.y * (1.0f / kK) : X.y, vi = kScale ? X.x * (1.0f / kK) : X.x;
             if (kDemote) {
                 vr = demote4(vr);
                 vi = demote4(vi);
@@ -341,7 +344,7 @@ __global__ void __launch_bounds__(kThreads, 2) beam_kernel(const BeamArgs a)
         if (tid < 32 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, Wcc, a.nant, a.status);
         wola_step<kInt32, kFpga>(sm, it & 1, li, n0, hc);
         input_barrier(li);
-        fft_step<kDemote>(sm, tid);
+        fft_step<kDemote, kFpga>(sm, tid);
         __syncthreads();
 #pragma unroll
         for (int aa = 0; aa < 2; aa++) {
@@ -426,7 +429,7 @@ __global__ void __launch_bounds__(kThreads, 2) pack_kernel(const PackArgs a)
         if (tid < 32 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, nullptr, 0, a.status);
         wola_step<kInt32, kFpga>(sm, it & 1, li, n0, hc);
         input_barrier(li);
-        fft_step<kDemote>(sm, tid);
+        fft_step<kDemote, kFpga>(sm, tid);
         __syncthreads();
 #pragma unroll
         for (int r = 0; r < kG; r++) {
