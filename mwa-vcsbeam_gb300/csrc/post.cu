@@ -10,6 +10,8 @@
 //  * beamformer for fine-channel voltages already in legacy layout
 //    (v_IDX [s][c][i], 4+4-bit or complex FP64): vmApplyJ_kernel followed by
 //    vmBeamform_kernel (form_beam.cpp:122-371) in one pass.
+#include <cooperative_groups.h>
+
 #include "vgb_launch.cuh"
 
 namespace vgb {
@@ -180,22 +182,34 @@ int launch_weights(const double2 *J, const double2 *phi, long long n, float4 *W,
 // to an integer and keep the low 8 bits, so a channel's maximum sample
 // (256.5) becomes 0; NaN becomes 0. val is never negative here.
 // One warp lane per channel; the 8 warps of a block split the samples.
+constexpr int kRenormSplit = 8; // CTAs (one thread-block cluster) per (cc, pointing, stokes, 32 channels)
+
+// Cluster of kRenormSplit CTAs over one (cc, pointing, stokes, 32 channels):
+// CTA r scans samples [r n / 8, (r + 1) n / 8). Sequential-scan semantics of
+// the reference: every partial starts from sample 0 and uses the same
+// comparisons, so combining them in any order gives the same extremes (a NaN
+// first sample makes the result NaN; other NaNs are skipped). The partials
+// meet through distributed shared memory; each CTA then quantises its samples.
 __global__ void __launch_bounds__(256) renorm_kernel(const RenormArgs a)
 {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
     __shared__ float smin[8][32], smax[8][32];
+    __shared__ float cmin[32], cmax[32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int c = blockIdx.x * 32 + lane;
+    const int part = (int)cluster.block_rank();
+    const int c = (blockIdx.x / kRenormSplit) * 32 + lane;
     const int st = blockIdx.y % a.nstokes, p = blockIdx.y / a.nstokes;
     const int cc = blockIdx.z;
     const bool live = c < a.nchan;
     const long long sstride = (long long)a.nstokes * a.nchan;
     const float *S = a.S + cc * a.S_cc + ((long long)p * a.nstep * a.nstokes + st) * a.nchan + (live ? c : 0);
+    const int sb = (int)((long long)a.nstep * part / kRenormSplit);
+    const int se = (int)((long long)a.nstep * (part + 1) / kRenormSplit);
 
-    // Sequential-scan semantics of the reference: every partial starts from
-    // sample 0 and uses the same comparisons, so the result is the same.
     const float s0 = S[0];
     float mn = s0, mx = s0;
-    for (int s = wid; s < a.nstep; s += 8) {
+    for (int s = sb + wid; s < se; s += 8) {
         const float v = S[s * sstride];
         mn = (v < mn ? v : mn);
         mx = (v > mx ? v : mx);
@@ -203,20 +217,32 @@ __global__ void __launch_bounds__(256) renorm_kernel(const RenormArgs a)
     smin[wid][lane] = mn;
     smax[wid][lane] = mx;
     __syncthreads();
-    mn = smin[0][lane];
-    mx = smax[0][lane];
-    for (int w = 1; w < 8; w++) {
-        const float v0 = smin[w][lane], v1 = smax[w][lane];
+    if (wid == 0) {
+        for (int w = 1; w < 8; w++) {
+            const float v0 = smin[w][lane], v1 = smax[w][lane];
+            mn = (v0 < mn ? v0 : mn);
+            mx = (v1 > mx ? v1 : mx);
+        }
+        cmin[lane] = mn;
+        cmax[lane] = mx;
+    }
+    cluster.sync(); // every CTA's partial is in its shared memory
+    mn = s0;
+    mx = s0;
+    for (int r = 0; r < kRenormSplit; r++) {
+        const float v0 = *cluster.map_shared_rank(&cmin[lane], r);
+        const float v1 = *cluster.map_shared_rank(&cmax[lane], r);
         mn = (v0 < mn ? v0 : mn);
         mx = (v1 > mx ? v1 : mx);
     }
+    cluster.sync(); // no CTA leaves while another still reads its partials
     const float scale = (float)((double)(mx - mn) / 256.0);
     const float offset = mn;
     if (live) {
         uint8_t *o = a.out + cc * a.out_cc + p * a.out_p + st * a.out_st + c;
         const float rcp = 1.f / scale;
-        for (int s = wid; s < a.nstep; s += 8) o[s * a.out_s] = quant_u8(S[s * sstride], offset, scale, rcp);
-        if (wid == 0) {
+        for (int s = sb + wid; s < se; s += 8) o[s * a.out_s] = quant_u8(S[s * sstride], offset, scale, rcp);
+        if (part == 0 && wid == 0) {
             const long long si = cc * a.stat_cc + ((long long)p * a.nstokes + st) * a.nchan + c;
             a.scales[si] = scale;
             a.offsets[si] = offset;
@@ -227,9 +253,19 @@ __global__ void __launch_bounds__(256) renorm_kernel(const RenormArgs a)
 int launch_renorm(const RenormArgs &a, int ncc, cudaStream_t st)
 {
     if (a.nstep <= 0 || ncc <= 0) return VGB_SUCCESS;
-    dim3 grid((a.nchan + 31) / 32, a.npointing * a.nstokes, ncc);
-    renorm_kernel<<<grid, 256, 0, st>>>(a);
-    return check_launch("renorm_kernel");
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kRenormSplit * ((a.nchan + 31) / 32), a.npointing * a.nstokes, ncc);
+    cfg.blockDim = dim3(256);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kRenormSplit;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const int rc = check_cuda(cudaLaunchKernelEx(&cfg, renorm_kernel, a), "cudaLaunchKernelEx(renorm_kernel)");
+    return rc ? rc : check_launch("renorm_kernel");
 }
 
 // ---------------------------------------------------------------------------
