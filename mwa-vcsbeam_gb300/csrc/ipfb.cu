@@ -51,17 +51,29 @@ __global__ void __launch_bounds__(256) ipfb_kernel(const IpfbArgs a)
     // load X_k[m] for m in [f0 - 11, f0 + kIFT), de-interleaving the pols
     const float4 *e = a.e + job * a.e_job;
     const float4 *hist = a.hist ? a.hist + job * a.hist_job : nullptr;
+    // asynchronous 8-byte copies, all in flight before one wait; samples with
+    // no source (outside the second and its history) are zero-filled
     for (int idx = tid; idx < (kIFT + kP - 1) * kK; idx += 256) {
         const int ml = idx / kK, k = idx % kK;
         const int m = mlo + ml;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (m >= 0 && m < a.nsamples)
-            v = __ldg(e + (long long)m * kK + k);
-        else if (m < 0 && hist && m >= -kP)
-            v = __ldg(hist + (long long)(m + kP) * kK + k);
-        sm.y[2 * ml][k] = make_float2(v.x, v.y);
-        sm.y[2 * ml + 1][k] = make_float2(v.z, v.w);
+        const float4 *src = e;
+        uint32_t bytes = 0;
+        if (m >= 0 && m < a.nsamples) {
+            src = e + (long long)m * kK + k;
+            bytes = 8;
+        } else if (m < 0 && hist && m >= -kP) {
+            src = hist + (long long)(m + kP) * kK + k;
+            bytes = 8;
+        }
+        const float2 *s2 = reinterpret_cast<const float2 *>(src);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(&sm.y[2 * ml][k])), "l"(s2),
+                     "r"(bytes)
+                     : "memory");
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(&sm.y[2 * ml + 1][k])),
+                     "l"(s2 + 1), "r"(bytes)
+                     : "memory");
     }
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
     __syncthreads();
 
     // inverse FFTs, 32 transforms per pass, (-1)^r applied on the way out
