@@ -340,18 +340,21 @@ __global__ void __launch_bounds__(256) legacy_beam_kernel(const LegacyArgs a)
     // Stage the 4+4-bit rows (s, c) of this block. Complex FP64 voltages are
     // read straight from global memory.
     if (kInt4) {
+        // 4-byte asynchronous copies, all in flight before one wait (rows
+        // outside the block's samples or channels are zero-filled)
         uint32_t *rows = reinterpret_cast<uint32_t *>(lsm);
         const int nw = ni / 4;
+        const uint32_t *v32 = static_cast<const uint32_t *>(a.v);
         for (int idx = tid; idx < kLS * kLC * nw; idx += blockDim.x) {
             const int rr = idx / nw, wdx = idx % nw;
             const int rs = s0 + rr / kLC, rc = c0 + rr % kLC;
-            uint32_t val = 0;
-            if (rs < a.nsamples && rc < a.nchan)
-                val = __ldg(reinterpret_cast<const uint32_t *>(static_cast<const uint8_t *>(a.v) +
-                                                                ((long long)rs * a.nchan + rc) * ni) +
-                            wdx);
-            rows[rr * wpr + wdx] = val;
+            const bool in = rs < a.nsamples && rc < a.nchan;
+            const uint32_t *src = in ? v32 + ((long long)rs * a.nchan + rc) * (ni / 4) + wdx : v32;
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(&rows[rr * wpr + wdx])),
+                         "l"(src), "r"(in ? 4u : 0u)
+                         : "memory");
         }
+        asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
     }
     // the tiles' (Q, P) input pairs, checked against the row once per block
     uint32_t *pq = reinterpret_cast<uint32_t *>(lsm + (kInt4 ? (size_t)kLS * kLC * wpr * 4 : 0));
