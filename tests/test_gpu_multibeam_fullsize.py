@@ -1,0 +1,97 @@
+"""The 1024-beam case at its full size (256 tiles x 2 pols of 4-bit voltages,
+1024 beams, 128 fine channels x 1 s, full Stokes at 1 ms, split BF16),
+checked through properties that do not depend on size:
+
+* the 8-bit PSRFITS bytes, offsets and scales equal the oracle's renormalise
+  of the device's own Stokes, bit for bit;
+* three beams x two channels x the first 20 integrations match the FP64
+  oracle chain (reference tables, per-sample beamformer summed over each
+  integration) within 1e-4 of each Stokes parameter's largest magnitude;
+* beams are independent: permuting the pointings (and their primary-beam
+  matrices) permutes every product, bit for bit.
+"""
+import numpy as np
+import pytest
+
+import synthetic as SY
+from helpers import dev, host, pol_lists, torch_cuda
+
+pytestmark = pytest.mark.gpu
+
+NANT, NF, NS, NB, NINT = 256, 128, 10000, 1024, 10
+NT = NS // NINT
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return torch_cuda()
+
+
+@pytest.fixture(scope="module")
+def vgb_mod(torch):
+    import vgb
+
+    vgb.lib()
+    return vgb
+
+
+def test_multibeam_full_size(vgb_mod, torch, oracle_mod):
+    O, vgb = oracle_mod, vgb_mod
+    D = SY.calibration_jones(NANT, NF, seed=3)
+    B = np.ascontiguousarray(SY.identity_beam(NB, NANT) +
+                             0.05 * (1 + 1j) * O.gauss(7, NB * NANT * 4).reshape(NB, NANT, 2, 2))
+    east, north, height, cable = SY.tile_layout(NANT, seed=5)
+    az, za = SY.grid_pointings(32, 0.02)
+    unit = np.ascontiguousarray(SY.unit_vectors(az, za))
+    freqs = SY.fine_chan_freqs_hz(SY.coarse_chan_start_hz(0))[:NF].astype(np.float64)
+    polQ, polP = pol_lists(SY.legacy_input_order(NANT))
+    g = torch.Generator(device="cuda").manual_seed(11)
+    nb = NS * NF * 2 * NANT
+    re = torch.randn(nb, device="cuda", generator=g).mul_(2.5).round_().clamp_(-8, 7).to(torch.int32)
+    im = torch.randn(nb, device="cuda", generator=g).mul_(2.5).round_().clamp_(-8, 7).to(torch.int32)
+    v = (((re & 15) << 4) | (im & 15)).to(torch.uint8)
+    del re, im
+    invw = 1.0 / (2 * NANT)
+
+    def run(unit_, B_):
+        mb = vgb.Multibeam(1, NF, NANT, NB, NS, nstokes=4, precision=vgb.MB_SPLIT_BF16, input=vgb.MB_INT4,
+                           invw=invw)
+        mb.set_geometry(dev(unit_), dev(east), dev(north), dev(height), dev(cable))
+        mb.set_jones(dev(D), dev(np.ascontiguousarray(B_)), dev(freqs), dev(polQ), dev(polP))
+        S = torch.empty(NF * NB * 4 * NT, dtype=torch.float32, device="cuda")
+        out = torch.empty(NB * NT * 4 * NF, dtype=torch.uint8, device="cuda")
+        off = torch.empty(NB * 4 * NF, dtype=torch.float32, device="cuda")
+        scl = torch.empty_like(off)
+        mb.run(v, S=S, out=out, offsets=off, scales=scl)
+        torch.cuda.synchronize()
+        assert vgb.check_device_status() == 0
+        mb.close()
+        return (host(S).reshape(NF, NB, 4, NT), host(out).reshape(NB, NT, 4, NF), host(off).reshape(NB, 4, NF),
+                host(scl).reshape(NB, 4, NF))
+
+    S1, u1, off1, sc1 = run(unit, B)
+
+    # PSRFITS bytes from the device's own Stokes, in [beam][t][stokes][chan]
+    off, sc, u8 = O.renormalise(np.ascontiguousarray(S1.transpose(1, 3, 2, 0)))
+    assert np.array_equal(u1, u8)
+    assert np.array_equal(off1, off) and np.array_equal(sc1, sc)
+
+    # spot check against the FP64 oracle chain
+    beams, chans, nsamp = [0, 517, 1023], [0, 77], 20 * NINT
+    vsub = np.ascontiguousarray(v[: nsamp * NF * 2 * NANT].cpu().numpy().reshape(nsamp, NF, 2 * NANT)[:, chans])
+    J = O.calc_j(np.ascontiguousarray(D[:, chans]), np.ascontiguousarray(B[beams]))
+    phi = O.calc_phi(unit[beams], east, north, height, cable, freqs[chans])
+    Sref, _ = O.beamform(vsub, J, phi, polQ, polP, invw, nstokes=4, want_e=False)
+    ref = Sref.astype(np.float64).reshape(len(beams), 20, NINT, 4, len(chans)).sum(axis=2)   # [p][t][st][c]
+    got = S1[chans][:, beams][..., :20].transpose(1, 3, 2, 0)                               # [p][t][st][c]
+    for st in range(4):
+        err = np.abs(got[:, :, st] - ref[:, :, st]).max() / np.abs(ref[:, :, st]).max()
+        assert err < 1e-4, (st, err)
+
+    # permuting the pointings permutes the products
+    perm = np.random.default_rng(13).permutation(NB)
+    S2, u2, off2, sc2 = run(unit[perm], B[perm])
+    assert np.array_equal(S2, S1[:, perm])
+    assert np.array_equal(u2, u1[perm])
+    assert np.array_equal(off2, off1[perm]) and np.array_equal(sc2, sc1[perm])
+    torch.cuda.empty_cache()
