@@ -117,6 +117,13 @@ typedef struct vgb_voltages {
 int vgb_beamform_mwax(const vgb_voltages *v, int ncc, int nspectra, const int32_t *filter, int ntaps,
                       int nchan, unsigned pfb_flags, const void *W, int nant, float invw, int nstokes,
                       float *S, void *e, float *incoh, void *stream);
+/* The fused front end takes 4 inputs (two tiles) per step in 256-thread CTAs
+ * (two per SM) or 8 inputs per step in 512-thread CTAs (one per SM); both give
+ * identical results. The first call for a shape times both and keeps the
+ * faster (a call made while the stream is being captured uses the known
+ * choice, else 4). Force one with 4 or 8, or 0 for the timed choice; returns
+ * the previous setting, -1 on a bad value. */
+int vgb_pfb_variant(int inputs_per_step);
 
 /*
  * Forward fine PFB only, packed to the legacy recombined layout (the output

@@ -20,23 +20,30 @@
 //      (form_beam.cpp:298-315) and the incoherent sum; or the PFB-only back
 //      end, which writes the packed legacy-order output (pfb.cpp:316-340).
 // The fine-channel voltages never reach HBM on the beamformer path.
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "vgb_launch.cuh"
 
 namespace vgb {
 
 constexpr int kT = 8;                      // spectra per CTA
-constexpr int kG = 4;                      // inputs per step (two tiles)
+constexpr int kG = 4;                      // inputs per step (two tiles) of the PFB-only kernel
 constexpr int kThreads = 256;
 constexpr int kWin = kT + kP - 1;          // frames per input per step
 constexpr int kFrameBytes = kK * 2;        // 256
 
-struct FrontSmem {
-    char2 stage[2][kG][kWin][kK];          // TMA destinations: frames
-    float4 wst[2][2][kK][2];               // TMA destinations: weights of the step's two tiles
-    float2 buf[kG * kT][kFftRow];          // WOLA output -> FFT (in place) -> voltages
+// Shared memory of a front-end CTA taking G inputs (G/2 tiles) per step with
+// 64 threads per input: 95 KB for G = 4 (two CTAs per SM), 188 KB for G = 8.
+template <int G> struct FrontSmemT {
+    char2 stage[2][G][kWin][kK];           // TMA destinations: frames
+    float4 wst[2][G / 2][kK][2];           // TMA destinations: weights of the step's tiles
+    float2 buf[G * kT][kFftRow];           // WOLA output -> FFT (in place) -> voltages
     float2 tw[128];                        // W128 twiddles, [k1][j]
     uint64_t bar[2];
 };
+using FrontSmem = FrontSmemT<kG>;
 
 // ---------------------------------------------------------------------------
 // Copy the frames input `i` needs for spectra [m0, m0 + kT) into `dst`.
@@ -75,32 +82,34 @@ __device__ __forceinline__ uint32_t issue_frames(const VoltView &vv, int cc, int
 // Producer: warp 0 queues step `it`'s frames (and, when W is given, the
 // weight rows of its two tiles) into stage it & 1, one input per lane (lane
 // kG the weights), so the copy set-up costs the warp about one input's worth.
-__device__ __forceinline__ void produce(FrontSmem &sm, const VoltView &vv, int cc, int it, int m0, int nspectra,
+template <int G>
+__device__ __forceinline__ void produce(FrontSmemT<G> &sm, const VoltView &vv, int cc, int it, int m0, int nspectra,
                                        const float4 *Wcc, int nant, unsigned *status)
 {
     const int lane = threadIdx.x & 31;
     const int s = it & 1;
     const int w_end = min(m0 + kWin, nspectra + kP - 1);
     uint32_t total = 0;
-    for (int li = 0; li < kG; li++)
-        if (it * kG + li < vv.ninputs) total += (w_end - m0) * kFrameBytes;
+    for (int li = 0; li < G; li++)
+        if (it * G + li < vv.ninputs) total += (w_end - m0) * kFrameBytes;
     int nw = 0;
     if (Wcc) {
-        nw = min(2, nant - 2 * it);
+        nw = min(G / 2, nant - (G / 2) * it);
         total += nw * kK * 32;
     }
     if (lane == 0) mbar_arrive_expect_tx(&sm.bar[s], total);
     __syncwarp();
     uint32_t issued = 0;
-    if (lane < kG) {
-        const int i = it * kG + lane;
+    if (lane < G) {
+        const int i = it * G + lane;
         if (i < vv.ninputs) issued = issue_frames(vv, cc, i, m0, w_end, sm.stage[s][lane][0], &sm.bar[s], status);
-    } else if (lane == kG && nw > 0) {
-        bulk_g2s(sm.wst[s][0][0], Wcc + (long long)(2 * it) * kK * 2, nw * kK * 32, &sm.bar[s]);
+    } else if (lane == G && nw > 0) {
+        bulk_g2s(sm.wst[s][0][0], Wcc + (long long)((G / 2) * it) * kK * 2, nw * kK * 32, &sm.bar[s]);
         issued = nw * kK * 32;
     }
+    // lanes 0..G issue copies: a butterfly over the lowest 8 (G = 4) or 16 lanes
 #pragma unroll
-    for (int o = 4; o; o >>= 1) issued += __shfl_xor_sync(0xffffffffu, issued, o);
+    for (int o = G >= 8 ? 8 : 4; o; o >>= 1) issued += __shfl_xor_sync(0xffffffffu, issued, o);
     if (lane == 0 && issued != total) {
         // Some frames were outside the buffers: complete the remaining
         // transaction count so consumers are not left waiting; the status
@@ -144,8 +153,8 @@ __device__ __forceinline__ float fpga_round(float X)
 // ---------------------------------------------------------------------------
 // Steps 2-3: weighted overlap-add for thread (li, n0..n0+1) into buf rows.
 // ---------------------------------------------------------------------------
-template <bool kInt32, bool kFpga>
-__device__ __forceinline__ void wola_step(FrontSmem &sm, int s, int li, int n0, const int (&hc)[2][kP])
+template <bool kInt32, bool kFpga, int G>
+__device__ __forceinline__ void wola_step(FrontSmemT<G> &sm, int s, int li, int n0, const int (&hc)[2][kP])
 {
     const uint32_t *x = reinterpret_cast<const uint32_t *>(sm.stage[s][li][0] + n0);
     if (kInt32) {
@@ -230,8 +239,8 @@ __device__ __forceinline__ float demote4(float x)
 // kScale: apply the 1/K here (after FPGA rounding); without FPGA rounding the
 // WOLA output already carries it (scaling by a power of two commutes exactly
 // with the FFT's arithmetic).
-template <bool kDemote, bool kScale>
-__device__ __forceinline__ void fft_step(FrontSmem &sm, int tid)
+template <bool kDemote, bool kScale, int G>
+__device__ __forceinline__ void fft_step(FrontSmemT<G> &sm, int tid)
 {
     const int g = tid >> 3, j = tid & 7;
     float2 *row = sm.buf[g];
@@ -256,7 +265,7 @@ __device__ __forceinline__ void fft_step(FrontSmem &sm, int tid)
         }
 }
 
-__device__ __forceinline__ void init_front(FrontSmem &sm, int tid)
+template <int G> __device__ __forceinline__ void init_front(FrontSmemT<G> &sm, int tid)
 {
     if (tid < 128) {
         const int k1 = tid >> 3, j = tid & 7;
@@ -291,7 +300,7 @@ __device__ __forceinline__ void input_barrier(int li)
 // Wait for step `it`'s data; every thread learns whether any thread timed
 // out, so the CTA leaves together. The barrier also orders the previous
 // step's reads of the buffers before this step's writes.
-__device__ __forceinline__ bool wait_frames(FrontSmem &sm, int it, unsigned *status)
+template <int G> __device__ __forceinline__ bool wait_frames(FrontSmemT<G> &sm, int it, unsigned *status)
 {
     const bool ok = mbar_wait_bounded(&sm.bar[it & 1], (it >> 1) & 1, 1u << 22);
     const int any_bad = __syncthreads_or(!ok);
@@ -300,7 +309,7 @@ __device__ __forceinline__ bool wait_frames(FrontSmem &sm, int it, unsigned *sta
 }
 
 // Before leaving early, give copies in flight a bounded chance to land.
-__device__ __forceinline__ void drain(FrontSmem &sm, int it)
+template <int G> __device__ __forceinline__ void drain(FrontSmemT<G> &sm, int it)
 {
     if (threadIdx.x == 0) mbar_wait_bounded(&sm.bar[it & 1], (it >> 1) & 1, 1u << 20);
     __syncthreads();
@@ -309,15 +318,22 @@ __device__ __forceinline__ void drain(FrontSmem &sm, int it)
 // ---------------------------------------------------------------------------
 // Beamformer kernel.
 // ---------------------------------------------------------------------------
-template <bool kInt32, bool kFpga, bool kDemote>
-__global__ void __launch_bounds__(kThreads, 2) beam_kernel(const BeamArgs a)
+// G inputs (G/2 tiles) per step, 64 G threads: G = 4 (two CTAs per SM) or
+// G = 8 (one CTA of 512 threads, half the steps and block barriers per
+// input). Every (k', m) is summed by one thread over the tiles in the same
+// order either way, so both give identical results; the host picks by timing.
+template <bool kInt32, bool kFpga, bool kDemote, int G>
+__global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1) beam_kernel(const BeamArgs a)
 {
+    constexpr int kTiles = G / 2;        // tiles per step
+    constexpr int kMh = G / 2;           // threads per k' (spectra m = mh + kMh mi)
+    constexpr int kMi = kT / kMh;        // spectra per thread
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    FrontSmem &sm = *reinterpret_cast<FrontSmem *>(smem_raw);
+    FrontSmemT<G> &sm = *reinterpret_cast<FrontSmemT<G> *>(smem_raw);
     const int tid = threadIdx.x;
     const int cc = blockIdx.y;
     const int m0 = blockIdx.x * kT;
-    const int nsteps = (a.vv.ninputs + kG - 1) / kG;
+    const int nsteps = (a.vv.ninputs + G - 1) / G;
     const float4 *Wcc = a.W + cc * a.W_cc;
 
     init_front(sm, tid);
@@ -327,11 +343,11 @@ __global__ void __launch_bounds__(kThreads, 2) beam_kernel(const BeamArgs a)
     __syncthreads();
     if (tid < 32) produce(sm, a.vv, cc, 0, m0, a.nspectra, Wcc, a.nant, a.status);
 
-    // beam accumulators for (k', m = mh + 2 mi)
+    // beam accumulators for (k', m = mh + kMh mi)
     const int kp = tid & (kK - 1), mh = tid >> 7;
-    float acc[4][9];
+    float acc[kMi][9];
 #pragma unroll
-    for (int mi = 0; mi < 4; mi++)
+    for (int mi = 0; mi < kMi; mi++)
 #pragma unroll
         for (int q = 0; q < 9; q++) acc[mi][q] = 0.f;
 
@@ -347,14 +363,14 @@ __global__ void __launch_bounds__(kThreads, 2) beam_kernel(const BeamArgs a)
         fft_step<kDemote, kFpga>(sm, tid);
         __syncthreads();
 #pragma unroll
-        for (int aa = 0; aa < 2; aa++) {
-            const int ant = it * 2 + aa;
+        for (int aa = 0; aa < kTiles; aa++) {
+            const int ant = it * kTiles + aa;
             if (ant >= a.nant) break;
             const float4 wa = sm.wst[it & 1][aa][kp][0];
             const float4 wb = sm.wst[it & 1][aa][kp][1];
 #pragma unroll
-            for (int mi = 0; mi < 4; mi++) {
-                const int m = mh + 2 * mi;
+            for (int mi = 0; mi < kMi; mi++) {
+                const int m = mh + kMh * mi;
                 const float2 vq = sm.buf[(2 * aa) * kT + m][kp];
                 const float2 vp = sm.buf[(2 * aa + 1) * kT + m][kp];
                 const float exr = wa.x * vq.x - wa.y * vq.y + wa.z * vp.x - wa.w * vp.y;
@@ -377,8 +393,8 @@ __global__ void __launch_bounds__(kThreads, 2) beam_kernel(const BeamArgs a)
 
     // form_beam.cpp:322-338
 #pragma unroll
-    for (int mi = 0; mi < 4; mi++) {
-        const int m = m0 + mh + 2 * mi;
+    for (int mi = 0; mi < kMi; mi++) {
+        const int m = m0 + mh + kMh * mi;
         if (m >= a.nspectra) continue;
         const float *c = acc[mi];
         const float bnXX = c[0] * c[0] + c[1] * c[1] - c[4];
@@ -460,11 +476,11 @@ __global__ void __launch_bounds__(kThreads, 2) pack_kernel(const PackArgs a)
 // ---------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------
-static size_t front_smem() { return sizeof(FrontSmem); }
+template <int G = kG> static size_t front_smem() { return sizeof(FrontSmemT<G>); }
 
-template <class K> static int prep(K kern)
+template <int G = kG, class K> static int prep(K kern)
 {
-    return check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)front_smem()),
+    return check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)front_smem<G>()),
                       "cudaFuncSetAttribute(front smem)");
 }
 
@@ -485,25 +501,88 @@ static int dispatch(const Args &a, dim3 grid, bool i32, bool fpga, bool demote, 
     }
 }
 
+static int g_pfb_variant = 0; // 0: autotuned; else forced inputs per step (4 or 8)
+
 template <bool A, bool B, bool C> struct BeamSel {
+    static int run_g(const BeamArgs &a, dim3 grid, cudaStream_t st, int g)
+    {
+        if (g == 8) {
+            int rc = prep<8>(beam_kernel<A, B, C, 8>);
+            if (rc) return rc;
+            beam_kernel<A, B, C, 8><<<grid, 512, front_smem<8>(), st>>>(a);
+        } else {
+            int rc = prep<4>(beam_kernel<A, B, C, 4>);
+            if (rc) return rc;
+            beam_kernel<A, B, C, 4><<<grid, 256, front_smem<4>(), st>>>(a);
+        }
+        return check_launch("beam_kernel");
+    }
+    // Inputs per step for this shape: timed once per shape (one warm-up and
+    // two timed launches of each variant with CUDA events on the caller's
+    // stream; the outputs are the same either way) and cached. While the
+    // stream is being captured the cached choice is used if known, else 4.
     static int run(const BeamArgs &a, dim3 grid, cudaStream_t st)
     {
-        int rc = prep(beam_kernel<A, B, C>);
+        if (g_pfb_variant) return run_g(a, grid, st, g_pfb_variant);
+        static std::mutex mu;
+        static std::map<std::tuple<int, int, int, int, int, bool, bool>, int> cache;
+        const auto key = std::make_tuple((int)grid.x, (int)grid.y, a.vv.ninputs, a.nant, a.nstokes, a.e != nullptr,
+                                         a.incoh != nullptr);
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            auto it = cache.find(key);
+            if (it != cache.end()) return run_g(a, grid, st, it->second);
+        }
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(st, &cs);
+        if (cs != cudaStreamCaptureStatusNone) return run_g(a, grid, st, 4);
+        cudaEvent_t e0, e1;
+        int rc = check_cuda(cudaEventCreate(&e0), "cudaEventCreate");
+        if (!rc) rc = check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
+        float best = 0.f;
+        int pick = 4;
+        for (int g : {4, 8}) {
+            if (rc) break;
+            rc = run_g(a, grid, st, g);
+            if (!rc) rc = check_cuda(cudaEventRecord(e0, st), "cudaEventRecord");
+            for (int r = 0; r < 2 && !rc; r++) rc = run_g(a, grid, st, g);
+            if (!rc) rc = check_cuda(cudaEventRecord(e1, st), "cudaEventRecord");
+            if (!rc) rc = check_cuda(cudaEventSynchronize(e1), "cudaEventSynchronize");
+            float ms = 0.f;
+            if (!rc) rc = check_cuda(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+            if (!rc && (g == 4 || ms < best)) {
+                best = ms;
+                pick = g;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
         if (rc) return rc;
-        beam_kernel<A, B, C><<<grid, kThreads, front_smem(), st>>>(a);
-        return check_launch("beam_kernel");
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            cache[key] = pick;
+        }
+        return run_g(a, grid, st, pick);
     }
 };
 
 template <bool A, bool B, bool C> struct PackSel {
     static int run(const PackArgs &a, dim3 grid, cudaStream_t st)
     {
-        int rc = prep(pack_kernel<A, B, C>);
+        int rc = prep<kG>(pack_kernel<A, B, C>);
         if (rc) return rc;
-        pack_kernel<A, B, C><<<grid, kThreads, front_smem(), st>>>(a);
+        pack_kernel<A, B, C><<<grid, kThreads, front_smem<kG>(), st>>>(a);
         return check_launch("pack_kernel");
     }
 };
+
+int pfb_variant(int g)
+{
+    if (g != 0 && g != 4 && g != 8) return -1;
+    const int prev = g_pfb_variant;
+    g_pfb_variant = g;
+    return prev;
+}
 
 int launch_beam(const BeamArgs &a, int ncc, bool int32_wola, bool fpga, bool demote, cudaStream_t st)
 {

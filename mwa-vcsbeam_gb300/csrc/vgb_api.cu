@@ -190,6 +190,13 @@ int vgb_beamform_mwax(const vgb_voltages *v, int ncc, int nspectra, const int32_
                        (pfb_flags & VGB_PFB_COMPLEX_INT4) != 0, S(stream));
 }
 
+int vgb_pfb_variant(int inputs_per_step)
+{
+    const int prev = pfb_variant(inputs_per_step);
+    if (prev < 0) set_error(VGB_ERR_INVALID, "pfb_variant: 0 (timed choice), 4 or 8");
+    return prev;
+}
+
 int vgb_fpfb(const vgb_voltages *v, int ncc, int nspectra, const int32_t *filter, int ntaps, int nchan,
              const int32_t *i_idx, unsigned pfb_flags, void *out, void *stream)
 {
@@ -408,6 +415,7 @@ struct vgb_pipeline {
     };
     std::vector<Graph> graphs;
     bool use_graphs = true;
+    bool front_timed = false; // the fused front end's inputs-per-step choice has been timed
 };
 
 namespace {
@@ -422,6 +430,21 @@ template <class T> int dalloc(T **p, size_t bytes)
     return VGB_SUCCESS;
 }
 
+// The voltage view of one second: history of the previous second + `volt`.
+vgb_voltages pipeline_voltages(const vgb_pipeline *p, const char2 *volt, long long cc_stride_bytes)
+{
+    vgb_voltages v{};
+    v.hist = p->d_hist[(int)(p->second & 1)];
+    v.hist_input_stride = (long long)kHistFrames * kK * 2;
+    v.hist_cc_stride = (long long)p->ninputs * kHistFrames * kK * 2;
+    v.cur = volt;
+    v.cur_block_stride = (long long)p->ninputs * kVSPVB * 2;
+    v.cur_cc_stride = cc_stride_bytes;
+    v.ninputs = p->ninputs;
+    v.nblocks = p->cfg.nblocks;
+    return v;
+}
+
 // One second of compute on s_comp with the voltages at `volt`.
 int pipeline_second(vgb_pipeline *p, const char2 *volt, long long cc_stride_bytes)
 {
@@ -430,15 +453,7 @@ int pipeline_second(vgb_pipeline *p, const char2 *volt, long long cc_stride_byte
     const int cur = (int)(p->second & 1), nxt = cur ^ 1;
     int rc;
     p->launches = 0;
-    vgb_voltages v{};
-    v.hist = p->d_hist[cur];
-    v.hist_input_stride = (long long)kHistFrames * kK * 2;
-    v.hist_cc_stride = (long long)p->ninputs * kHistFrames * kK * 2;
-    v.cur = volt;
-    v.cur_block_stride = (long long)p->ninputs * kVSPVB * 2;
-    v.cur_cc_stride = cc_stride_bytes;
-    v.ninputs = p->ninputs;
-    v.nblocks = c.nblocks;
+    const vgb_voltages v = pipeline_voltages(p, volt, cc_stride_bytes);
     const unsigned flags = c.pfb_flags | (p->fp32_wola ? VGB_WOLA_FP32 : 0u);
     auto mark = [&](int i) {
         return p->timing ? check_cuda(cudaEventRecord(p->ev_stage[i], p->s_comp), "stage event") : VGB_SUCCESS;
@@ -524,7 +539,20 @@ int pipeline_second_graph(vgb_pipeline *p, const char2 *volt, long long cc_strid
         }
     if (p->graphs.size() >= 8) drop_graphs(p);
     const long long saved = p->second;
-    int rc = check_cuda(cudaStreamBeginCapture(p->s_comp, cudaStreamCaptureModeRelaxed), "cudaStreamBeginCapture");
+    // one eager fused PFB + beamformer pass first, so the front end's
+    // inputs-per-step choice is timed (and cached) outside the capture; it
+    // writes only the Stokes and beam buffers the second then rewrites
+    int rc = VGB_SUCCESS;
+    if (!p->front_timed) {
+        const vgb_pipeline_config &c = p->cfg;
+        const vgb_voltages v = pipeline_voltages(p, volt, cc_stride_bytes);
+        rc = vgb_beamform_mwax(&v, c.ncc, p->nspectra, p->d_filter, kP, kK,
+                               c.pfb_flags | (p->fp32_wola ? VGB_WOLA_FP32 : 0u), p->d_W, c.nant, c.invw, c.nstokes,
+                               p->d_S, p->d_e, p->d_incoh, p->s_comp);
+        if (rc) return rc;
+        p->front_timed = true; // one shape per pipeline
+    }
+    rc = check_cuda(cudaStreamBeginCapture(p->s_comp, cudaStreamCaptureModeRelaxed), "cudaStreamBeginCapture");
     if (rc) return rc;
     rc = pipeline_second(p, volt, cc_stride_bytes);
     cudaGraph_t graph = nullptr;

@@ -76,6 +76,9 @@ struct IpfbArgs {
 };
 
 int launch_beam(const BeamArgs &a, int ncc, bool int32_wola, bool fpga, bool demote, cudaStream_t st);
+// Force the fused front end's inputs per step (4 or 8), or 0 for the timed
+// choice; returns the previous setting, -1 for a bad value.
+int pfb_variant(int g);
 int launch_pack(const PackArgs &a, int ncc, bool int32_wola, bool fpga, bool demote, cudaStream_t st);
 int launch_phase(const double *unit, const double *east, const double *north, const double *height,
                  const double *cable, const double *freqs, int npointing, int nant, int nchan, double href,

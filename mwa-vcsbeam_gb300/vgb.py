@@ -140,6 +140,7 @@ _SIGS = {
     "vgb_gemm_batched": (I, [V, V, V, I, I, I, I, I, V]),
     "vgb_gemm_batched_planes": (I, [V, V, V, I, I, I, I, I, V]),
     "vgb_gemm_variant": (I, [I]),
+    "vgb_pfb_variant": (I, [I]),
     "vgb_pipeline_create": (I, [ctypes.POINTER(PipelineConfig), ctypes.POINTER(V)]),
     "vgb_pipeline_destroy": (I, [V]),
     "vgb_pipeline_set_filters": (I, [V, V, V]),
@@ -248,6 +249,14 @@ def gemm_bf16(A, B, C, M, N, K, stream=None):
 def gemm_variant(v: int) -> int:
     """Force a GEMM kernel variant (0 autotuned, 128, 256, 512 persistent)."""
     prev = lib().vgb_gemm_variant(v)
+    if prev < 0:
+        raise VGBError(lib().vgb_last_error().decode())
+    return prev
+
+
+def pfb_variant(g: int) -> int:
+    """Force the fused front end's inputs per step (4 or 8; 0 = timed choice)."""
+    prev = lib().vgb_pfb_variant(g)
     if prev < 0:
         raise VGBError(lib().vgb_last_error().decode())
     return prev

@@ -84,6 +84,31 @@ def test_fused_beam_matches_oracle(vgb_mod, torch, oracle_mod, mode):
         assert rel_err(inc[0], (np.abs(v) ** 2).sum(axis=-1)) < 1e-5
 
 
+@pytest.mark.parametrize("flags_name", ["smart", "full"])
+def test_fused_beam_inputs_per_step_identical(vgb_mod, torch, oracle_mod, flags_name):
+    """The front end's two shapes (4 inputs per step in 256-thread CTAs, 8 in
+    512-thread CTAs) give identical Stokes, beam voltages and incoherent sums;
+    an odd tile count leaves the last step partly filled."""
+    nant, ns = 18, 64
+    ninputs = 2 * nant
+    htr = oracle_mod.mwax_buffer(31, 2, ninputs)
+    filt = SY.analysis_filter_int16()
+    J, phi = tables(nant)
+    W = weights_on_device(J, phi)
+    flags = (vgb_mod.PFB_SMART if flags_name == "smart" else vgb_mod.PFB_FULL_PRECISION) | vgb_mod.WOLA_FP32
+    out = {}
+    for g in (4, 8):
+        prev = vgb_mod.pfb_variant(g)
+        try:
+            out[g] = run_beam(vgb_mod, torch, htr, nant, 1, ns, filt, flags, W, 1 / 36)
+        finally:
+            vgb_mod.pfb_variant(prev)
+    for x4, x8 in zip(out[4], out[8]):
+        assert np.array_equal(x4, x8)
+    with pytest.raises(vgb_mod.VGBError):
+        vgb_mod.pfb_variant(6)
+
+
 def test_fused_beam_stokes_i_only_and_batched(vgb_mod, torch, oracle_mod):
     nant, ninputs, ns = 16, 32, 64
     a = oracle_mod.mwax_buffer(21, 2, ninputs)
