@@ -177,6 +177,7 @@ template <int kA> struct PersistSmem {
     static constexpr int kStages = kA == 2 ? 3 : kPStages;
     uint8_t a[kStages][kA][kTileBytes];
     uint8_t b[kStages][256 * 128];
+    float epi[4][32][33];                  // epilogue: each warp's 32 x 32 block, transposed for row-contiguous stores
     uint64_t full[kStages], empty[kStages];
     uint64_t tfull[2], tempty[2], drain;
     uint32_t tmem;
@@ -289,15 +290,20 @@ __global__ void __launch_bounds__(192, 1)
                 break;
             }
             tc_fence_after();
-            const int row = m * 128 + q4 * 32 + lane;
-            float *out = C + ((long long)b * M + row) * N + n * 256;
+            // this warp's 32 rows: each 32-column block goes through shared
+            // memory so that a store instruction writes 128 contiguous bytes of one row
+            float *out = C + ((long long)b * M + m * 128 + q4 * 32) * N + n * 256;
+            float(*stg)[33] = sm.epi[q4];
 #pragma unroll 1
             for (int c = 0; c < 8; c++) {
                 float v[32];
                 tmem_ld32(tmem + ((uint32_t)(q4 * 32) << 16) + buf * 256 + c * 32, v);
-                float4 *o = reinterpret_cast<float4 *>(out + c * 32);
 #pragma unroll
-                for (int j = 0; j < 8; j++) o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+                for (int j = 0; j < 32; j++) stg[lane][j] = v[j];
+                __syncwarp();
+#pragma unroll 8
+                for (int r = 0; r < 32; r++) out[(long long)r * N + c * 32 + lane] = stg[r][lane];
+                __syncwarp();
             }
             tc_fence_before();
             __syncwarp();
