@@ -1521,12 +1521,15 @@ extern "C" int vgb_multibeam_run_host(vgb_multibeam *mb, const void *v_host, uin
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const uint8_t *vin = static_cast<const uint8_t *>(v_host);
-    // the caller's earlier work on st comes first
-    rc = check_cuda(cudaEventRecord(mb->ev_comp[1], st), "cudaEventRecord");
-    if (!rc) rc = check_cuda(cudaStreamWaitEvent(mb->s_h2d, mb->ev_comp[1], 0), "cudaStreamWaitEvent");
+    // the first two channels in as soon as each slot's last reader (the
+    // previous call's compute on it) is done, so consecutive calls overlap;
+    // on the first call the slot events have not been recorded and do not wait
     for (int cc = 0; cc < 2 && cc < c.ncc && !rc; cc++) {
-        rc = check_cuda(cudaMemcpyAsync(mb->d_vin[cc], vin + cc * vbytes, vbytes, cudaMemcpyHostToDevice, mb->s_h2d),
-                        "cudaMemcpyAsync(H2D)");
+        rc = check_cuda(cudaStreamWaitEvent(mb->s_h2d, mb->ev_comp[cc], 0), "cudaStreamWaitEvent");
+        if (!rc)
+            rc = check_cuda(cudaMemcpyAsync(mb->d_vin[cc], vin + cc * vbytes, vbytes, cudaMemcpyHostToDevice,
+                                            mb->s_h2d),
+                            "cudaMemcpyAsync(H2D)");
         if (!rc) rc = check_cuda(cudaEventRecord(mb->ev_h2d[cc], mb->s_h2d), "cudaEventRecord");
     }
     mb->last_launches = 0;
