@@ -138,6 +138,8 @@ struct SurBatch {
     int ndir, nfreq, nsets;
     const float *Y;                // [set][freq][dir][8]
     uint64_t seed;
+    const uint64_t *seed_dev;      // training: seed of step kdev[0] (graph replay), or NULL
+    const int *kdev;
     const float *feat_in;          // [B][4] given raw features (sin, cos, za, f scaled) or NULL
     const int *set_in;             // [B]
     const float *y_in;             // [B][8]
@@ -163,7 +165,8 @@ __global__ void sur_batch_kernel(const SurBatch a)
         for (int k = 0; k < 8; k++) a.y[8 * i + k] = a.y_in[8 * i + k];
     } else {
         const long long n = (long long)a.nsets * a.nfreq * a.ndir;
-        const long long idx = (long long)(sur_hash(a.seed * 0x9E3779B1ull + i) % (uint64_t)n);
+        const uint64_t seed = a.seed_dev ? a.seed_dev[*a.kdev] : a.seed;
+        const long long idx = (long long)(sur_hash(seed * 0x9E3779B1ull + i) % (uint64_t)n);
         const int d = idx % a.ndir, fi = (idx / a.ndir) % a.nfreq;
         s = idx / ((long long)a.ndir * a.nfreq);
         sur_features(a.az[d], a.za[d], a.freq[fi], a.params + a.L.emb + 2 * s, x);
@@ -191,7 +194,7 @@ __global__ void sur_act_kernel(const float *C, const float *b, int B, float *pre
 
 // outputs, loss and dL/dout = 2 (pred - y) / (8 B) as hi | lo (128 columns each)
 __global__ void sur_out_kernel(const float *C4, const float *b4, const float *y, int B, float *pred, uint16_t *dY,
-                               float *loss, float *db4)
+                               float *loss, float *db4, const int *kslot = nullptr)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float l = 0.f;
@@ -212,7 +215,7 @@ __global__ void sur_out_kernel(const float *C4, const float *b4, const float *y,
     }
     if (loss) {
         for (int o = 16; o; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
-        if ((threadIdx.x & 31) == 0) atomicAdd(loss, l / (8.f * B));
+        if ((threadIdx.x & 31) == 0) atomicAdd(kslot ? loss + *kslot : loss, l / (8.f * B));
     }
 }
 
@@ -261,6 +264,8 @@ struct SurAdamArgs {
     float *db, *demb;
     int nslice;
     float lr, b1, b2, eps, bc1, bc2;
+    const float *sched;   // training: [step][3] (lr, bc1, bc2) of step kdev[0] (graph replay), or NULL
+    const int *kdev;
     int update;
     uint16_t *W0p, *W1, *W2, *W3, *W4p, *W0t, *W1t, *W2t, *W3t, *W4t;
 };
@@ -295,11 +300,18 @@ __global__ void sur_adam_kernel(const SurAdamArgs a)
     if (a.grad_out) a.grad_out[i] = g;
     float p = a.p[i];
     if (a.update) {
+        float lr = a.lr, bc1 = a.bc1, bc2 = a.bc2;
+        if (a.sched) {
+            const float *sc = a.sched + 3 * (*a.kdev);
+            lr = sc[0];
+            bc1 = sc[1];
+            bc2 = sc[2];
+        }
         const float m = a.b1 * a.m[i] + (1.f - a.b1) * g;
         const float v = a.b2 * a.v[i] + (1.f - a.b2) * g * g;
         a.m[i] = m;
         a.v[i] = v;
-        p -= a.lr * (m / a.bc1) / (sqrtf(v / a.bc2) + a.eps);
+        p -= lr * (m / bc1) / (sqrtf(v / bc2) + a.eps);
         a.p[i] = p;
     }
     const uint16_t w = bfbits(p);
@@ -312,6 +324,9 @@ __global__ void sur_adam_kernel(const SurAdamArgs a)
     default: break;
     }
 }
+
+// The training step index of a graph-replayed step, advanced once per step.
+__global__ void sur_next_step_kernel(int *kdev) { *kdev += 1; }
 
 // ---------------------------------------------------------------------------
 // validation and inference
@@ -474,6 +489,12 @@ struct vgb_surrogate {
     long long step = 0;
     float *Jsur = nullptr;
     double2 *Bsur = nullptr;
+    // training schedule for graph replay: [step][3] (lr, bc1, bc2), [step] seeds,
+    // per-step losses, and the device step index
+    float *sched = nullptr, *loss_dev = nullptr;
+    uint64_t *seed_dev = nullptr;
+    int *kdev = nullptr;
+    long long sched_cap = 0;
     long long Jsur_cap = 0;
     int *set_map = nullptr; // queries: [nsets] evaluated sets in row order, then [nsets] slot of each set
 };
@@ -549,9 +570,13 @@ int sur_backward(vgb_surrogate *s)
     return VGB_SUCCESS;
 }
 
-int sur_adam(vgb_surrogate *s, int update, float lr, float *grad_out)
+int sur_adam(vgb_surrogate *s, int update, float lr, float *grad_out, bool scheduled = false)
 {
     SurAdamArgs a{};
+    if (scheduled) {
+        a.sched = s->sched;
+        a.kdev = s->kdev;
+    }
     a.L = s->L;
     a.p = s->p;
     a.m = s->m;
@@ -678,7 +703,8 @@ extern "C" void vgb_surrogate_destroy(vgb_surrogate *s)
     if (s->st) cudaStreamSynchronize(s->st);
     for (void *p : s->allocs) cudaFree(p);
     for (void *p : {(void *)s->tab_az, (void *)s->tab_za, (void *)s->tab_f, (void *)s->tab_Y, (void *)s->tab_delays,
-                    (void *)s->Jsur, (void *)s->Bsur})
+                    (void *)s->Jsur, (void *)s->Bsur, (void *)s->sched, (void *)s->loss_dev, (void *)s->seed_dev,
+                    (void *)s->kdev})
         if (p) cudaFree(p);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
@@ -749,44 +775,104 @@ extern "C" int vgb_surrogate_set_training(vgb_surrogate *s, const uint32_t *dela
     return check_cuda(cudaStreamSynchronize(s->st), "cudaStreamSynchronize");
 }
 
+// One training step on s->st with its schedule (seed, learning rate, Adam bias
+// corrections) read on the device at index kdev[0], its loss accumulated into
+// loss_dev[kdev[0]], and kdev advanced: the same launches every step, so the
+// step is captured once and replayed.
+static int sur_train_step(vgb_surrogate *s)
+{
+    SurBatch b{};
+    b.az = s->tab_az;
+    b.za = s->tab_za;
+    b.freq = s->tab_f;
+    b.ndir = s->ndir;
+    b.nfreq = s->nfreq;
+    b.nsets = s->nsets;
+    b.Y = s->tab_Y;
+    b.seed_dev = s->seed_dev;
+    b.kdev = s->kdev;
+    b.params = s->p;
+    b.L = s->L;
+    b.B = s->B;
+    b.X0 = s->X0;
+    b.set_of = s->set_of;
+    b.y = s->y;
+    sur_batch_kernel<<<(s->B + 255) / 256, 256, 0, s->st>>>(b);
+    int rc = check_launch("sur_batch_kernel");
+    if (!rc) rc = sur_forward(s);
+    if (!rc) {
+        sur_out_kernel<<<(s->B + 255) / 256, 256, 0, s->st>>>(s->C4, s->p + s->L.b4, s->y, s->B, nullptr, s->dY,
+                                                              s->loss_dev, s->db + 4 * kSurH, s->kdev);
+        rc = check_launch("sur_out_kernel");
+    }
+    if (!rc) rc = sur_backward(s);
+    if (!rc) rc = sur_adam(s, 1, 0.f, nullptr, true);
+    if (!rc) {
+        sur_next_step_kernel<<<1, 1, 0, s->st>>>(s->kdev);
+        rc = check_launch("sur_next_step_kernel");
+    }
+    return rc;
+}
+
 extern "C" int vgb_surrogate_train(vgb_surrogate *s, int steps, float lr_max, float lr_min, float *loss_host)
 {
     if (!s || steps < 0) return set_error(VGB_ERR_INVALID, "surrogate_train: bad arguments");
     if (!s->tab_Y) return set_error(VGB_ERR_STATE, "surrogate_train: set_training first");
+    if (steps == 0) return VGB_SUCCESS;
     int rc = VGB_SUCCESS;
-    for (int k = 0; k < steps && !rc; k++) {
-        const float lr = lr_min + 0.5f * (lr_max - lr_min) * (1.f + cosf(3.14159265f * k / (float)steps));
-        SurBatch b{};
-        b.az = s->tab_az;
-        b.za = s->tab_za;
-        b.freq = s->tab_f;
-        b.ndir = s->ndir;
-        b.nfreq = s->nfreq;
-        b.nsets = s->nsets;
-        b.Y = s->tab_Y;
-        b.seed = (uint64_t)s->step * 0x632BE59BD9B4E019ull + 7;
-        b.params = s->p;
-        b.L = s->L;
-        b.B = s->B;
-        b.X0 = s->X0;
-        b.set_of = s->set_of;
-        b.y = s->y;
-        sur_batch_kernel<<<(s->B + 255) / 256, 256, 0, s->st>>>(b);
-        if ((rc = check_launch("sur_batch_kernel"))) break;
-        const bool want_loss = loss_host != nullptr;
-        if (want_loss && (rc = check_cuda(cudaMemsetAsync(s->loss, 0, sizeof(float), s->st), "cudaMemsetAsync")))
-            break;
-        if ((rc = sur_forward(s))) break;
-        sur_out_kernel<<<(s->B + 255) / 256, 256, 0, s->st>>>(s->C4, s->p + s->L.b4, s->y, s->B, nullptr, s->dY,
-                                                              want_loss ? s->loss : nullptr, s->db + 4 * kSurH);
-        if ((rc = check_launch("sur_out_kernel"))) break;
-        if ((rc = sur_backward(s))) break;
-        if ((rc = sur_adam(s, 1, lr, nullptr))) break;
-        s->step++;
-        if (want_loss)
-            rc = check_cuda(cudaMemcpyAsync(loss_host + k, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->st),
-                            "cudaMemcpyAsync");
+    // the schedule on the host: cosine learning rate, Adam bias corrections, batch seeds
+    if (steps > s->sched_cap) {
+        for (void *p : {(void *)s->sched, (void *)s->loss_dev, (void *)s->seed_dev})
+            if (p) cudaFree(p);
+        s->sched = s->loss_dev = nullptr;
+        s->seed_dev = nullptr;
+        s->sched_cap = 0;
+        rc = check_cuda(cudaMalloc(&s->sched, sizeof(float) * 3 * steps), "cudaMalloc(schedule)");
+        if (!rc) rc = check_cuda(cudaMalloc(&s->loss_dev, sizeof(float) * steps), "cudaMalloc(losses)");
+        if (!rc) rc = check_cuda(cudaMalloc(&s->seed_dev, sizeof(uint64_t) * steps), "cudaMalloc(seeds)");
+        if (!rc && !s->kdev) rc = check_cuda(cudaMalloc(&s->kdev, sizeof(int)), "cudaMalloc(step index)");
+        if (rc) return rc;
+        s->sched_cap = steps;
     }
+    std::vector<float> sched(3 * (size_t)steps);
+    std::vector<uint64_t> seeds(steps);
+    for (int k = 0; k < steps; k++) {
+        const double t = (double)(s->step + k + 1);
+        sched[3 * k] = lr_min + 0.5f * (lr_max - lr_min) * (1.f + cosf(3.14159265f * k / (float)steps));
+        sched[3 * k + 1] = (float)(1.0 - pow(0.9, t));
+        sched[3 * k + 2] = (float)(1.0 - pow(0.999, t));
+        seeds[k] = (uint64_t)(s->step + k) * 0x632BE59BD9B4E019ull + 7;
+    }
+    rc = check_cuda(cudaMemcpyAsync(s->sched, sched.data(), sizeof(float) * sched.size(), cudaMemcpyHostToDevice,
+                                    s->st),
+                    "cudaMemcpyAsync(schedule)");
+    if (!rc)
+        rc = check_cuda(cudaMemcpyAsync(s->seed_dev, seeds.data(), sizeof(uint64_t) * steps, cudaMemcpyHostToDevice,
+                                        s->st),
+                        "cudaMemcpyAsync(seeds)");
+    if (!rc) rc = check_cuda(cudaMemsetAsync(s->loss_dev, 0, sizeof(float) * steps, s->st), "cudaMemsetAsync");
+    if (!rc) rc = check_cuda(cudaMemsetAsync(s->kdev, 0, sizeof(int), s->st), "cudaMemsetAsync");
+    // the first step eagerly (the GEMM shapes get their tuned variants), then one
+    // captured step replayed for the rest
+    if (!rc) rc = sur_train_step(s);
+    if (!rc && steps > 1) {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        rc = check_cuda(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeRelaxed), "cudaStreamBeginCapture");
+        if (!rc) {
+            const int rs = sur_train_step(s);
+            const int re = check_cuda(cudaStreamEndCapture(s->st, &graph), "cudaStreamEndCapture");
+            rc = rs ? rs : re;
+        }
+        if (!rc) rc = check_cuda(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+        for (int k = 1; k < steps && !rc; k++) rc = check_cuda(cudaGraphLaunch(exec, s->st), "cudaGraphLaunch");
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+    if (!rc) s->step += steps;
+    if (!rc && loss_host)
+        rc = check_cuda(cudaMemcpyAsync(loss_host, s->loss_dev, sizeof(float) * steps, cudaMemcpyDeviceToHost, s->st),
+                        "cudaMemcpyAsync(losses)");
     s->validated = false;
     if (!rc) rc = check_cuda(cudaStreamSynchronize(s->st), "cudaStreamSynchronize");
     return rc;
