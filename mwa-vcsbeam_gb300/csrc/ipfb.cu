@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(256) ipfb_kernel(const IpfbArgs a)
             for (int h = 0; h < 2; h++)
 #pragma unroll
                 for (int k2 = 0; k2 < 8; k2++) {
-                    const int r = 2 * j + h + 16 * k2;
+                    const int r = fft128_index(j, h, k2);
                     const float2 v = out[h][k2];
                     row[r] = (r & 1) ? make_float2(-v.x, -v.y) : v;
                 }
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(256) fft_staged_kernel(float2 *rows, long long
 #pragma unroll
         for (int h = 0; h < 2; h++)
 #pragma unroll
-            for (int k2 = 0; k2 < 8; k2++) rows[(r0 + g) * kK + 2 * j + h + 16 * k2] = out[h][k2];
+            for (int k2 = 0; k2 < 8; k2++) rows[(r0 + g) * kK + fft128_index(j, h, k2)] = out[h][k2];
     }
 }
 

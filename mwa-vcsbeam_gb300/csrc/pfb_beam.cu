@@ -4,9 +4,10 @@
 // One CTA (256 threads, ~93 KB of shared memory, two CTAs per SM) owns a
 // tile of T = 8 consecutive fine spectra of one coarse channel and walks the
 // RF inputs four at a time (two tiles x two pols). Per step:
-//   1. the TMA unit copies the 19 voltage frames (T + 11) each input needs,
-//      and the two tiles' weight rows, into shared memory (1-D bulk copies,
-//      double-buffered with mbarriers: step i+1 lands while step i computes);
+//   1. the TMA unit copies the 19 voltage frames (T + 11) each input needs
+//      (1-D bulk copies) and the two tiles' weights (a 5-D tensor map that
+//      splits the two Jones rows apart) into shared memory, double-buffered
+//      with mbarriers: step i+1 lands while step i computes;
 //   2. weighted overlap-add, exactly (pfb.cpp:121-179): one thread per
 //      (input, pair of adjacent samples), the pair's 12 taps in registers,
 //      packed FP32x2 FMAs (or int32 when FP32 would not be exact);
@@ -24,6 +25,7 @@
 #include <mutex>
 #include <tuple>
 
+#include "tcgen05.cuh"
 #include "vgb_launch.cuh"
 
 namespace vgb {
@@ -38,7 +40,7 @@ constexpr int kFrameBytes = kK * 2;        // 256
 // 64 threads per input: 95 KB for G = 4 (two CTAs per SM), 188 KB for G = 8.
 template <int G> struct FrontSmemT {
     char2 stage[2][G][kWin][kK];           // TMA destinations: frames
-    float4 wst[2][G / 2][kK][2];           // TMA destinations: weights of the step's tiles
+    float4 wst[2][2][G / 2][kK];           // TMA destinations: weights [row][tile][k'] of the step's tiles
     float2 buf[G * kT][kFftRow];           // WOLA output -> FFT (in place) -> voltages
     float2 tw[128];                        // W128 twiddles, [k1][j]
     uint64_t bar[2];
@@ -79,12 +81,13 @@ __device__ __forceinline__ uint32_t issue_frames(const VoltView &vv, int cc, int
     return bytes;
 }
 
-// Producer: warp 0 queues step `it`'s frames (and, when W is given, the
-// weight rows of its two tiles) into stage it & 1, one input per lane (lane
-// kG the weights), so the copy set-up costs the warp about one input's worth.
+// Producer: warp 0 queues step `it`'s frames (and, when a weight map is
+// given, the two Jones rows of its G/2 tiles, tiles past the last one
+// zero-filled) into stage it & 1, one input per lane (lane G the weights), so
+// the copy set-up costs the warp about one input's worth.
 template <int G>
 __device__ __forceinline__ void produce(FrontSmemT<G> &sm, const VoltView &vv, int cc, int it, int m0, int nspectra,
-                                       const float4 *Wcc, int nant, unsigned *status)
+                                       const CUtensorMap *wmap, unsigned *status)
 {
     const int lane = threadIdx.x & 31;
     const int s = it & 1;
@@ -92,20 +95,18 @@ __device__ __forceinline__ void produce(FrontSmemT<G> &sm, const VoltView &vv, i
     uint32_t total = 0;
     for (int li = 0; li < G; li++)
         if (it * G + li < vv.ninputs) total += (w_end - m0) * kFrameBytes;
-    int nw = 0;
-    if (Wcc) {
-        nw = min(G / 2, nant - (G / 2) * it);
-        total += nw * kK * 32;
-    }
+    constexpr uint32_t kWBytes = (G / 2) * kK * 16;   // one Jones row of G/2 tiles
+    if (wmap) total += 2 * kWBytes;
     if (lane == 0) mbar_arrive_expect_tx(&sm.bar[s], total);
     __syncwarp();
     uint32_t issued = 0;
     if (lane < G) {
         const int i = it * G + lane;
         if (i < vv.ninputs) issued = issue_frames(vv, cc, i, m0, w_end, sm.stage[s][lane][0], &sm.bar[s], status);
-    } else if (lane == G && nw > 0) {
-        bulk_g2s(sm.wst[s][0][0], Wcc + (long long)((G / 2) * it) * kK * 2, nw * kK * 32, &sm.bar[s]);
-        issued = nw * kK * 32;
+    } else if (lane == G && wmap) {
+        tma_load_5d(sm.wst[s][0][0], wmap, 0, 0, 0, (G / 2) * it, cc, &sm.bar[s]);
+        tma_load_5d(sm.wst[s][1][0], wmap, 0, 1, 0, (G / 2) * it, cc, &sm.bar[s]);
+        issued = 2 * kWBytes;
     }
     // lanes 0..G issue copies: a butterfly over the lowest 8 (G = 4) or 16 lanes
 #pragma unroll
@@ -253,7 +254,7 @@ __device__ __forceinline__ void fft_step(FrontSmemT<G> &sm, int tid)
     for (int h = 0; h < 2; h++)
 #pragma unroll
         for (int k2 = 0; k2 < 8; k2++) {
-            const int k = 2 * j + h + 16 * k2;
+            const int k = fft128_index(j, h, k2);
             const int kp = (k + kK / 2) & (kK - 1);
             const float2 X = out[h][k2];
             float vr = kScale ? X.y * (1.0f / kK) : X.y, vi = kScale ? X.x * (1.0f / kK) : X.x;
@@ -323,7 +324,8 @@ template <int G> __device__ __forceinline__ void drain(FrontSmemT<G> &sm, int it
 // input). Every (k', m) is summed by one thread over the tiles in the same
 // order either way, so both give identical results; the host picks by timing.
 template <bool kInt32, bool kFpga, bool kDemote, int G>
-__global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1) beam_kernel(const BeamArgs a)
+__global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1)
+    beam_kernel(const BeamArgs a, const __grid_constant__ CUtensorMap wmap)
 {
     constexpr int kTiles = G / 2;        // tiles per step
     constexpr int kMh = G / 2;           // threads per k' (spectra m = mh + kMh mi)
@@ -334,14 +336,14 @@ __global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1) beam_kernel(const Beam
     const int cc = blockIdx.y;
     const int m0 = blockIdx.x * kT;
     const int nsteps = (a.vv.ninputs + G - 1) / G;
-    const float4 *Wcc = a.W + cc * a.W_cc;
 
+    if (tid == 0) prefetch_tmap(&wmap);
     init_front(sm, tid);
     int hc[2][kP];
     const int li = tid >> 6, n0 = 2 * (tid & 63);
     load_taps(a.filter, n0, hc);
     __syncthreads();
-    if (tid < 32) produce(sm, a.vv, cc, 0, m0, a.nspectra, Wcc, a.nant, a.status);
+    if (tid < 32) produce(sm, a.vv, cc, 0, m0, a.nspectra, &wmap, a.status);
 
     // beam accumulators for (k', m = mh + kMh mi)
     const int kp = tid & (kK - 1), mh = tid >> 7;
@@ -357,7 +359,7 @@ __global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1) beam_kernel(const Beam
             return;
         }
         // everyone has finished step it-1, so its buffers may be refilled
-        if (tid < 32 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, Wcc, a.nant, a.status);
+        if (tid < 32 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, &wmap, a.status);
         wola_step<kInt32, kFpga>(sm, it & 1, li, n0, hc);
         input_barrier(li);
         fft_step<kDemote, kFpga>(sm, tid);
@@ -366,8 +368,8 @@ __global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1) beam_kernel(const Beam
         for (int aa = 0; aa < kTiles; aa++) {
             const int ant = it * kTiles + aa;
             if (ant >= a.nant) break;
-            const float4 wa = sm.wst[it & 1][aa][kp][0];
-            const float4 wb = sm.wst[it & 1][aa][kp][1];
+            const float4 wa = sm.wst[it & 1][0][aa][kp];
+            const float4 wb = sm.wst[it & 1][1][aa][kp];
 #pragma unroll
             for (int mi = 0; mi < kMi; mi++) {
                 const int m = mh + kMh * mi;
@@ -432,7 +434,7 @@ __global__ void __launch_bounds__(kThreads, 2) pack_kernel(const PackArgs a)
     const int li = tid >> 6, n0 = 2 * (tid & 63);
     load_taps(a.filter, n0, hc);
     __syncthreads();
-    if (tid < 32) produce(sm, a.vv, cc, 0, m0, a.nspectra, nullptr, 0, a.status);
+    if (tid < 32) produce(sm, a.vv, cc, 0, m0, a.nspectra, nullptr, a.status);
 
     const bool int4 = (a.flags & VGB_PFB_COMPLEX_INT4) != 0;
     const bool imag_first = (a.flags & VGB_PFB_IMAG_PART_FIRST) != 0;
@@ -442,7 +444,7 @@ __global__ void __launch_bounds__(kThreads, 2) pack_kernel(const PackArgs a)
             drain(sm, it);
             return;
         }
-        if (tid < 32 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, nullptr, 0, a.status);
+        if (tid < 32 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, nullptr, a.status);
         wola_step<kInt32, kFpga>(sm, it & 1, li, n0, hc);
         input_barrier(li);
         fft_step<kDemote, kFpga>(sm, tid);
@@ -506,14 +508,15 @@ static int g_pfb_variant = 0; // 0: autotuned; else forced inputs per step (4 or
 template <bool A, bool B, bool C> struct BeamSel {
     static int run_g(const BeamArgs &a, dim3 grid, cudaStream_t st, int g)
     {
+        CUtensorMap wmap;
+        int rc = make_tmap_beam_weights(&wmap, a.W, a.nant, (int)grid.y, a.W_cc, g / 2);
+        if (rc) return rc;
         if (g == 8) {
-            int rc = prep<8>(beam_kernel<A, B, C, 8>);
-            if (rc) return rc;
-            beam_kernel<A, B, C, 8><<<grid, 512, front_smem<8>(), st>>>(a);
+            if ((rc = prep<8>(beam_kernel<A, B, C, 8>))) return rc;
+            beam_kernel<A, B, C, 8><<<grid, 512, front_smem<8>(), st>>>(a, wmap);
         } else {
-            int rc = prep<4>(beam_kernel<A, B, C, 4>);
-            if (rc) return rc;
-            beam_kernel<A, B, C, 4><<<grid, 256, front_smem<4>(), st>>>(a);
+            if ((rc = prep<4>(beam_kernel<A, B, C, 4>))) return rc;
+            beam_kernel<A, B, C, 4><<<grid, 256, front_smem<4>(), st>>>(a, wmap);
         }
         return check_launch("beam_kernel");
     }

@@ -68,6 +68,25 @@ int make_tmap_bf16(CUtensorMap *map, const void *base, uint64_t rows, uint64_t c
     return VGB_SUCCESS;
 }
 
+int make_tmap_beam_weights(CUtensorMap *map, const void *W, int nant, int ncc, long long W_cc, int tiles_per_box)
+{
+    auto fn = encode_fn();
+    if (!fn) return set_error(VGB_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    if ((reinterpret_cast<uintptr_t>(W) & 15) || nant <= 0 || ncc <= 0 || W_cc < (long long)nant * kK * 2 ||
+        tiles_per_box <= 0 || tiles_per_box > 256)
+        return set_error(VGB_ERR_INVALID, "weight tensor map: bad base, sizes or stride");
+    // [cc][ant][k][row][4 floats], innermost first
+    cuuint64_t dims[5] = {4, 2, (cuuint64_t)kK, (cuuint64_t)nant, (cuuint64_t)ncc};
+    cuuint64_t strides[4] = {16, 32, (cuuint64_t)kK * 32, (cuuint64_t)W_cc * 16};
+    cuuint32_t box[5] = {4, 1, (cuuint32_t)kK, (cuuint32_t)tiles_per_box, 1};
+    cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, const_cast<void *>(W), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(VGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return VGB_SUCCESS;
+}
+
 template <bool kF16, int BN>
 __global__ void __launch_bounds__(128, 1)
     gemm_bf16_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, float *C,

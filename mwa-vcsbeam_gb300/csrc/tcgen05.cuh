@@ -125,6 +125,17 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
         : "memory");
 }
 
+// 5-D tiled load, coordinates innermost first (elements); used for the
+// beamformer's weight rows, whose innermost coordinate is always 0.
+__device__ __forceinline__ void tma_load_5d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, int c3, int c4,
+                                            uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+                 "%5, %6}], [%7];" ::"r"(smem_u32(dst)),
+                 "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_u32(bar))
+                 : "memory");
+}
+
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap *map)
 {
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
@@ -136,5 +147,12 @@ __device__ __forceinline__ void prefetch_tmap(const CUtensorMap *map)
 // run time so the library loads without a driver).
 int make_tmap_bf16(CUtensorMap *map, const void *base, uint64_t rows, uint64_t cols, uint64_t row_bytes,
                    uint32_t box_rows, bool fp16 = false);
+
+// Host: 5-D tensor map over the beamformer weights W[cc][ant][k][row]
+// (row 0 = (w00, w01), row 1 = (w10, w11), 16 bytes each; `W_cc` float4
+// between coarse channels) whose box {4 floats, 1 row, K, tiles_per_box, 1}
+// lands as [tile][k] float4 of one row: loading rows 0 and 1 separately
+// de-interleaves them, so a warp's reads of one row are contiguous.
+int make_tmap_beam_weights(CUtensorMap *map, const void *W, int nant, int ncc, long long W_cc, int tiles_per_box);
 
 } // namespace vgb

@@ -322,18 +322,24 @@ __device__ __forceinline__ void fft128_pass1(float2 *row, const float2 *tw, int 
     for (int k1 = 0; k1 < 16; k1++) row[k1 * 9 + j] = x[k1];
 }
 
-// Pass 2: thread t of the group produces X[k1 + 16 k2] for k1 = 2t, 2t+1 and
-// all k2, into `out[2][8]` (out[h][k2] for k1 = 2t + h).
+// Pass 2: thread t of the group produces X[k1 + 16 k2] for k1 = t, t + 8 and
+// all k2, into `out[2][8]` (out[h][k2] for k1 = t + 8h, output index
+// fft128_index(t, h, k2)). The 8 threads of a row read at a stride of 9
+// float2, which with rows 64 bytes apart modulo 128 (kFftRow) puts a warp's
+// four rows on complementary banks: two wavefronts per read, as in pass 1.
 template <int SIGN>
 __device__ __forceinline__ void fft128_pass2(const float2 *row, int t, float2 (&out)[2][8])
 {
 #pragma unroll
     for (int h = 0; h < 2; h++) {
-        const int k1 = 2 * t + h;
+        const int k1 = t + 8 * h;
 #pragma unroll
         for (int j = 0; j < 8; j++) out[h][j] = row[k1 * 9 + j];
         dft8<SIGN>(out[h]);
     }
 }
+
+// Frequency index of pass 2's out[h][k2] in thread t.
+__device__ __forceinline__ int fft128_index(int t, int h, int k2) { return t + 8 * h + 16 * k2; }
 
 } // namespace vgb
