@@ -204,12 +204,50 @@ int vgb_renormalise(const float *S, int ncc, int npointing, int nstep, int nstok
  *   coeffs  12*128 float synthesis taps, already scaled (vmScaleFilterCoeffs)
  *   out_f   [job][nsamples*128][2][2] float (data_buffer_vdif layout), or NULL
  *   vdif    [job][nsamples][544] bytes: 32-byte header + 512 payload, or NULL
- *   hdr     [job][8] uint32 header of the second's first frame (words other
- *           than the frame number are copied), or NULL for zeros
+ *   hdr     [job][8] uint32 DEVICE header template, or NULL for zeros;
+ *           frame f carries it advanced by frame_offset + f frames (see the
+ *           VDIF header functions below); frame_offset >= 0
  */
 int vgb_ipfb(const void *e, long long e_job_stride, const void *hist, long long hist_job_stride,
              const float *coeffs, int ntaps, int nchan, int nsamples, int njobs, float *out_f, uint8_t *vdif,
              const uint32_t *hdr, int frame_offset, void *stream);
+
+/*
+ * VDIF frame headers (8 uint32 words, VDIF 1.0 layout; host memory unless
+ * noted). Frame f of a vgb_ipfb call carries the template hdr advanced by
+ * frame_offset + f frames at 10000 frames per second, the MWA fine sample
+ * rate (nextVDIFHeader applied f times, beam_vdif.c:80): the frame number
+ * rolls over to 0 and the seconds field steps on at each whole second.
+ *
+ * vgb_vdif_header_create     createVDIFHeader (beam_vdif.c:201-202): zero the
+ *                            header, set frame length ((bytes + 32) / 8),
+ *                            log2(nchan), bits - 1, complex flag, thread id
+ *                            and the two-character station id
+ * vgb_vdif_header_set_epoch_mjd  setVDIFEpochMJD (beam_vdif.c:209): reference
+ *                            epoch = half-years from 2000 to the MJD's date
+ * vgb_vdif_header_epoch_mjd  MJD of the header's reference epoch
+ * vgb_vdif_header_set_mjdsec setVDIFFrameMJDSec (beam_vdif.c:210): seconds
+ *                            since the reference epoch from MJD x 86400 + s
+ * vgb_vdif_header_set_frame  setVDIFFrameNumber (beam_vdif.c:211)
+ * vgb_vdif_header_next       nextVDIFHeader (beam_vdif.c:80)
+ * vgb_vdif_populate_header   the header part of vmPopulateVDIFHeader
+ *                            (beam_vdif.c:178-211): 8-bit complex, 2
+ *                            channels (one per pol), 512 data bytes, epoch
+ *                            and seconds of intmjd + roundf(fracmjd x 86400),
+ *                            frame 0; stationid NULL = "mw"
+ * vgb_vdif_advance           DEVICE templates d_hdr [njobs][8]: advance each
+ *                            by nframes frames (the second-to-second step
+ *                            the pipeline takes after every second)
+ */
+int vgb_vdif_header_create(uint32_t *hdr, int dataarraylength, int threadid, int bits, int nchan, int iscomplex,
+                           const char *stationid);
+int vgb_vdif_header_set_epoch_mjd(uint32_t *hdr, int mjd);
+int vgb_vdif_header_epoch_mjd(const uint32_t *hdr, int *mjd);
+int vgb_vdif_header_set_mjdsec(uint32_t *hdr, long long mjdsec);
+int vgb_vdif_header_set_frame(uint32_t *hdr, int frame);
+int vgb_vdif_header_next(uint32_t *hdr, int frames_per_second);
+int vgb_vdif_populate_header(uint32_t *hdr, int intmjd, double fracmjd, int threadid, const char *stationid);
+int vgb_vdif_advance(uint32_t *d_hdr, int njobs, int nframes, void *stream);
 
 /*
  * MWAX voltages to 8-bit PSRFITS bytes without allocating any memory. This
@@ -468,7 +506,11 @@ int vgb_pipeline_destroy(vgb_pipeline *p);
 int vgb_pipeline_set_filters(vgb_pipeline *p, const int32_t *analysis, const float *synthesis);
 /* W [ncc][nant][128][2][2] complex float on the host or device. */
 int vgb_pipeline_set_weights(vgb_pipeline *p, const void *W, int on_device);
-/* VDIF header template of frame 0, [ncc][8] uint32 on the host (optional). */
+/* VDIF header template of the next second's first frame, [ncc][8] uint32 on
+ * the host (optional; zeros by default). After every second the pipeline
+ * advances the templates by that second's frames (vgb_vdif_advance), so the
+ * headers run on across seconds as nextVDIFHeader's do (beam_vdif.c:80); the
+ * templates are part of the saved state. */
 int vgb_pipeline_set_vdif_header(vgb_pipeline *p, const uint32_t *hdr);
 /* Process one second whose voltages are already on the device, laid out
  * [cc][block][input][sample] char2 (cc stride cur_cc_stride bytes). The

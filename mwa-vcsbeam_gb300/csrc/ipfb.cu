@@ -23,6 +23,16 @@
 
 namespace vgb {
 
+// The seconds / frame words of the header template (w0, w1) advanced by n
+// frames at kVdifFramesPerSecond (nextVDIFHeader applied n times,
+// beam_vdif.c:80): word `which` (0 or 1) of the result.
+__device__ __forceinline__ uint32_t vdif_advanced_word(uint32_t w0, uint32_t w1, long long n, int which)
+{
+    const long long total = (long long)(w1 & 0xFFFFFFu) + n;
+    if (which == 0) return (w0 & 0xC0000000u) | ((w0 + (uint32_t)(total / kVdifFramesPerSecond)) & 0x3FFFFFFFu);
+    return (w1 & 0xFF000000u) | (uint32_t)(total % kVdifFramesPerSecond);
+}
+
 constexpr int kIFT = 32;                 // frames per CTA
 
 constexpr int kIRowsPad = 96;            // padded to whole warps of groups
@@ -142,7 +152,11 @@ __global__ void __launch_bounds__(256) ipfb_kernel(const IpfbArgs a)
                 reinterpret_cast<uint16_t *>(frame + 32)[r * 2 + pol] = (uint16_t)(br | (bi << 8));
                 if (tid < 8) {
                     uint32_t wv = a.hdr ? __ldg(a.hdr + job * 8 + tid) : 0u;
-                    if (tid == 1) wv = (wv & 0xFF000000u) | ((uint32_t)(f + a.frame_offset) & 0x00FFFFFFu);
+                    if (tid < 2) {
+                        const uint32_t w0 = a.hdr ? __ldg(a.hdr + job * 8) : 0u;
+                        const uint32_t w1 = a.hdr ? __ldg(a.hdr + job * 8 + 1) : 0u;
+                        wv = vdif_advanced_word(w0, w1, (long long)a.frame_offset + f, tid);
+                    }
                     reinterpret_cast<uint32_t *>(frame)[tid] = wv;
                 }
             }
@@ -160,6 +174,24 @@ int launch_ipfb(const IpfbArgs &a, int njobs, cudaStream_t st)
     dim3 grid((a.nsamples + kIFT - 1) / kIFT, njobs);
     ipfb_kernel<<<grid, 256, smem, st>>>(a);
     return check_launch("ipfb_kernel");
+}
+
+// Advance each job's header template [job][8] by n frames.
+__global__ void vdif_advance_kernel(uint32_t *hdr, int njobs, int n)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= njobs) return;
+    uint32_t *h = hdr + j * 8;
+    const uint32_t w0 = h[0], w1 = h[1];
+    h[0] = vdif_advanced_word(w0, w1, n, 0);
+    h[1] = vdif_advanced_word(w0, w1, n, 1);
+}
+
+int launch_vdif_advance(uint32_t *hdr, int njobs, int nframes, cudaStream_t st)
+{
+    if (njobs <= 0) return VGB_SUCCESS;
+    vdif_advance_kernel<<<(njobs + 127) / 128, 128, 0, st>>>(hdr, njobs, nframes);
+    return check_launch("vdif_advance_kernel");
 }
 
 // ===========================================================================

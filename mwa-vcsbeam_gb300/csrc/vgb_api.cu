@@ -351,6 +351,7 @@ int vgb_ipfb(const void *e, long long e_job_stride, const void *hist, long long 
     int rc = check_geometry(ntaps, nchan);
     if (rc) return rc;
     if (!e || !coeffs || (!out_f && !vdif)) return set_error(VGB_ERR_INVALID, "NULL pointer");
+    if (frame_offset < 0) return set_error(VGB_ERR_INVALID, "frame_offset must be >= 0");
     if (!aligned16(e) || (hist && !aligned16(hist)) || (e_job_stride & 15) || (hist_job_stride & 15))
         return set_error(VGB_ERR_INVALID, "e/hist must be 16-byte aligned with 16-byte job strides");
     IpfbArgs a{};
@@ -367,6 +368,12 @@ int vgb_ipfb(const void *e, long long e_job_stride, const void *hist, long long 
     a.hdr = hdr;
     a.frame_offset = frame_offset;
     return launch_ipfb(a, njobs, S(stream));
+}
+
+int vgb_vdif_advance(uint32_t *d_hdr, int njobs, int nframes, void *stream)
+{
+    if (!d_hdr || njobs < 0 || nframes < 0) return set_error(VGB_ERR_INVALID, "vdif_advance: bad argument");
+    return launch_vdif_advance(d_hdr, njobs, nframes, S(stream));
 }
 
 } // extern "C"
@@ -475,6 +482,10 @@ int pipeline_second(vgb_pipeline *p, const char2 *volt, long long cc_stride_byte
         const long long ejob = (long long)p->nspectra * kK * 16;
         rc = vgb_ipfb(p->d_e, ejob, p->second > 0 ? p->d_ehist[cur] : nullptr, (long long)kHistFrames * kK * 16,
                       p->d_coeffs, kP, kK, p->nspectra, c.ncc, nullptr, p->d_vdif, p->d_hdr, 0, p->s_comp);
+        if (rc) return rc;
+        p->launches++;
+        // the next second's headers start where this second's end
+        rc = launch_vdif_advance(p->d_hdr, c.ncc, p->nspectra, p->s_comp);
         if (rc) return rc;
         p->launches++;
         // carry the last 12 beam samples of each coarse channel
@@ -706,10 +717,13 @@ static long long state_hist_bytes(const vgb_pipeline *p)
     return (long long)p->cfg.ncc * p->ninputs * kHistFrames * kK * 2;
 }
 static long long state_ehist_bytes(const vgb_pipeline *p) { return (long long)sizeof(float4) * p->cfg.ncc * kHistFrames * kK; }
+static long long state_hdr_bytes(const vgb_pipeline *p) { return (long long)sizeof(uint32_t) * 8 * p->cfg.ncc; }
+constexpr uint32_t kStateVersion = 2; // version 2 adds the VDIF header templates
 
 long long vgb_pipeline_state_bytes(const vgb_pipeline *p)
 {
-    return p ? (long long)sizeof(PipelineStateHeader) + state_hist_bytes(p) + state_ehist_bytes(p) : 0;
+    return p ? (long long)sizeof(PipelineStateHeader) + state_hist_bytes(p) + state_ehist_bytes(p) + state_hdr_bytes(p)
+             : 0;
 }
 
 int vgb_pipeline_save_state(vgb_pipeline *p, void *host, long long bytes)
@@ -718,7 +732,8 @@ int vgb_pipeline_save_state(vgb_pipeline *p, void *host, long long bytes)
     if (bytes < vgb_pipeline_state_bytes(p)) return set_error(VGB_ERR_INVALID, "pipeline_save_state: buffer too small");
     int rc = check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
     if (rc) return rc;
-    PipelineStateHeader h{kStateMagic, 1, p->cfg.ncc, p->ninputs, p->cfg.nblocks, p->cfg.do_ipfb, p->second};
+    PipelineStateHeader h{kStateMagic, kStateVersion, p->cfg.ncc, p->ninputs, p->cfg.nblocks, p->cfg.do_ipfb,
+                          p->second};
     char *out = static_cast<char *>(host);
     std::memcpy(out, &h, sizeof(h));
     const int cur = (int)(p->second & 1);
@@ -728,6 +743,10 @@ int vgb_pipeline_save_state(vgb_pipeline *p, void *host, long long bytes)
         rc = check_cuda(cudaMemcpy(out + sizeof(h) + state_hist_bytes(p), p->d_ehist[cur], state_ehist_bytes(p),
                                    cudaMemcpyDeviceToHost),
                         "save beam history");
+    if (!rc)
+        rc = check_cuda(cudaMemcpy(out + sizeof(h) + state_hist_bytes(p) + state_ehist_bytes(p), p->d_hdr,
+                                   state_hdr_bytes(p), cudaMemcpyDeviceToHost),
+                        "save VDIF headers");
     return rc;
 }
 
@@ -737,7 +756,7 @@ int vgb_pipeline_load_state(vgb_pipeline *p, const void *host, long long bytes)
     if (bytes < vgb_pipeline_state_bytes(p)) return set_error(VGB_ERR_INVALID, "pipeline_load_state: buffer too small");
     PipelineStateHeader h;
     std::memcpy(&h, host, sizeof(h));
-    if (h.magic != kStateMagic || h.version != 1 || h.ncc != p->cfg.ncc || h.ninputs != p->ninputs ||
+    if (h.magic != kStateMagic || h.version != kStateVersion || h.ncc != p->cfg.ncc || h.ninputs != p->ninputs ||
         h.nblocks != p->cfg.nblocks || h.do_ipfb != p->cfg.do_ipfb || h.second < 0)
         return set_error(VGB_ERR_INVALID, "pipeline_load_state: state is from a different pipeline configuration");
     int rc = check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
@@ -752,6 +771,10 @@ int vgb_pipeline_load_state(vgb_pipeline *p, const void *host, long long bytes)
         rc = check_cuda(cudaMemcpy(p->d_ehist[cur], in + sizeof(h) + state_hist_bytes(p), state_ehist_bytes(p),
                                    cudaMemcpyHostToDevice),
                         "load beam history");
+    if (!rc)
+        rc = check_cuda(cudaMemcpy(p->d_hdr, in + sizeof(h) + state_hist_bytes(p) + state_ehist_bytes(p),
+                                   state_hdr_bytes(p), cudaMemcpyHostToDevice),
+                        "load VDIF headers");
     return rc;
 }
 

@@ -76,6 +76,10 @@ struct IpfbArgs {
 };
 
 int launch_beam(const BeamArgs &a, int ncc, bool int32_wola, bool fpga, bool demote, cudaStream_t st);
+// VDIF frames per second (the MWA fine sample rate, 1.28 MHz / 128): where a
+// header's frame number rolls over to the next second.
+constexpr int kVdifFramesPerSecond = 10000;
+int launch_vdif_advance(uint32_t *hdr, int njobs, int nframes, cudaStream_t st);
 // Force the fused front end's inputs per step (4 or 8), or 0 for the timed
 // choice; returns the previous setting, -1 for a bad value.
 int pfb_variant(int g);

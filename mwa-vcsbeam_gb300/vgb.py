@@ -106,6 +106,14 @@ _SIGS = {
     "vgb_incoh_beam": (I, [V, LL, I, V, V]),
     "vgb_renormalise": (I, [V, I, I, I, I, I, V, LL, LL, LL, LL, V, V, V]),
     "vgb_ipfb": (I, [V, LL, V, LL, V, I, I, I, I, V, V, V, I, V]),
+    "vgb_vdif_header_create": (I, [V, I, I, I, I, I, ctypes.c_char_p]),
+    "vgb_vdif_header_set_epoch_mjd": (I, [V, I]),
+    "vgb_vdif_header_epoch_mjd": (I, [V, ctypes.POINTER(I)]),
+    "vgb_vdif_header_set_mjdsec": (I, [V, LL]),
+    "vgb_vdif_header_set_frame": (I, [V, I]),
+    "vgb_vdif_header_next": (I, [V, I]),
+    "vgb_vdif_populate_header": (I, [V, I, Db, I, ctypes.c_char_p]),
+    "vgb_vdif_advance": (I, [V, I, I, V]),
     "vgb_beamform_mwax_psrfits_noalloc": (I, [ctypes.POINTER(Voltages), I, I, V, I, I, U, V, I, Fl, I, V, V, V,
                                               V]),
     "vgb_gemm_bf16": (I, [V, V, V, I, I, I, V]),
@@ -328,6 +336,60 @@ def ipfb(e, e_job_stride, hist, hist_job_stride, coeffs, nsamples, njobs, out_f=
          frame_offset=0, stream=None):
     check(lib().vgb_ipfb(ptr(e), e_job_stride, ptr(hist), hist_job_stride, ptr(coeffs), NTAPS, NCHAN, nsamples,
                          njobs, ptr(out_f), ptr(vdif), ptr(hdr), frame_offset, stream_ptr(stream)))
+
+
+VDIF_FRAMES_PER_SECOND = 10000
+
+
+def _hdr_buf(hdr):
+    if hdr is None:
+        hdr = np.zeros(8, np.uint32)
+    if not (isinstance(hdr, np.ndarray) and hdr.dtype == np.uint32 and hdr.flags.c_contiguous and hdr.size == 8):
+        raise VGBError("a VDIF header is a contiguous uint32 array of 8 words")
+    return hdr
+
+
+def vdif_header_create(dataarraylength=512, threadid=0, bits=8, nchan=2, iscomplex=True, stationid="mw"):
+    """createVDIFHeader: a new 8-word header (see the C header)."""
+    hdr = np.zeros(8, np.uint32)
+    check(lib().vgb_vdif_header_create(hdr.ctypes.data, dataarraylength, threadid, bits, nchan, int(iscomplex),
+                                       stationid.encode()))
+    return hdr
+
+
+def vdif_header_set_epoch_mjd(hdr, mjd):
+    check(lib().vgb_vdif_header_set_epoch_mjd(_hdr_buf(hdr).ctypes.data, int(mjd)))
+
+
+def vdif_header_epoch_mjd(hdr):
+    out = I()
+    check(lib().vgb_vdif_header_epoch_mjd(_hdr_buf(hdr).ctypes.data, ctypes.byref(out)))
+    return out.value
+
+
+def vdif_header_set_mjdsec(hdr, mjdsec):
+    check(lib().vgb_vdif_header_set_mjdsec(_hdr_buf(hdr).ctypes.data, int(mjdsec)))
+
+
+def vdif_header_set_frame(hdr, frame):
+    check(lib().vgb_vdif_header_set_frame(_hdr_buf(hdr).ctypes.data, int(frame)))
+
+
+def vdif_header_next(hdr, frames_per_second=VDIF_FRAMES_PER_SECOND):
+    check(lib().vgb_vdif_header_next(_hdr_buf(hdr).ctypes.data, int(frames_per_second)))
+
+
+def vdif_populate_header(intmjd, fracmjd, threadid=0, stationid="mw"):
+    """The header vmPopulateVDIFHeader gives a beam's first frame."""
+    hdr = np.zeros(8, np.uint32)
+    check(lib().vgb_vdif_populate_header(hdr.ctypes.data, int(intmjd), float(fracmjd), threadid,
+                                         None if stationid is None else stationid.encode()))
+    return hdr
+
+
+def vdif_advance(d_hdr, njobs, nframes, stream=None):
+    """Advance device header templates [njobs][8] by nframes frames."""
+    check(lib().vgb_vdif_advance(ptr(d_hdr), njobs, nframes, stream_ptr(stream)))
 
 
 def selftest_bounded_wait(polls=1000, stream=None):

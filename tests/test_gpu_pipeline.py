@@ -60,10 +60,18 @@ def make_pipeline(vgb, torch, filt, syn, tabs, invw):
     p.set_filters(filt, syn)
     W = torch.cat([weights_on_device(J, phi) for J, phi in tabs])
     p.set_weights(W, on_device=True)
-    hdr = np.zeros((NCC, 8), np.uint32)
-    hdr[:, 0] = [100, 200]
-    p.set_vdif_header(hdr)
+    p.set_vdif_header(vdif_templates(vgb))
     return p
+
+
+def vdif_templates(vgb):
+    """Channel 0 starts 600 frames before a second boundary, channel 1 at one."""
+    hdrs = []
+    for cc, frame in enumerate([10000 - 600, 0][:NCC]):
+        h = vgb.vdif_populate_header(60123, 0.25 + cc / 86400)
+        vgb.vdif_header_set_frame(h, frame)
+        hdrs.append(h)
+    return np.stack(hdrs)
 
 
 def test_pipeline_two_seconds(vgb_mod, torch, oracle_mod, setup):
@@ -71,6 +79,7 @@ def test_pipeline_two_seconds(vgb_mod, torch, oracle_mod, setup):
     invw = 1.0 / NI
     p = make_pipeline(vgb_mod, torch, filt, syn, tabs, invw)
     e_prev = [None] * NCC
+    hdr_run = vdif_templates(vgb_mod)
     for t in range(2):
         d = dev(volt[t].reshape(-1).view(np.uint8))
         p.run_device(d)
@@ -101,7 +110,12 @@ def test_pipeline_two_seconds(vgb_mod, torch, oracle_mod, setup):
             q = oracle_mod.vdif_quantise(flt)
             dq = np.abs(vd[cc, :, 32:].astype(np.int16) - q.astype(np.int16))
             assert dq.max() <= 1 and (dq > 0).mean() <= 1e-4
-            assert np.all(vd[cc, :, :4].copy().view(np.uint32)[:, 0] == (100, 200)[cc])
+            # headers run on from the template across the second boundary
+            h = hdr_run[cc]
+            words = vd[cc, :, :32].copy().view(np.uint32)
+            for f in range(NS):
+                assert np.array_equal(words[f], h), (t, cc, f)
+                vgb_mod.vdif_header_next(h)
             e_prev[cc] = eref[0]
     p.close()
 
@@ -147,7 +161,7 @@ def test_pipeline_graph_replay_equals_eager(vgb_mod, torch, setup):
             vd = np.empty((NCC, NS, 544), np.uint8)
             p.fetch(ps, None, None, vd)
             res.append((ps, vd))
-            assert p.launch_count() == 4
+            assert p.launch_count() == 5      # beam, renormalise, inverse PFB, VDIF headers, history
         p.close()
         outs.append(res)
     for (a, b), (c, d) in zip(outs[0], outs[1]):

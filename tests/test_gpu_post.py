@@ -148,3 +148,33 @@ def test_ipfb_vdif_against_oracle(vgb_mod, torch, oracle_mod, golden):
     assert np.array_equal(words[:, 1] & 0xFFFFFF, np.arange(ns, dtype=np.uint32))
     assert np.all(words[:, 1] >> 24 == 0x2A)
     assert np.array_equal(words[:, 2:], np.broadcast_to(hdr[0, 2:], (ns, 6)))
+
+
+def test_vdif_headers_roll_over(vgb_mod, torch, golden):
+    """Frame f of a call carries the template advanced f frames at 10000
+    frames per second (nextVDIFHeader); vgb_vdif_advance takes a template the
+    same number of frames as the host's vgb_vdif_header_next."""
+    ev = golden["ipfb_e"]
+    ns = ev.shape[1]
+    hdrs = []
+    for j, frame in enumerate([9990, 0, 10000 - ns]):
+        h = vgb_mod.vdif_populate_header(60123 + j, 0.25, threadid=j)
+        vgb_mod.vdif_header_set_frame(h, frame)
+        hdrs.append(h)
+    hdr = np.stack(hdrs)
+    e = np.broadcast_to(ev[1][None], (3,) + ev[1].shape)
+    _, vd = run_ipfb(vgb_mod, torch, np.ascontiguousarray(e), None, golden["ipfb_coeffs"], hdr=hdr)
+    for j in range(3):
+        h = hdr[j].copy()
+        words = vd[j, :, :32].copy().view(np.uint32)
+        for f in range(ns):
+            assert np.array_equal(words[f], h), (j, f)
+            vgb_mod.vdif_header_next(h)
+    d = dev(hdr)
+    for n in (1, 9, 10000, 23457):
+        vgb_mod.vdif_advance(d, 3, n)
+        for j in range(3):
+            for _ in range(n):
+                vgb_mod.vdif_header_next(hdr[j])
+        torch.cuda.synchronize()
+        assert np.array_equal(host(d, dtype=np.uint32).reshape(3, 8), hdr), n
