@@ -213,6 +213,41 @@ int vgb_ipfb(const void *e, long long e_job_stride, const void *hist, long long 
              const uint32_t *hdr, int frame_offset, void *stream);
 
 /*
+ * Voltage files on the host, one second of one coarse channel into a caller's
+ * (ideally pinned) buffer, for vgb_pipeline_run_host or an upload. They
+ * replace mwalib_voltage_context_read_second (metadata.c:973-985) and
+ * mwalib_metafits_get_expected_volt_filename (metadata.c:1214-1226); mwalib
+ * itself is not used. Reads are split over `nthreads` positioned reads.
+ *
+ * MWAX subfile: an ASCII "KEY value" header (HDR_SIZE bytes, default 4096;
+ * NINPUTS required; NBIT must be 8 if given; SECS_PER_SUBOBS default 8;
+ * OBS_ID, SUBOBS_ID = GPS second of the first block, COARSE_CHANNEL), one
+ * metadata block, then 20 blocks of [ninputs][64000] char2 per second.
+ * vgb_subfile_read_second writes the second's 20 blocks, [block][input]
+ * [sample] (the layout of one coarse channel of the pipeline's input).
+ * Legacy recombined file: the whole file (one second, v_IDX 4+4-bit bytes).
+ * vgb_volt_filename: <obsid>_<gps>_<rec_chan>.sub (gps rounded down to a
+ * multiple of 8, metadata.c:1152) or <obsid>_<gps>_ch<rec_chan>.dat.
+ */
+typedef struct vgb_subfile_info {
+    long long header_bytes;     /* HDR_SIZE */
+    long long block_bytes;      /* ninputs * 64000 * 2 */
+    long long file_bytes;
+    long long obs_id;           /* OBS_ID (0 if absent) */
+    long long subobs_id;        /* SUBOBS_ID: GPS second of the first voltage block */
+    int ninputs;
+    int samples_per_block;      /* 64000 */
+    int secs_per_subobs;
+    int coarse_channel;         /* COARSE_CHANNEL (-1 if absent) */
+    int metadata_blocks;        /* blocks before the voltages (1) */
+    int complete;               /* 1 if the file holds every second it names */
+} vgb_subfile_info;
+int vgb_subfile_info_read(const char *path, vgb_subfile_info *info);
+int vgb_subfile_read_second(const char *path, long long gps_second, void *dst, long long dst_bytes, int nthreads);
+int vgb_legacy_read_second(const char *path, void *dst, long long dst_bytes, int nthreads);
+int vgb_volt_filename(char *out, int out_len, long long obs_id, long long gps_second, int rec_chan, int mwax);
+
+/*
  * VDIF frame headers (8 uint32 words, VDIF 1.0 layout; host memory unless
  * noted). Frame f of a vgb_ipfb call carries the template hdr advanced by
  * frame_offset + f frames at 10000 frames per second, the MWA fine sample

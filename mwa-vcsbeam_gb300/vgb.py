@@ -68,6 +68,13 @@ MB_INT4, MB_INT8 = 0, 1
 MB_INT = 10  # samples per integration
 
 
+class SubfileInfo(ctypes.Structure):
+    _fields_ = [("header_bytes", ctypes.c_longlong), ("block_bytes", ctypes.c_longlong),
+                ("file_bytes", ctypes.c_longlong), ("obs_id", ctypes.c_longlong), ("subobs_id", ctypes.c_longlong),
+                ("ninputs", ctypes.c_int), ("samples_per_block", ctypes.c_int), ("secs_per_subobs", ctypes.c_int),
+                ("coarse_channel", ctypes.c_int), ("metadata_blocks", ctypes.c_int), ("complete", ctypes.c_int)]
+
+
 class PipelineConfig(ctypes.Structure):
     _fields_ = [
         ("ncc", ctypes.c_int),
@@ -114,6 +121,10 @@ _SIGS = {
     "vgb_vdif_header_next": (I, [V, I]),
     "vgb_vdif_populate_header": (I, [V, I, Db, I, ctypes.c_char_p]),
     "vgb_vdif_advance": (I, [V, I, I, V]),
+    "vgb_subfile_info_read": (I, [ctypes.c_char_p, ctypes.POINTER(SubfileInfo)]),
+    "vgb_subfile_read_second": (I, [ctypes.c_char_p, LL, V, LL, I]),
+    "vgb_legacy_read_second": (I, [ctypes.c_char_p, V, LL, I]),
+    "vgb_volt_filename": (I, [ctypes.c_char_p, I, LL, LL, I, I]),
     "vgb_beamform_mwax_psrfits_noalloc": (I, [ctypes.POINTER(Voltages), I, I, V, I, I, U, V, I, Fl, I, V, V, V,
                                               V]),
     "vgb_gemm_bf16": (I, [V, V, V, I, I, I, V]),
@@ -390,6 +401,34 @@ def vdif_populate_header(intmjd, fracmjd, threadid=0, stationid="mw"):
 def vdif_advance(d_hdr, njobs, nframes, stream=None):
     """Advance device header templates [njobs][8] by nframes frames."""
     check(lib().vgb_vdif_advance(ptr(d_hdr), njobs, nframes, stream_ptr(stream)))
+
+
+def _nbytes(buf):
+    if isinstance(buf, np.ndarray):
+        return buf.nbytes
+    return buf.numel() * buf.element_size()
+
+
+def subfile_info(path):
+    """Header fields of an MWAX voltage subfile (see the C header)."""
+    info = SubfileInfo()
+    check(lib().vgb_subfile_info_read(os.fsencode(path), ctypes.byref(info)))
+    return {name: getattr(info, name) for name, _ in SubfileInfo._fields_}
+
+
+def subfile_read_second(path, gps_second, dst, nthreads=4):
+    """One second ([20 blocks][inputs][64000] char2) of a subfile into dst (host)."""
+    check(lib().vgb_subfile_read_second(os.fsencode(path), int(gps_second), ptr(dst), _nbytes(dst), nthreads))
+
+
+def legacy_read_second(path, dst, nthreads=4):
+    check(lib().vgb_legacy_read_second(os.fsencode(path), ptr(dst), _nbytes(dst), nthreads))
+
+
+def volt_filename(obs_id, gps_second, rec_chan, mwax=True):
+    buf = ctypes.create_string_buffer(256)
+    check(lib().vgb_volt_filename(buf, 256, int(obs_id), int(gps_second), int(rec_chan), int(mwax)))
+    return buf.value.decode()
 
 
 def selftest_bounded_wait(polls=1000, stream=None):

@@ -201,3 +201,54 @@ def test_pipeline_checkpoint_resume(vgb_mod, torch, setup):
     with pytest.raises(vgb_mod.VGBError, match="different pipeline configuration"):
         c.load_state(bad)
     c.close()
+
+
+def test_pipeline_from_subfiles(vgb_mod, torch, setup, tmp_path):
+    """Whole seconds (20 blocks) read from MWAX subfiles straight into the
+    pinned host buffer (vgb_subfile_read_second, one call per coarse channel)
+    and streamed through the pipeline give the bytes of the same voltages
+    already on the device."""
+    _, filt, syn, tabs = setup
+    invw = 1.0 / NI
+    nblk, secs, subobs = 20, 2, 1300000000
+    ns = nblk * 500
+    rng = np.random.default_rng(21)
+    volt = rng.integers(-127, 128, (secs, NCC, nblk, NI, 64000, 2), dtype=np.int8)
+    paths = []
+    for cc in range(NCC):
+        text = f"HDR_SIZE 4096\nOBS_ID {subobs}\nSUBOBS_ID {subobs}\nNBIT 8\nNINPUTS {NI}\nSECS_PER_SUBOBS {secs}\n"
+        hdr = text.encode() + b"\0" * (4096 - len(text))
+        meta = np.zeros(NI * 64000 * 2, np.uint8)
+        path = tmp_path / vgb_mod.volt_filename(subobs, subobs, 109 + cc)
+        path.write_bytes(hdr + meta.tobytes() + np.ascontiguousarray(volt[:, cc]).tobytes())
+        paths.append(path)
+
+    def make():
+        p = vgb_mod.Pipeline(NCC, NANT, nblk, nstokes=4, pfb_flags=0, do_ipfb=True, invw=invw)
+        p.set_filters(filt, syn)
+        from helpers import weights_on_device
+
+        p.set_weights(torch.cat([weights_on_device(J, phi) for J, phi in tabs]), on_device=True)
+        return p
+
+    outs = []
+    for mode in ("device", "files"):
+        p = make()
+        res = []
+        for t in range(secs):
+            if mode == "device":
+                p.run_device(dev(volt[t].reshape(-1).view(np.uint8)))
+            else:
+                hb = torch.empty(NCC * nblk * NI * 64000 * 2, dtype=torch.uint8).pin_memory()
+                view = hb.numpy().reshape(NCC, -1)
+                for cc in range(NCC):
+                    vgb_mod.subfile_read_second(paths[cc], subobs + t, view[cc])
+                p.run_host(hb)
+            ps = np.empty((ns, 4, NCC * K), np.uint8)
+            vd = np.empty((NCC, ns, 544), np.uint8)
+            p.fetch(ps, None, None, vd)
+            res.append((ps, vd))
+        p.close()
+        outs.append(res)
+    for (a, b), (c, d) in zip(outs[0], outs[1]):
+        assert np.array_equal(a, c) and np.array_equal(b, d)
