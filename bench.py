@@ -44,7 +44,7 @@ NCC, NANT, NBLK, K, P = 24, 128, 20, 128, 12
 NI = 2 * NANT
 NSPEC = NBLK * 500
 SECOND_BYTES = NBLK * NI * 64000 * 2           # one coarse channel, one second
-BEAM_KERNEL_DRAM_BYTES_PER_CC = (1.322855e9 + 87.599872e6) / 2
+BEAM_KERNEL_DRAM_BYTES_PER_CC = (1.324512e9 + 87.549184e6) / 2
 
 
 def out_bytes(ncc):

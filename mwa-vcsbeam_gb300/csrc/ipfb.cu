@@ -25,12 +25,14 @@ namespace vgb {
 
 // The seconds / frame words of the header template (w0, w1) advanced by n
 // frames at kVdifFramesPerSecond (nextVDIFHeader applied n times,
-// beam_vdif.c:80): word `which` (0 or 1) of the result.
-__device__ __forceinline__ uint32_t vdif_advanced_word(uint32_t w0, uint32_t w1, long long n, int which)
+// beam_vdif.c:80): word `which` (0 or 1) of the result. n < 2^31, so the
+// frame total (< 2^24 + 2^31) and its division by the constant stay 32-bit.
+__device__ __forceinline__ uint32_t vdif_advanced_word(uint32_t w0, uint32_t w1, uint32_t n, int which)
 {
-    const long long total = (long long)(w1 & 0xFFFFFFu) + n;
-    if (which == 0) return (w0 & 0xC0000000u) | ((w0 + (uint32_t)(total / kVdifFramesPerSecond)) & 0x3FFFFFFFu);
-    return (w1 & 0xFF000000u) | (uint32_t)(total % kVdifFramesPerSecond);
+    const uint32_t total = (w1 & 0xFFFFFFu) + n;
+    const uint32_t sec = total / (uint32_t)kVdifFramesPerSecond;
+    if (which == 0) return (w0 & 0xC0000000u) | ((w0 + sec) & 0x3FFFFFFFu);
+    return (w1 & 0xFF000000u) | (total - sec * (uint32_t)kVdifFramesPerSecond);
 }
 
 constexpr int kIFT = 32;                 // frames per CTA
@@ -116,6 +118,20 @@ __global__ void __launch_bounds__(256) ipfb_kernel(const IpfbArgs a)
     const float invK = 1.0f / kK;
     float *outf = a.out_f ? a.out_f + job * a.outf_job : nullptr;
     uint8_t *vd = a.vdif ? a.vdif + job * a.vdif_job : nullptr;
+    // frame headers: one word per thread (kIFT frames x 8 words = 256)
+    if (vd) {
+        static_assert(kIFT * 8 == 256, "one header word per thread");
+        const int f = f0 + (tid >> 3), wi = tid & 7;
+        if (f < a.nsamples) {
+            uint32_t wv = a.hdr ? __ldg(a.hdr + job * 8 + wi) : 0u;
+            if (wi < 2) {
+                const uint32_t w0 = a.hdr ? __ldg(a.hdr + job * 8) : 0u;
+                const uint32_t w1 = a.hdr ? __ldg(a.hdr + job * 8 + 1) : 0u;
+                wv = vdif_advanced_word(w0, w1, (uint32_t)a.frame_offset + (uint32_t)f, wi);
+            }
+            reinterpret_cast<uint32_t *>(vd + (long long)f * 544)[wi] = wv;
+        }
+    }
 #pragma unroll
     for (int chunk = 0; chunk < kIFT; chunk += 16) {
         float ar[16], ai[16];
@@ -150,15 +166,6 @@ __global__ void __launch_bounds__(256) ipfb_kernel(const IpfbArgs a)
                 const uint32_t br = ((uint32_t)__float2int_rn(cr) ^ 0x80u) & 0xFFu;
                 const uint32_t bi = ((uint32_t)__float2int_rn(ci) ^ 0x80u) & 0xFFu;
                 reinterpret_cast<uint16_t *>(frame + 32)[r * 2 + pol] = (uint16_t)(br | (bi << 8));
-                if (tid < 8) {
-                    uint32_t wv = a.hdr ? __ldg(a.hdr + job * 8 + tid) : 0u;
-                    if (tid < 2) {
-                        const uint32_t w0 = a.hdr ? __ldg(a.hdr + job * 8) : 0u;
-                        const uint32_t w1 = a.hdr ? __ldg(a.hdr + job * 8 + 1) : 0u;
-                        wv = vdif_advanced_word(w0, w1, (long long)a.frame_offset + f, tid);
-                    }
-                    reinterpret_cast<uint32_t *>(frame)[tid] = wv;
-                }
             }
         }
     }
@@ -183,8 +190,8 @@ __global__ void vdif_advance_kernel(uint32_t *hdr, int njobs, int n)
     if (j >= njobs) return;
     uint32_t *h = hdr + j * 8;
     const uint32_t w0 = h[0], w1 = h[1];
-    h[0] = vdif_advanced_word(w0, w1, n, 0);
-    h[1] = vdif_advanced_word(w0, w1, n, 1);
+    h[0] = vdif_advanced_word(w0, w1, (uint32_t)n, 0);
+    h[1] = vdif_advanced_word(w0, w1, (uint32_t)n, 1);
 }
 
 int launch_vdif_advance(uint32_t *hdr, int njobs, int nframes, cudaStream_t st)

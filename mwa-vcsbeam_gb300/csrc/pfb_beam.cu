@@ -194,9 +194,13 @@ __device__ __forceinline__ void wola_step(FrontSmemT<G> &sm, int s, int li, int 
             *reinterpret_cast<float4 *>(&sm.buf[li * kT + m][n0]) = b;
         }
     } else {
+        // Without FPGA rounding the output scale 2^-14 / K (a power of two)
+        // rides on the taps: every product and partial sum is the exact one
+        // scaled, so the result is identical and the final multiply goes.
+        const float tsc = kFpga ? 1.0f : 1.0f / (16384.0f * kK);
         float2 h2[kP];
 #pragma unroll
-        for (int p = 0; p < kP; p++) h2[p] = make_float2((float)hc[0][p], (float)hc[1][p]);
+        for (int p = 0; p < kP; p++) h2[p] = make_float2((float)hc[0][p] * tsc, (float)hc[1][p] * tsc);
         float2 ar[kT], ai[kT];
 #pragma unroll
         for (int m = 0; m < kT; m++) ar[m] = ai[m] = make_float2(0.f, 0.f);
@@ -219,9 +223,7 @@ __device__ __forceinline__ void wola_step(FrontSmemT<G> &sm, int s, int li, int 
             if (kFpga) {
                 b = make_float4(fpga_round(ar[m].x), fpga_round(ai[m].x), fpga_round(ar[m].y), fpga_round(ai[m].y));
             } else {
-                const float2 sc = make_float2(1.0f / (16384.0f * kK), 1.0f / (16384.0f * kK));
-                const float2 r = __fmul2_rn(ar[m], sc), i = __fmul2_rn(ai[m], sc);
-                b = make_float4(r.x, i.x, r.y, i.y);
+                b = make_float4(ar[m].x, ai[m].x, ar[m].y, ai[m].y);
             }
             *reinterpret_cast<float4 *>(&sm.buf[li * kT + m][n0]) = b;
         }

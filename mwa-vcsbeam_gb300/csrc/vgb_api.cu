@@ -351,7 +351,8 @@ int vgb_ipfb(const void *e, long long e_job_stride, const void *hist, long long 
     int rc = check_geometry(ntaps, nchan);
     if (rc) return rc;
     if (!e || !coeffs || (!out_f && !vdif)) return set_error(VGB_ERR_INVALID, "NULL pointer");
-    if (frame_offset < 0) return set_error(VGB_ERR_INVALID, "frame_offset must be >= 0");
+    if (frame_offset < 0 || (long long)frame_offset + nsamples >= (1LL << 31))
+        return set_error(VGB_ERR_INVALID, "frame_offset must be >= 0 and frame_offset + nsamples < 2^31");
     if (!aligned16(e) || (hist && !aligned16(hist)) || (e_job_stride & 15) || (hist_job_stride & 15))
         return set_error(VGB_ERR_INVALID, "e/hist must be 16-byte aligned with 16-byte job strides");
     IpfbArgs a{};
