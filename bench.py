@@ -44,7 +44,7 @@ NCC, NANT, NBLK, K, P = 24, 128, 20, 128, 12
 NI = 2 * NANT
 NSPEC = NBLK * 500
 SECOND_BYTES = NBLK * NI * 64000 * 2           # one coarse channel, one second
-BEAM_KERNEL_DRAM_BYTES_PER_CC = (1.324512e9 + 87.549184e6) / 2
+BEAM_KERNEL_DRAM_BYTES_PER_CC = (1.320481e9 + 87.286784e6) / 2
 
 
 def out_bytes(ncc):
@@ -230,6 +230,8 @@ def gb300_arm(args, rank, local_rank, world):
     torch.cuda.set_device(local_rank)
     ctx = RankContext()
     vgb.lib()
+    if args.pfb_variant:
+        vgb.pfb_variant(args.pfb_variant)
 
     def barrier():
         ctx.barrier()
@@ -343,6 +345,7 @@ def gb300_arm(args, rank, local_rank, world):
                        "step": "one data-second (24 coarse channels x 1 s)",
                        "l2": "inputs larger than L2: each step reads a different 15.7 GB second",
                        "resident_seconds": args.resident,
+                       "pfb_inputs_per_step": vgb.pfb_variant_last(),
                        "cuda_graphs": "each second replayed from a captured CUDA graph (one per resident buffer "
                                       "and second parity); stage_ms from a separate eager pass with events"},
             "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
@@ -695,6 +698,8 @@ def main():
     ap.add_argument("--mb-modes", default=None, help="profiling: comma-separated precision modes")
     ap.add_argument("--mb-nfine", type=int, default=K, help="profiling: fine channels per case")
     ap.add_argument("--mb-stream-iters", type=int, default=3, help="many-beam host-streaming calls timed (0: skip)")
+    ap.add_argument("--pfb-variant", type=int, default=0, choices=[0, 4, 8],
+                    help="profiling: force the fused front end's inputs per step (0 = timed choice)")
     ap.add_argument("--beam-sweep", action="store_true",
                     help="time 1..1024 beams per coarse channel-second on both beamformers and print their JSON")
     ap.add_argument("--traffic", type=float, default=None,

@@ -124,6 +124,8 @@ int vgb_beamform_mwax(const vgb_voltages *v, int ncc, int nspectra, const int32_
  * choice, else 4). Force one with 4 or 8, or 0 for the timed choice; returns
  * the previous setting, -1 on a bad value. */
 int vgb_pfb_variant(int inputs_per_step);
+/* Inputs per step of the last fused front-end launch (0 before the first). */
+int vgb_pfb_variant_last(void);
 
 /*
  * Forward fine PFB only, packed to the legacy recombined layout (the output

@@ -506,6 +506,7 @@ static int dispatch(const Args &a, dim3 grid, bool i32, bool fpga, bool demote, 
 }
 
 static int g_pfb_variant = 0; // 0: autotuned; else forced inputs per step (4 or 8)
+static int g_pfb_last = 0;    // inputs per step of the last fused launch
 
 template <bool A, bool B, bool C> struct BeamSel {
     static int run_g(const BeamArgs &a, dim3 grid, cudaStream_t st, int g)
@@ -513,6 +514,7 @@ template <bool A, bool B, bool C> struct BeamSel {
         CUtensorMap wmap;
         int rc = make_tmap_beam_weights(&wmap, a.W, a.nant, (int)grid.y, a.W_cc, g / 2);
         if (rc) return rc;
+        g_pfb_last = g;
         if (g == 8) {
             if ((rc = prep<8>(beam_kernel<A, B, C, 8>))) return rc;
             beam_kernel<A, B, C, 8><<<grid, 512, front_smem<8>(), st>>>(a, wmap);
@@ -580,6 +582,8 @@ template <bool A, bool B, bool C> struct PackSel {
         return check_launch("pack_kernel");
     }
 };
+
+int pfb_variant_last() { return g_pfb_last; }
 
 int pfb_variant(int g)
 {

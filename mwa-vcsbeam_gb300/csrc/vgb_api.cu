@@ -190,6 +190,8 @@ int vgb_beamform_mwax(const vgb_voltages *v, int ncc, int nspectra, const int32_
                        (pfb_flags & VGB_PFB_COMPLEX_INT4) != 0, S(stream));
 }
 
+int vgb_pfb_variant_last(void) { return pfb_variant_last(); }
+
 int vgb_pfb_variant(int inputs_per_step)
 {
     const int prev = pfb_variant(inputs_per_step);

@@ -82,6 +82,7 @@ constexpr int kVdifFramesPerSecond = 10000;
 int launch_vdif_advance(uint32_t *hdr, int njobs, int nframes, cudaStream_t st);
 // Force the fused front end's inputs per step (4 or 8), or 0 for the timed
 // choice; returns the previous setting, -1 for a bad value.
+int pfb_variant_last();
 int pfb_variant(int g);
 int launch_pack(const PackArgs &a, int ncc, bool int32_wola, bool fpga, bool demote, cudaStream_t st);
 int launch_phase(const double *unit, const double *east, const double *north, const double *height,

@@ -113,6 +113,7 @@ _SIGS = {
     "vgb_incoh_beam": (I, [V, LL, I, V, V]),
     "vgb_renormalise": (I, [V, I, I, I, I, I, V, LL, LL, LL, LL, V, V, V]),
     "vgb_ipfb": (I, [V, LL, V, LL, V, I, I, I, I, V, V, V, I, V]),
+    "vgb_pfb_variant_last": (I, []),
     "vgb_vdif_header_create": (I, [V, I, I, I, I, I, ctypes.c_char_p]),
     "vgb_vdif_header_set_epoch_mjd": (I, [V, I]),
     "vgb_vdif_header_epoch_mjd": (I, [V, ctypes.POINTER(I)]),
@@ -279,6 +280,11 @@ def pfb_variant(g: int) -> int:
     if prev < 0:
         raise VGBError(lib().vgb_last_error().decode())
     return prev
+
+
+def pfb_variant_last() -> int:
+    """Inputs per step of the last fused front-end launch (0 before any)."""
+    return lib().vgb_pfb_variant_last()
 
 
 def gemm_batched(A, B, C, M, N, K, batch, fp16=False, stream=None):
