@@ -279,6 +279,25 @@ def gb300_arm(args, rank, local_rank, world):
     pipe.enable_timing(False)
     stage /= nstage
 
+    # the reference's --smart mode (PFB_SMART: FPGA rounding and 4-bit
+    # demotion of the fine channels) through the same stages
+    smart = vgb.Pipeline(ncc, NANT, NBLK, nstokes=4, pfb_flags=vgb.PFB_EMULATE_FPGA | vgb.PFB_COMPLEX_INT4,
+                         do_ipfb=True, invw=1.0 / NI)
+    smart.set_filters(h, syn)
+    smart.set_weights(W, on_device=True)
+    smart.enable_timing(True)
+    sstage = np.zeros(4)
+    for i in range(nstage + 1):
+        smart.run_device(volt[i % args.resident])
+        if i:
+            sstage += np.array(smart.stage_ms())
+    smart.close()
+    sstage /= nstage
+    smart_mode = {"pfb_flags": "PFB_EMULATE_FPGA | PFB_COMPLEX_INT4 (the reference's --smart)",
+                  "rtf_device_eager": (ncc / NCC) / (sstage.sum() / 1e3),
+                  "stage_ms": {"pfb_beam": sstage[0], "renormalise": sstage[1], "ipfb_vdif": sstage[2],
+                               "history": sstage[3]}}
+
     # ---- end to end through the host API ------------------------------------
     psr_b, vdif_b, stat_b = out_bytes(ncc)
     e2e = None
@@ -319,9 +338,9 @@ def gb300_arm(args, rank, local_rank, world):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     alg_bytes = ncc * SECOND_BYTES          # the voltages it must read, per launch
     # DRAM bytes (read + write) of one launch: the ncu capture of a 2-channel
-    # launch (profiles/beam_kernel_2cc.md: 1.3229 GB read + 87.6 MB written)
-    # scaled by the channels processed, since each channel's voltages are read
-    # once and its products written once
+    # launch (1.3205 GB read + 87.3 MB written) scaled by the channels
+    # processed, since each channel's voltages are read once and its products
+    # written once
     traffic = args.traffic if args.traffic is not None else ncc * BEAM_KERNEL_DRAM_BYTES_PER_CC
     achieved = alg_bytes / (stage[0] / 1e3) / 1e9
     roofline = {"kernel": "beam_kernel (fused PFB + tied-array/incoherent beam + Stokes)", "bound": "hbm",
@@ -348,7 +367,8 @@ def gb300_arm(args, rank, local_rank, world):
                        "pfb_inputs_per_step": vgb.pfb_variant_last(),
                        "cuda_graphs": "each second replayed from a captured CUDA graph (one per resident buffer "
                                       "and second parity); stage_ms from a separate eager pass with events"},
-            "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+            "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+            "smart_mode": smart_mode}
     if mb_section is not None:
         mb_section["gpu_launches"] = mb_launches
         line["multibeam"] = mb_section
