@@ -281,3 +281,48 @@ def test_multibeam_rejects_bad_config(vgb_mod):
         vgb_mod.Multibeam(1, 4, 20, 8, 100)
     with pytest.raises(vgb_mod.VGBError, match="multiple of 10"):
         vgb_mod.Multibeam(1, 4, 32, 8, 105)
+
+
+def test_mwax_smart_pfb_into_multibeam(vgb_mod, torch, oracle_mod):
+    """The --smart many-beam flow on one device: MWAX 8-bit voltages through
+    the fine PFB to 4+4-bit bytes in the legacy input order (vgb_fpfb), then
+    the many-beam GEMMs read those bytes where they are, with polQ/polP from
+    the same input order. The PFB bytes match the oracle's PFB (one LSB on
+    <= 1e-4 of nibbles, the FFT's rounding), the Stokes match the FP64
+    beamformer chain on the PFB's own bytes (split BF16, 1e-3)."""
+    from helpers import pol_lists
+
+    O = oracle_mod
+    nant, npnt, ns, K, P = 16, 40, 500, 128, 12
+    ni = 2 * nant
+    htr = O.mwax_buffer(77, 2, ni)                 # the margin block, then one block: 500 spectra
+    filt = SY.analysis_filter_int16()
+    i_idx = SY.legacy_input_order(nant)
+    d = dev(htr.reshape(-1).view(np.uint8))
+    v = vgb_mod.reference_buffer_voltages(d, ni, 1)
+    fine = torch.empty(ns * K * ni, dtype=torch.uint8, device="cuda")
+    vgb_mod.fpfb(v, 1, ns, dev(filt), dev(i_idx), vgb_mod.PFB_SMART, fine)
+    torch.cuda.synchronize()
+    assert vgb_mod.check_device_status() == 0
+    got = host(fine).reshape(ns, K, ni)
+    ref = O.fpfb(htr, ni, ns, filt, K, P, i_idx, O.PFB_SMART)
+    nib = lambda b: np.stack([(b.astype(np.int16) >> 4), (b.astype(np.int16) & 15)])
+    dn = np.abs(((nib(got) + 8) % 16) - ((nib(ref) + 8) % 16))
+    assert dn.max() <= 1 and (dn > 0).mean() <= 1e-4
+
+    case = make_case(O, nant, npnt, K, ns)
+    polQ, polP = pol_lists(i_idx)
+    case.update(polQ=polQ, polP=polP, v_oracle=got)
+    invw = 1.0 / ni
+    mb = vgb_mod.Multibeam(1, K, nant, npnt, ns, nstokes=4, precision=vgb_mod.MB_SPLIT_BF16, input=vgb_mod.MB_INT4,
+                           invw=invw)
+    mb.set_geometry(dev(case["unit"]), dev(case["east"]), dev(case["north"]), dev(case["height"]),
+                    dev(case["cable"]))
+    mb.set_jones(dev(case["D"]), dev(case["B"]), dev(case["freqs"]), dev(polQ), dev(polP))
+    S = torch.full((K * npnt * 4 * (ns // NINT),), float("nan"), dtype=torch.float32, device="cuda")
+    mb.run(fine, S=S)
+    torch.cuda.synchronize()
+    assert vgb_mod.check_device_status() == 0
+    mb.close()
+    errs = stokes_err(host(S).reshape(K, npnt, 4, ns // NINT), oracle_stokes(O, case, 4, invw))
+    assert max(errs) < 1e-3, errs
