@@ -21,6 +21,7 @@
 //      (form_beam.cpp:298-315) and the incoherent sum; or the PFB-only back
 //      end, which writes the packed legacy-order output (pfb.cpp:316-340).
 // The fine-channel voltages never reach HBM on the beamformer path.
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -505,8 +506,9 @@ static int dispatch(const Args &a, dim3 grid, bool i32, bool fpga, bool demote, 
     }
 }
 
-static int g_pfb_variant = 0; // 0: autotuned; else forced inputs per step (4 or 8)
-static int g_pfb_last = 0;    // inputs per step of the last fused launch
+// Process-wide switches, read and written from any host thread.
+static std::atomic<int> g_pfb_variant{0}; // 0: autotuned; else forced inputs per step (4 or 8)
+static std::atomic<int> g_pfb_last{0};    // inputs per step of the last fused launch
 
 template <bool A, bool B, bool C> struct BeamSel {
     static int run_g(const BeamArgs &a, dim3 grid, cudaStream_t st, int g)
@@ -530,7 +532,7 @@ template <bool A, bool B, bool C> struct BeamSel {
     // stream is being captured the cached choice is used if known, else 4.
     static int run(const BeamArgs &a, dim3 grid, cudaStream_t st)
     {
-        if (g_pfb_variant) return run_g(a, grid, st, g_pfb_variant);
+        if (const int forced = g_pfb_variant.load()) return run_g(a, grid, st, forced);
         static std::mutex mu;
         static std::map<std::tuple<int, int, int, int, int, bool, bool>, int> cache;
         const auto key = std::make_tuple((int)grid.x, (int)grid.y, a.vv.ninputs, a.nant, a.nstokes, a.e != nullptr,
@@ -588,9 +590,7 @@ int pfb_variant_last() { return g_pfb_last; }
 int pfb_variant(int g)
 {
     if (g != 0 && g != 4 && g != 8) return -1;
-    const int prev = g_pfb_variant;
-    g_pfb_variant = g;
-    return prev;
+    return g_pfb_variant.exchange(g);
 }
 
 int launch_beam(const BeamArgs &a, int ncc, bool int32_wola, bool fpga, bool demote, cudaStream_t st)

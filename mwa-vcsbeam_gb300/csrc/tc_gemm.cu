@@ -12,6 +12,7 @@
 // the device status word, frees its tensor memory and returns.
 #include <cudaTypedefs.h>
 
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -348,13 +349,13 @@ namespace vgb {
 // CUDA events on the caller's stream, after one warm-up) and cached; all give
 // identical results (same K order per output). While a stream is being
 // captured into a graph the measured choice is used if known, else 256.
-static int g_gemm_variant = 0; // 0: autotuned; else forced (128, 256, 512)
+static std::atomic<int> g_gemm_variant{0}; // 0: autotuned; else forced (128, 256, 512)
 
 template <class Launch>
 int gemm_tile_width(int M, int N, int K, int Kb, int batch, bool fp16, cudaStream_t st, Launch &launch)
 {
     if (N % 256) return 128;
-    if (g_gemm_variant) return g_gemm_variant;
+    if (const int forced = g_gemm_variant.load()) return forced;
     static std::mutex mu;
     static std::map<std::tuple<int, int, int, int, int, bool>, int> cache;
     const auto key = std::make_tuple(M, N, K, Kb, batch, fp16);
@@ -492,8 +493,7 @@ extern "C" int vgb_gemm_variant(int v)
 {
     if (v != 0 && v != 128 && v != 256 && v != 512)
         return set_error(VGB_ERR_INVALID, "gemm_variant: 0 (autotuned), 128, 256 or 512"), -1;
-    const int prev = g_gemm_variant;
-    g_gemm_variant = v;
+    const int prev = g_gemm_variant.exchange(v);
     return prev;
 }
 
