@@ -36,8 +36,11 @@ __device__ __forceinline__ uint32_t vdif_advanced_word(uint32_t w0, uint32_t w1,
 }
 
 constexpr int kIFT = 32;                 // frames per CTA
+constexpr int kIThreads = 512;           // two halves of 256: 16 frames each in the polyphase sum
 
-constexpr int kIRowsPad = 96;            // padded to whole warps of groups
+constexpr int kIRowsPad = 88;            // 2 x (kIFT + 11) = 86 rows, padded to whole warps of
+                                         // 8-thread groups; ~108 KB: two CTAs per SM
+static_assert(kIRowsPad >= 2 * (kIFT + kP - 1) && kIRowsPad % 4 == 0, "FFT rows");
 
 
 struct IpfbSmem {
@@ -45,7 +48,7 @@ struct IpfbSmem {
     float2 tw[128];
 };
 
-__global__ void __launch_bounds__(256) ipfb_kernel(const IpfbArgs a)
+__global__ void __launch_bounds__(kIThreads, 2) ipfb_kernel(const IpfbArgs a)
 {
     extern __shared__ __align__(16) unsigned char ism_raw[];
     IpfbSmem &sm = *reinterpret_cast<IpfbSmem *>(ism_raw);
@@ -65,7 +68,7 @@ __global__ void __launch_bounds__(256) ipfb_kernel(const IpfbArgs a)
     const float4 *hist = a.hist ? a.hist + job * a.hist_job : nullptr;
     // asynchronous 8-byte copies, all in flight before one wait; samples with
     // no source (outside the second and its history) are zero-filled
-    for (int idx = tid; idx < (kIFT + kP - 1) * kK; idx += 256) {
+    for (int idx = tid; idx < (kIFT + kP - 1) * kK; idx += kIThreads) {
         const int ml = idx / kK, k = idx % kK;
         const int m = mlo + ml;
         const float4 *src = e;
@@ -88,10 +91,12 @@ __global__ void __launch_bounds__(256) ipfb_kernel(const IpfbArgs a)
     asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
     __syncthreads();
 
-    // inverse FFTs, 32 transforms per pass, (-1)^r applied on the way out
+    // inverse FFTs, 64 transforms per pass (whole warps past the padded rows
+    // sit the last pass out), (-1)^r applied on the way out
     {
         const int g = tid >> 3, j = tid & 7;
-        for (int base = 0; base < kIRowsPad; base += 32) {
+        for (int base = 0; base < kIRowsPad; base += kIThreads / 8) {
+            if (base + g >= kIRowsPad) break;
             float2 *row = sm.y[base + g];
             fft128_pass1<+1>(row, sm.tw, j);
             __syncwarp();
@@ -110,8 +115,8 @@ __global__ void __launch_bounds__(256) ipfb_kernel(const IpfbArgs a)
     }
     __syncthreads();
 
-    // polyphase sum: thread (r, pol), frames in two chunks of 16
-    const int r = tid >> 1, pol = tid & 1;
+    // polyphase sum: thread (r, pol) of half h sums frames 16 h .. 16 h + 15
+    const int r = (tid & 255) >> 1, pol = tid & 1, half = tid >> 8;
     float fr[kP];
 #pragma unroll
     for (int p = 0; p < kP; p++) fr[p] = __ldg(a.coeffs + p * kK + r);
@@ -119,8 +124,7 @@ __global__ void __launch_bounds__(256) ipfb_kernel(const IpfbArgs a)
     float *outf = a.out_f ? a.out_f + job * a.outf_job : nullptr;
     uint8_t *vd = a.vdif ? a.vdif + job * a.vdif_job : nullptr;
     // frame headers: one word per thread (kIFT frames x 8 words = 256)
-    if (vd) {
-        static_assert(kIFT * 8 == 256, "one header word per thread");
+    if (vd && tid < kIFT * 8) {
         const int f = f0 + (tid >> 3), wi = tid & 7;
         if (f < a.nsamples) {
             uint32_t wv = a.hdr ? __ldg(a.hdr + job * 8 + wi) : 0u;
@@ -132,8 +136,9 @@ __global__ void __launch_bounds__(256) ipfb_kernel(const IpfbArgs a)
             reinterpret_cast<uint32_t *>(vd + (long long)f * 544)[wi] = wv;
         }
     }
-#pragma unroll
-    for (int chunk = 0; chunk < kIFT; chunk += 16) {
+    static_assert(kIThreads == 512 && kIFT == 32, "two halves of 16 frames");
+    {
+        const int chunk = 16 * half;
         float ar[16], ai[16];
 #pragma unroll
         for (int q = 0; q < 16; q++) ar[q] = ai[q] = 0.f;
@@ -179,7 +184,7 @@ int launch_ipfb(const IpfbArgs &a, int njobs, cudaStream_t st)
                         "cudaFuncSetAttribute(ipfb)");
     if (rc) return rc;
     dim3 grid((a.nsamples + kIFT - 1) / kIFT, njobs);
-    ipfb_kernel<<<grid, 256, smem, st>>>(a);
+    ipfb_kernel<<<grid, kIThreads, smem, st>>>(a);
     return check_launch("ipfb_kernel");
 }
 

@@ -209,8 +209,21 @@ __global__ void __launch_bounds__(256) renorm_kernel(const RenormArgs a)
 
     const float s0 = S[0];
     float mn = s0, mx = s0;
-    for (int s = sb + wid; s < se; s += 8) {
-        const float v = S[s * sstride];
+    // four independent loads in flight per lane (the scan order does not
+    // change the extremes: a NaN first value stays, later NaNs are skipped)
+    int s = sb + wid;
+    for (; s + 24 < se; s += 32) {
+        float v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) v[u] = S[(long long)(s + 8 * u) * sstride];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            mn = (v[u] < mn ? v[u] : mn);
+            mx = (v[u] > mx ? v[u] : mx);
+        }
+    }
+    for (; s < se; s += 8) {
+        const float v = S[(long long)s * sstride];
         mn = (v < mn ? v : mn);
         mx = (v > mx ? v : mx);
     }
@@ -241,7 +254,15 @@ __global__ void __launch_bounds__(256) renorm_kernel(const RenormArgs a)
     if (live) {
         uint8_t *o = a.out + cc * a.out_cc + p * a.out_p + st * a.out_st + c;
         const float rcp = 1.f / scale;
-        for (int s = sb + wid; s < se; s += 8) o[s * a.out_s] = quant_u8(S[s * sstride], offset, scale, rcp);
+        int s = sb + wid;
+        for (; s + 24 < se; s += 32) {
+            float v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = S[(long long)(s + 8 * u) * sstride];
+#pragma unroll
+            for (int u = 0; u < 4; u++) o[(long long)(s + 8 * u) * a.out_s] = quant_u8(v[u], offset, scale, rcp);
+        }
+        for (; s < se; s += 8) o[(long long)s * a.out_s] = quant_u8(S[(long long)s * sstride], offset, scale, rcp);
         if (part == 0 && wid == 0) {
             const long long si = cc * a.stat_cc + ((long long)p * a.nstokes + st) * a.nchan + c;
             a.scales[si] = scale;
