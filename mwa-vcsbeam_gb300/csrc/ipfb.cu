@@ -47,6 +47,7 @@ struct IpfbSmem {
     float2 y[kIRowsPad][kFftRow];
     float2 tw[128];
 };
+static_assert(sizeof(float2) * kIRowsPad * kFftRow % 16 == 0, "twiddles are read 16 bytes at a time");
 
 __global__ void __launch_bounds__(kIThreads, 2) ipfb_kernel(const IpfbArgs a)
 {
@@ -61,7 +62,7 @@ __global__ void __launch_bounds__(kIThreads, 2) ipfb_kernel(const IpfbArgs a)
         const int k1 = tid >> 3, j = tid & 7;
         double sn, cs;
         sincospi((double)(j * k1) / 64.0, &sn, &cs);
-        sm.tw[tid] = make_float2((float)cs, (float)sn);
+        sm.tw[fft128_tw_slot(k1, j)] = make_float2((float)cs, (float)sn);
     }
     // load X_k[m] for m in [f0 - 11, f0 + kIFT), de-interleaving the pols
     const float4 *e = a.e + job * a.e_job;
@@ -258,14 +259,14 @@ __global__ void round_staged_kernel(int *data, long long n, int fpga)
 __global__ void __launch_bounds__(256) fft_staged_kernel(float2 *rows, long long nrows)
 {
     __shared__ float2 buf[32][kFftRow];
-    __shared__ float2 tw[128];
+    __shared__ __align__(16) float2 tw[128];
     const int tid = threadIdx.x;
     const long long r0 = blockIdx.x * 32LL;
     if (tid < 128) {
         const int k1 = tid >> 3, j = tid & 7;
         double sn, cs;
         sincospi((double)(j * k1) / 64.0, &sn, &cs);
-        tw[tid] = make_float2((float)cs, (float)sn);
+        tw[fft128_tw_slot(k1, j)] = make_float2((float)cs, (float)sn);
     }
     for (int idx = tid; idx < 32 * kK; idx += 256) {
         const int r = idx / kK, n = idx % kK;

@@ -22,6 +22,7 @@
 //      end, which writes the packed legacy-order output (pfb.cpp:316-340).
 // The fine-channel voltages never reach HBM on the beamformer path.
 #include <atomic>
+#include <cstddef>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -43,10 +44,12 @@ template <int G> struct FrontSmemT {
     char2 stage[2][G][kWin][kK];           // TMA destinations: frames
     float4 wst[2][2][G / 2][kK];           // TMA destinations: weights [row][tile][k'] of the step's tiles
     float2 buf[G * kT][kFftRow];           // WOLA output -> FFT (in place) -> voltages
-    float2 tw[128];                        // W128 twiddles, [k1][j]
+    float2 tw[128];                        // W128 twiddles at fft128_tw_slot(k1, j) (16-byte aligned)
     uint64_t bar[2];
 };
 using FrontSmem = FrontSmemT<kG>;
+static_assert(offsetof(FrontSmemT<4>, tw) % 16 == 0 && offsetof(FrontSmemT<8>, tw) % 16 == 0,
+              "twiddles are read 16 bytes at a time");
 
 // ---------------------------------------------------------------------------
 // Copy the frames input `i` needs for spectra [m0, m0 + kT) into `dst`.
@@ -275,7 +278,7 @@ template <int G> __device__ __forceinline__ void init_front(FrontSmemT<G> &sm, i
         const int k1 = tid >> 3, j = tid & 7;
         double sn, cs;
         sincospi((double)(j * k1) / 64.0, &sn, &cs);
-        sm.tw[tid] = make_float2((float)cs, (float)sn);
+        sm.tw[fft128_tw_slot(k1, j)] = make_float2((float)cs, (float)sn);
     }
     if (tid == 0) {
         mbar_init(&sm.bar[0], 1);

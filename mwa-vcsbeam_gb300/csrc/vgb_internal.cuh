@@ -302,9 +302,15 @@ template <int SIGN> __device__ __forceinline__ void dft16(float2 *x)
 // alternating bank halves.
 constexpr int kFftRow = 152;
 
+// Slot (float2 units) of the twiddle W128^{j k1} in a 16-byte aligned table
+// of 128 float2: pairs k1 = 2i, 2i + 1 of one j sit together, so pass 1 reads
+// two twiddles per 16-byte load.
+__host__ __device__ __forceinline__ int fft128_tw_slot(int k1, int j) { return ((k1 >> 1) * 8 + j) * 2 + (k1 & 1); }
+
 // Pass 1: the 8 threads of one group read x[8q + j] (row `row`), transform
-// over q, twiddle by W128^{j k1} from `tw` (laid out [k1][j], cos/sin pairs of
-// the positive angle 2*pi*j*k1/128) and write back in place as Y_j[k1].
+// over q, twiddle by W128^{j k1} from `tw` (cos/sin pairs of the positive
+// angle 2*pi*j*k1/128 at fft128_tw_slot(k1, j)) and write back in place as
+// Y_j[k1].
 template <int SIGN>
 __device__ __forceinline__ void fft128_pass1(float2 *row, const float2 *tw, int j)
 {
@@ -313,10 +319,12 @@ __device__ __forceinline__ void fft128_pass1(float2 *row, const float2 *tw, int 
     for (int q = 0; q < 16; q++) x[q] = row[8 * q + j];
     __syncwarp();
     dft16<SIGN>(x);
+    const float4 *tw4 = reinterpret_cast<const float4 *>(tw);
 #pragma unroll
-    for (int k1 = 1; k1 < 16; k1++) {
-        float2 w = tw[k1 * 8 + j];
-        x[k1] = cmul_tw<SIGN>(x[k1], w.x, w.y);
+    for (int i = 0; i < 8; i++) {
+        const float4 w = tw4[i * 8 + j]; // W^{j 2i}, W^{j (2i + 1)}
+        if (i > 0) x[2 * i] = cmul_tw<SIGN>(x[2 * i], w.x, w.y);
+        x[2 * i + 1] = cmul_tw<SIGN>(x[2 * i + 1], w.z, w.w);
     }
 #pragma unroll
     for (int k1 = 0; k1 < 16; k1++) row[k1 * 9 + j] = x[k1];
