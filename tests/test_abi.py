@@ -57,6 +57,18 @@ def test_argument_errors_are_status_codes(vgb_mod):
     rc = lib.vgb_beamform_mwax_psrfits_noalloc(ctypes.byref(v), 2, 10000, None, 12, 128, 0, None, 16, 1.0, 4,
                                                None, None, None, None)
     assert rc == 1 and b"static scratch" in lib.vgb_last_error()
+    # inverse PFB: a negative or overflowing frame offset (checked before any launch)
+    rc = lib.vgb_ipfb(16, 16 * 128 * 16, None, 0, 16, 12, 128, 16, 1, 16, None, None, -1, None)
+    assert rc == 1 and b"frame_offset" in lib.vgb_last_error()
+    rc = lib.vgb_ipfb(16, 16 * 128 * 16, None, 0, 16, 12, 128, 16, 1, 16, None, None, (1 << 31) - 8, None)
+    assert rc == 1 and b"frame_offset" in lib.vgb_last_error()
+    assert lib.vgb_vdif_advance(None, 1, 10, None) == 1
+    assert lib.vgb_vdif_advance(16, 1, -1, None) == 1
+    # readers: a missing file is a status code, not an exit
+    info = vgb_mod.SubfileInfo()
+    assert lib.vgb_subfile_info_read(b"/nonexistent/x.sub", ctypes.byref(info)) == 1
+    assert lib.vgb_legacy_read_second(b"/nonexistent/x.dat", 16, 0, 1) == 1
+    assert lib.vgb_pfb_variant(5) == -1
 
 
 def test_filter_exactness_rule(vgb_mod):
