@@ -64,16 +64,6 @@ constexpr uint32_t kMbPolls = 1u << 26;
 // (form_beam.cpp:408-449) starts from the first value and compares with <, >:
 // a NaN there makes the result NaN, any other NaN is skipped; fminf/fmaxf over
 // the rest give the same extremes.
-__device__ __forceinline__ uint32_t fkey(float f)
-{
-    const uint32_t b = __float_as_uint(f);
-    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-}
-__device__ __forceinline__ float fkey_inv(uint32_t k)
-{
-    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
-}
-
 struct MbStats {
     uint32_t *mn, *mx; // [nfine][B][nst] keys
     uint32_t *nan0;    // [nfine][B][nst]: the row's first value is NaN

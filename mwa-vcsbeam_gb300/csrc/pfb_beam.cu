@@ -400,6 +400,7 @@ __global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1)
     }
 
     // form_beam.cpp:322-338
+    uint32_t kmn[4] = {~0u, ~0u, ~0u, ~0u}, kmx[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
     for (int mi = 0; mi < kMi; mi++) {
         const int m = m0 + mh + kMh * mi;
@@ -410,14 +411,40 @@ __global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1)
         const float bxr = c[0] * c[2] + c[1] * c[3] - c[6];
         const float bxi = c[1] * c[2] - c[0] * c[3] - c[7];
         float *S = a.S + cc * a.S_cc + ((long long)m * a.nstokes) * kK + kp;
-        S[0] = a.invw * (bnXX + bnYY);
+        const float sv[4] = {a.invw * (bnXX + bnYY), a.invw * (bnXX - bnYY), 2.0f * a.invw * bxr,
+                             -2.0f * a.invw * bxi};
+        S[0] = sv[0];
         if (a.nstokes == 4) {
-            S[kK] = a.invw * (bnXX - bnYY);
-            S[2 * kK] = 2.0f * a.invw * bxr;
-            S[3 * kK] = -2.0f * a.invw * bxi;
+            S[kK] = sv[1];
+            S[2 * kK] = sv[2];
+            S[3 * kK] = sv[3];
+        }
+        if (a.st_mn) {
+#pragma unroll
+            for (int st = 0; st < 4; st++) {
+                if (st >= a.nstokes) break;
+                if (isnan(sv[st])) {
+                    if (m == 0) a.st_nan0[(long long)(cc * a.nstokes + st) * kK + kp] = 1u;
+                } else {
+                    const uint32_t k = fkey(sv[st]);
+                    kmn[st] = min(kmn[st], k);
+                    kmx[st] = max(kmx[st], k);
+                }
+            }
         }
         if (a.e) a.e[cc * a.e_cc + (long long)m * kK + kp] = make_float4(c[0], c[1], c[2], c[3]);
         if (a.incoh) a.incoh[cc * a.inc_cc + (long long)m * kK + kp] = c[8];
+    }
+    // the row extremes for the 8-bit stage (min and max are idempotent, so a
+    // repeated launch over the same data leaves them unchanged)
+    if (a.st_mn) {
+#pragma unroll
+        for (int st = 0; st < 4; st++) {
+            if (st >= a.nstokes) break;
+            const long long r = (long long)(cc * a.nstokes + st) * kK + kp;
+            if (kmn[st] != ~0u) atomicMin(&a.st_mn[r], kmn[st]);
+            if (kmx[st] != 0u) atomicMax(&a.st_mx[r], kmx[st]);
+        }
     }
 }
 

@@ -207,48 +207,61 @@ __global__ void __launch_bounds__(256) renorm_kernel(const RenormArgs a)
     const int sb = (int)((long long)a.nstep * part / kRenormSplit);
     const int se = (int)((long long)a.nstep * (part + 1) / kRenormSplit);
 
-    const float s0 = S[0];
-    float mn = s0, mx = s0;
-    // four independent loads in flight per lane (the scan order does not
-    // change the extremes: a NaN first value stays, later NaNs are skipped)
-    int s = sb + wid;
-    for (; s + 24 < se; s += 32) {
-        float v[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) v[u] = S[(long long)(s + 8 * u) * sstride];
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            mn = (v[u] < mn ? v[u] : mn);
-            mx = (v[u] > mx ? v[u] : mx);
+    float mn, mx;
+    if (a.st_mn) {
+        // extremes gathered by the beam kernel: one pass over the samples
+        const long long si = cc * a.stat_cc + ((long long)p * a.nstokes + st) * a.nchan + (live ? c : 0);
+        if (a.st_nan0[si]) {
+            mn = mx = __int_as_float(0x7fffffff);
+        } else {
+            mn = fkey_inv(a.st_mn[si]);
+            mx = fkey_inv(a.st_mx[si]);
         }
-    }
-    for (; s < se; s += 8) {
-        const float v = S[(long long)s * sstride];
-        mn = (v < mn ? v : mn);
-        mx = (v > mx ? v : mx);
-    }
-    smin[wid][lane] = mn;
-    smax[wid][lane] = mx;
-    __syncthreads();
-    if (wid == 0) {
-        for (int w = 1; w < 8; w++) {
-            const float v0 = smin[w][lane], v1 = smax[w][lane];
+    } else {
+        const float s0 = S[0];
+        mn = s0;
+        mx = s0;
+        // four independent loads in flight per lane (the scan order does not
+        // change the extremes: a NaN first value stays, later NaNs are skipped)
+        int s = sb + wid;
+        for (; s + 24 < se; s += 32) {
+            float v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = S[(long long)(s + 8 * u) * sstride];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                mn = (v[u] < mn ? v[u] : mn);
+                mx = (v[u] > mx ? v[u] : mx);
+            }
+        }
+        for (; s < se; s += 8) {
+            const float v = S[(long long)s * sstride];
+            mn = (v < mn ? v : mn);
+            mx = (v > mx ? v : mx);
+        }
+        smin[wid][lane] = mn;
+        smax[wid][lane] = mx;
+        __syncthreads();
+        if (wid == 0) {
+            for (int w = 1; w < 8; w++) {
+                const float v0 = smin[w][lane], v1 = smax[w][lane];
+                mn = (v0 < mn ? v0 : mn);
+                mx = (v1 > mx ? v1 : mx);
+            }
+            cmin[lane] = mn;
+            cmax[lane] = mx;
+        }
+        cluster.sync(); // every CTA's partial is in its shared memory
+        mn = s0;
+        mx = s0;
+        for (int r = 0; r < kRenormSplit; r++) {
+            const float v0 = *cluster.map_shared_rank(&cmin[lane], r);
+            const float v1 = *cluster.map_shared_rank(&cmax[lane], r);
             mn = (v0 < mn ? v0 : mn);
             mx = (v1 > mx ? v1 : mx);
         }
-        cmin[lane] = mn;
-        cmax[lane] = mx;
+        cluster.sync(); // no CTA leaves while another still reads its partials
     }
-    cluster.sync(); // every CTA's partial is in its shared memory
-    mn = s0;
-    mx = s0;
-    for (int r = 0; r < kRenormSplit; r++) {
-        const float v0 = *cluster.map_shared_rank(&cmin[lane], r);
-        const float v1 = *cluster.map_shared_rank(&cmax[lane], r);
-        mn = (v0 < mn ? v0 : mn);
-        mx = (v1 > mx ? v1 : mx);
-    }
-    cluster.sync(); // no CTA leaves while another still reads its partials
     const float scale = (float)((double)(mx - mn) / 256.0);
     const float offset = mn;
     if (live) {

@@ -157,9 +157,16 @@ int vgb_check_device_status(void *stream, unsigned *flags_out)
     return VGB_SUCCESS;
 }
 
-int vgb_beamform_mwax(const vgb_voltages *v, int ncc, int nspectra, const int32_t *filter, int ntaps, int nchan,
-                      unsigned pfb_flags, const void *W, int nant, float invw, int nstokes, float *S_, void *e,
-                      float *incoh, void *stream)
+} // extern "C"
+
+namespace {
+
+// vgb_beamform_mwax, optionally gathering the per-(cc, stokes, channel)
+// extremes of S for the 8-bit stage (rstat: min keys, max keys, NaN flags,
+// [ncc][nstokes][128] each, or NULL).
+int beamform_mwax_impl(const vgb_voltages *v, int ncc, int nspectra, const int32_t *filter, int ntaps, int nchan,
+                       unsigned pfb_flags, const void *W, int nant, float invw, int nstokes, float *S_, void *e,
+                       float *incoh, uint32_t *rstat, void *stream)
 {
     int rc = check_geometry(ntaps, nchan);
     if (rc) return rc;
@@ -186,8 +193,26 @@ int vgb_beamform_mwax(const vgb_voltages *v, int ncc, int nspectra, const int32_
     a.inc_cc = (long long)nspectra * kK;
     a.status = status_word();
     if (!a.status) return set_error(VGB_ERR_CUDA, "device status word unavailable");
+    if (rstat) {
+        const long long n = (long long)ncc * nstokes * kK;
+        a.st_mn = rstat;
+        a.st_mx = rstat + n;
+        a.st_nan0 = rstat + 2 * n;
+    }
     return launch_beam(a, ncc, !(pfb_flags & VGB_WOLA_FP32), (pfb_flags & VGB_PFB_EMULATE_FPGA) != 0,
                        (pfb_flags & VGB_PFB_COMPLEX_INT4) != 0, S(stream));
+}
+
+} // namespace
+
+extern "C" {
+
+int vgb_beamform_mwax(const vgb_voltages *v, int ncc, int nspectra, const int32_t *filter, int ntaps, int nchan,
+                      unsigned pfb_flags, const void *W, int nant, float invw, int nstokes, float *S_, void *e,
+                      float *incoh, void *stream)
+{
+    return beamform_mwax_impl(v, ncc, nspectra, filter, ntaps, nchan, pfb_flags, W, nant, invw, nstokes, S_, e, incoh,
+                              nullptr, stream);
 }
 
 int vgb_pfb_variant_last(void) { return pfb_variant_last(); }
@@ -321,11 +346,18 @@ int vgb_incoh_beam(const uint8_t *data, long long nrows, int ninput, float *inco
     return launch_incoh(data, nrows, ninput, incoh, S(stream));
 }
 
-int vgb_renormalise(const float *S_, int ncc, int npointing, int nstep, int nstokes, int nchan, uint8_t *out,
-                    long long out_cc, long long out_p, long long out_s, long long out_st, float *offsets,
-                    float *scales, void *stream)
+} // extern "C"
+
+namespace {
+
+// vgb_renormalise, optionally from extremes the beam kernel gathered (rstat
+// as in beamform_mwax_impl, one pointing) instead of its own first pass.
+int renormalise_impl(const float *S_, int ncc, int npointing, int nstep, int nstokes, int nchan, uint8_t *out,
+                     long long out_cc, long long out_p, long long out_s, long long out_st, float *offsets,
+                     float *scales, const uint32_t *rstat, void *stream)
 {
     if (!S_ || !out || !offsets || !scales) return set_error(VGB_ERR_INVALID, "NULL pointer");
+    if (rstat && npointing != 1) return set_error(VGB_ERR_INVALID, "gathered extremes cover one pointing");
     if (ncc <= 0 || npointing <= 0 || nstokes <= 0 || nchan <= 0 || nstep < 0)
         return set_error(VGB_ERR_INVALID, "bad sizes");
     RenormArgs a{};
@@ -343,7 +375,25 @@ int vgb_renormalise(const float *S_, int ncc, int npointing, int nstep, int nsto
     a.offsets = offsets;
     a.scales = scales;
     a.stat_cc = (long long)npointing * nstokes * nchan;
+    if (rstat) {
+        const long long n = (long long)ncc * nstokes * nchan;
+        a.st_mn = rstat;
+        a.st_mx = rstat + n;
+        a.st_nan0 = rstat + 2 * n;
+    }
     return launch_renorm(a, ncc, S(stream));
+}
+
+} // namespace
+
+extern "C" {
+
+int vgb_renormalise(const float *S_, int ncc, int npointing, int nstep, int nstokes, int nchan, uint8_t *out,
+                    long long out_cc, long long out_p, long long out_s, long long out_st, float *offsets,
+                    float *scales, void *stream)
+{
+    return renormalise_impl(S_, ncc, npointing, nstep, nstokes, nchan, out, out_cc, out_p, out_s, out_st, offsets,
+                            scales, nullptr, stream);
 }
 
 int vgb_ipfb(const void *e, long long e_job_stride, const void *hist, long long hist_job_stride, const float *coeffs,
@@ -404,6 +454,7 @@ struct vgb_pipeline {
     float *d_off = nullptr, *d_scl = nullptr;
     uint8_t *d_vdif = nullptr;       // [cc][ns][544]
     uint32_t *d_hdr = nullptr;
+    uint32_t *d_rstat = nullptr;     // [3][cc][stokes][128]: Stokes min / max keys, first-value NaN flags
     long long second = 0;            // seconds completed
     int launches = 0;
     int host_buf = 0;
@@ -455,6 +506,16 @@ vgb_voltages pipeline_voltages(const vgb_pipeline *p, const char2 *volt, long lo
     return v;
 }
 
+// Empty extremes (min keys all ones, max keys and NaN flags zero) for the
+// next second's beam kernel to gather into.
+int reset_rstat(vgb_pipeline *p)
+{
+    const size_t n = (size_t)p->cfg.ncc * p->cfg.nstokes * kK;
+    int rc = check_cuda(cudaMemsetAsync(p->d_rstat, 0xFF, n * sizeof(uint32_t), p->s_comp), "reset extremes");
+    return rc ? rc : check_cuda(cudaMemsetAsync(p->d_rstat + n, 0, 2 * n * sizeof(uint32_t), p->s_comp),
+                                "reset extremes");
+}
+
 // One second of compute on s_comp with the voltages at `volt`.
 int pipeline_second(vgb_pipeline *p, const char2 *volt, long long cc_stride_bytes)
 {
@@ -469,17 +530,20 @@ int pipeline_second(vgb_pipeline *p, const char2 *volt, long long cc_stride_byte
         return p->timing ? check_cuda(cudaEventRecord(p->ev_stage[i], p->s_comp), "stage event") : VGB_SUCCESS;
     };
     if ((rc = mark(0))) return rc;
-    rc = vgb_beamform_mwax(&v, c.ncc, p->nspectra, p->d_filter, kP, kK, flags, p->d_W, c.nant, c.invw, c.nstokes,
-                           p->d_S, p->d_e, p->d_incoh, p->s_comp);
+    rc = beamform_mwax_impl(&v, c.ncc, p->nspectra, p->d_filter, kP, kK, flags, p->d_W, c.nant, c.invw, c.nstokes,
+                            p->d_S, p->d_e, p->d_incoh, p->d_rstat, p->s_comp);
     if (rc) return rc;
     p->launches++;
     if ((rc = mark(1))) return rc;
     // spliced PSRFITS rows: [s][st][cc*128 + c]
     const long long row = (long long)c.nstokes * c.ncc * kK;
-    rc = vgb_renormalise(p->d_S, c.ncc, 1, p->nspectra, c.nstokes, kK, p->d_psrfits, kK, 0, row,
-                         (long long)c.ncc * kK, p->d_off, p->d_scl, p->s_comp);
+    rc = renormalise_impl(p->d_S, c.ncc, 1, p->nspectra, c.nstokes, kK, p->d_psrfits, kK, 0, row,
+                          (long long)c.ncc * kK, p->d_off, p->d_scl, p->d_rstat, p->s_comp);
     if (rc) return rc;
     p->launches++;
+    // the next second's extremes start empty
+    rc = reset_rstat(p);
+    if (rc) return rc;
     if ((rc = mark(2))) return rc;
     if (c.do_ipfb) {
         const long long ejob = (long long)p->nspectra * kK * 16;
@@ -621,12 +685,14 @@ int vgb_pipeline_create(const vgb_pipeline_config *cfg, vgb_pipeline **out)
     rc = rc ? rc : dalloc(&p->d_scl, sizeof(float) * ncc * cfg->nstokes * kK);
     if (cfg->do_ipfb) rc = rc ? rc : dalloc(&p->d_vdif, (size_t)ncc * ns * 544);
     rc = rc ? rc : dalloc(&p->d_hdr, sizeof(uint32_t) * 8 * ncc);
+    rc = rc ? rc : dalloc(&p->d_rstat, sizeof(uint32_t) * 3 * ncc * cfg->nstokes * kK);
     if (!rc) {
         for (int b = 0; b < 2 && !rc; b++)
             rc = check_cuda(cudaMemsetAsync(p->d_hist[b], 0, (size_t)ncc * p->ninputs * kHistFrames * kK * 2,
                                             p->s_comp),
                             "memset history");
         rc = rc ? rc : check_cuda(cudaMemsetAsync(p->d_hdr, 0, sizeof(uint32_t) * 8 * ncc, p->s_comp), "memset hdr");
+        rc = rc ? rc : reset_rstat(p);
         rc = rc ? rc : check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
     }
     if (rc) {
@@ -650,7 +716,7 @@ int vgb_pipeline_destroy(vgb_pipeline *p)
     drop_graphs(p);
     void *bufs[] = {p->d_filter, p->d_coeffs, p->d_W, p->d_volt[0], p->d_volt[1], p->d_hist[0], p->d_hist[1],
                     p->d_S, p->d_e, p->d_incoh, p->d_ehist[0], p->d_ehist[1], p->d_psrfits, p->d_off, p->d_scl,
-                    p->d_vdif, p->d_hdr};
+                    p->d_vdif, p->d_hdr, p->d_rstat};
     for (void *b : bufs)
         if (b) cudaFree(b);
     for (int i = 0; i < 5; i++)

@@ -138,6 +138,18 @@ __device__ __forceinline__ uint8_t sat_u8_half(float v)
     return sat_u8((double)v + 0.5);
 }
 
+// Order-preserving unsigned keys of floats (for atomicMin / atomicMax over
+// the extremes of a row); NaN is never passed in.
+__device__ __forceinline__ uint32_t fkey(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float fkey_inv(uint32_t k)
+{
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
 // The reference's byte for one value, (uint8_t)((e - off) / scl + 0.5) with
 // the division correctly rounded, without a division on the common path.
 // With rcp = 1/scl (correctly rounded), q0 = x * rcp is within 1.5 ulp of

@@ -22,6 +22,11 @@ struct BeamArgs {
     float *incoh;           // [cc][s][K], nullable
     long long inc_cc;
     unsigned *status;
+    // nullable: per (cc, stokes, channel) extremes of S over the spectra, as
+    // order-preserving keys (atomicMin / atomicMax; reset to ~0 / 0 / 0), and
+    // whether spectrum 0's value is NaN: [cc][nstokes][K] each (the index of
+    // the 8-bit stage's offsets for one pointing)
+    uint32_t *st_mn, *st_mx, *st_nan0;
 };
 
 struct PackArgs {
@@ -43,6 +48,9 @@ struct RenormArgs {
     long long out_cc, out_p, out_s, out_st;
     float *offsets, *scales; // + cc*stat_cc + (p*nstokes + st)*nchan + c
     long long stat_cc;
+    // nullable: the extremes gathered by the beam kernel (same index as
+    // offsets); with them the samples are read once instead of twice
+    const uint32_t *st_mn, *st_mx, *st_nan0;
 };
 
 struct LegacyArgs {
