@@ -44,7 +44,7 @@ NCC, NANT, NBLK, K, P = 24, 128, 20, 128, 12
 NI = 2 * NANT
 NSPEC = NBLK * 500
 SECOND_BYTES = NBLK * NI * 64000 * 2           # one coarse channel, one second
-BEAM_KERNEL_DRAM_BYTES_PER_CC = (1.320481e9 + 87.286784e6) / 2
+BEAM_KERNEL_DRAM_BYTES_PER_CC = (1.322368e9 + 86.6944e6) / 2
 
 
 def out_bytes(ncc):
@@ -338,7 +338,7 @@ def gb300_arm(args, rank, local_rank, world):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     alg_bytes = ncc * SECOND_BYTES          # the voltages it must read, per launch
     # DRAM bytes (read + write) of one launch: the ncu capture of a 2-channel
-    # launch (1.3205 GB read + 87.3 MB written) scaled by the channels
+    # launch (1.3224 GB read + 86.7 MB written) scaled by the channels
     # processed, since each channel's voltages are read once and its products
     # written once
     traffic = args.traffic if args.traffic is not None else ncc * BEAM_KERNEL_DRAM_BYTES_PER_CC
