@@ -298,6 +298,27 @@ def gb300_arm(args, rank, local_rank, world):
                   "stage_ms": {"pfb_beam": sstage[0], "renormalise": sstage[1], "ipfb_vdif": sstage[2],
                                "history": sstage[3]}}
 
+    # a filter as large as the reference's FINEPFB (peak tap 117,964): its
+    # partial sums can pass 2^24, so the weighted overlap-add runs in int32
+    hbig = (h.astype(np.int64) * 117964 // int(np.abs(h).max())).astype(np.int32)
+    assert not vgb.filter_fp32_exact(hbig)
+    big = vgb.Pipeline(ncc, NANT, NBLK, nstokes=4, pfb_flags=0, do_ipfb=True, invw=1.0 / NI)
+    big.set_filters(hbig, syn)
+    big.set_weights(W, on_device=True)
+    big.enable_timing(True)
+    bstage = np.zeros(4)
+    for i in range(nstage + 1):
+        big.run_device(volt[i % args.resident])
+        if i:
+            bstage += np.array(big.stage_ms())
+    big.close()
+    bstage /= nstage
+    int32_wola = {"filter": "the int16 prototype scaled to a peak tap of 117,964 (the reference's FINEPFB range): "
+                            "exact int32 weighted overlap-add",
+                  "rtf_device_eager": (ncc / NCC) / (bstage.sum() / 1e3),
+                  "stage_ms": {"pfb_beam": bstage[0], "renormalise": bstage[1], "ipfb_vdif": bstage[2],
+                               "history": bstage[3]}}
+
     # ---- end to end through the host API ------------------------------------
     psr_b, vdif_b, stat_b = out_bytes(ncc)
     e2e = None
@@ -368,7 +389,7 @@ def gb300_arm(args, rank, local_rank, world):
                        "cuda_graphs": "each second replayed from a captured CUDA graph (one per resident buffer "
                                       "and second parity); stage_ms from a separate eager pass with events"},
             "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
-            "smart_mode": smart_mode}
+            "smart_mode": smart_mode, "int32_wola": int32_wola}
     if mb_section is not None:
         mb_section["gpu_launches"] = mb_launches
         line["multibeam"] = mb_section
