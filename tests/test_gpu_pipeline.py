@@ -252,3 +252,35 @@ def test_pipeline_from_subfiles(vgb_mod, torch, setup, tmp_path):
         outs.append(res)
     for (a, b), (c, d) in zip(outs[0], outs[1]):
         assert np.array_equal(a, c) and np.array_equal(b, d)
+
+
+def test_pipeline_nan_channel(vgb_mod, torch, oracle_mod, setup):
+    """A NaN weight makes one channel's Stokes NaN at every sample: the
+    extremes the beam kernel gathers then flag the channel's first value as
+    NaN, and the PSRFITS bytes, offsets and scales equal the oracle's
+    renormalise of the device's own Stokes (the reference's sequential scan:
+    a NaN first value makes the extremes NaN)."""
+    from helpers import weights_on_device
+
+    volt, filt, syn, tabs = setup
+    p = vgb_mod.Pipeline(NCC, NANT, NBLK, nstokes=4, pfb_flags=0, do_ipfb=True, invw=1.0 / NI)
+    p.set_filters(filt, syn)
+    W = torch.cat([weights_on_device(J, phi) for J, phi in tabs])
+    W[(0 * NANT + 3) * K + 17] = float("nan")            # cc 0, tile 3, channel 17
+    p.set_weights(W, on_device=True)
+    for t in range(2):
+        p.run_device(dev(volt[t].reshape(-1).view(np.uint8)))
+        ps = np.empty((NS, 4, NCC * K), np.uint8)
+        off = np.empty((NCC, 4, K), np.float32)
+        sc = np.empty((NCC, 4, K), np.float32)
+        p.fetch(ps, off, sc, None)
+        S = np.empty((NCC, NS, 4, K), np.float32)
+        e = np.empty((NCC, NS, K, 2), np.complex64)
+        p.fetch_raw(S, e)
+        assert np.isnan(S[0, :, :, 17]).all() and not np.isnan(S[0, :, :, 16]).any()
+        for cc in range(NCC):
+            o, s, u = oracle_mod.renormalise(S[cc][None])
+            assert np.array_equal(ps[:, :, cc * K:(cc + 1) * K], u[0]), (t, cc)
+            assert np.array_equal(off[cc], o[0], equal_nan=True) and np.array_equal(sc[cc], s[0], equal_nan=True)
+        assert np.isnan(off[0, :, 17]).all()
+    p.close()
