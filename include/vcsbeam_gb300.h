@@ -131,7 +131,11 @@ int vgb_pfb_variant_last(void);
  * Forward fine PFB only, packed to the legacy recombined layout (the output
  * of vmExecuteForwardPFB, pfb.cpp:730-773): out [ncc][nspectra][128][ninputs]
  * uint8 (4+4-bit, VGB_PFB_COMPLEX_INT4) or complex double, input i written at
- * column i_idx[i] (the VCS order, pfb.cpp:410-419).
+ * column i_idx[i] (the VCS order, pfb.cpp:410-419). i_idx must be a
+ * permutation of 0 .. ninputs-1 (the reference's map is; otherwise nothing is
+ * written and the device status word reports bad input); at most 1024 inputs.
+ * The inputs are processed in the order of their output columns, so each row
+ * of the output is written in whole adjacent groups.
  */
 int vgb_fpfb(const vgb_voltages *v, int ncc, int nspectra, const int32_t *filter, int ntaps, int nchan,
              const int32_t *i_idx, unsigned pfb_flags, void *out, void *stream);

@@ -88,10 +88,12 @@ __device__ __forceinline__ uint32_t issue_frames(const VoltView &vv, int cc, int
 // Producer: warp 0 queues step `it`'s frames (and, when a weight map is
 // given, the two Jones rows of its G/2 tiles, tiles past the last one
 // zero-filled) into stage it & 1, one input per lane (lane G the weights), so
-// the copy set-up costs the warp about one input's worth.
+// the copy set-up costs the warp about one input's worth. Step position
+// it * G + li holds input order[it * G + li] when an order is given, else
+// that input itself.
 template <int G>
 __device__ __forceinline__ void produce(FrontSmemT<G> &sm, const VoltView &vv, int cc, int it, int m0, int nspectra,
-                                       const CUtensorMap *wmap, unsigned *status)
+                                       const CUtensorMap *wmap, unsigned *status, const int *order = nullptr)
 {
     const int lane = threadIdx.x & 31;
     const int s = it & 1;
@@ -105,8 +107,10 @@ __device__ __forceinline__ void produce(FrontSmemT<G> &sm, const VoltView &vv, i
     __syncwarp();
     uint32_t issued = 0;
     if (lane < G) {
-        const int i = it * G + lane;
-        if (i < vv.ninputs) issued = issue_frames(vv, cc, i, m0, w_end, sm.stage[s][lane][0], &sm.bar[s], status);
+        const int pos = it * G + lane;
+        if (pos < vv.ninputs)
+            issued = issue_frames(vv, cc, order ? order[pos] : pos, m0, w_end, sm.stage[s][lane][0], &sm.bar[s],
+                                  status);
     } else if (lane == G && wmap) {
         tma_load_5d(sm.wst[s][0][0], wmap, 0, 0, 0, (G / 2) * it, cc, &sm.bar[s]);
         tma_load_5d(sm.wst[s][1][0], wmap, 0, 1, 0, (G / 2) * it, cc, &sm.bar[s]);
@@ -462,47 +466,97 @@ __global__ void __launch_bounds__(kThreads, 2) pack_kernel(const PackArgs a)
     const int I = a.vv.ninputs;
     const int nsteps = (I + kG - 1) / kG;
 
+    // Inputs are taken in the order of their output columns (inv[col] = the
+    // input written there), so each step fills kG adjacent columns of every
+    // (spectrum, channel) row: one 4-byte store in the 4-bit mode, 64
+    // contiguous bytes in the complex-double mode. The per-input results do
+    // not depend on the order.
+    int *inv = reinterpret_cast<int *>(smem_raw + sizeof(FrontSmem));
+    for (int j = tid; j < I; j += kThreads) inv[j] = -1;
+    __syncthreads();
+    for (int i = tid; i < I; i += kThreads) {
+        const int io = __ldg(a.i_idx + i);
+        if (io >= 0 && io < I) inv[io] = i;
+    }
     init_front(sm, tid);
     int hc[2][kP];
     const int li = tid >> 6, n0 = 2 * (tid & 63);
     load_taps(a.filter, n0, hc);
     __syncthreads();
-    if (tid < 32) produce(sm, a.vv, cc, 0, m0, a.nspectra, nullptr, a.status);
+    // i_idx must be a permutation of the inputs: a column nobody writes means
+    // it is not (out of range or repeated)
+    int unset = 0;
+    for (int j = tid; j < I; j += kThreads) unset |= inv[j] < 0;
+    if (__syncthreads_or(unset)) {
+        if (tid == 0) atomicOr(a.status, kErrBadInput);
+        return;
+    }
+    if (tid < 32) produce(sm, a.vv, cc, 0, m0, a.nspectra, nullptr, a.status, inv);
 
     const bool int4 = (a.flags & VGB_PFB_COMPLEX_INT4) != 0;
     const bool imag_first = (a.flags & VGB_PFB_IMAG_PART_FIRST) != 0;
     const int kp = tid & (kK - 1), mh = tid >> 7;
+    // 4-bit mode with 16-byte stores: the last four steps' words of each of
+    // the thread's spectra, oldest in .x, written together every fourth step
+    uint4 held[kT / 2];
+#pragma unroll
+    for (int mi = 0; mi < kT / 2; mi++) held[mi] = make_uint4(0u, 0u, 0u, 0u);
     for (int it = 0; it < nsteps; it++) {
         if (!wait_frames(sm, it, a.status)) {
             drain(sm, it);
             return;
         }
-        if (tid < 32 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, nullptr, a.status);
+        if (tid < 32 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, nullptr, a.status, inv);
         wola_step<kInt32, kFpga>(sm, it & 1, li, n0, hc);
         input_barrier(li);
         fft_step<kDemote, kFpga>(sm, tid);
         __syncthreads();
-#pragma unroll
-        for (int r = 0; r < kG; r++) {
-            const int i = it * kG + r;
-            if (i >= I) break;
-            const int io = __ldg(a.i_idx + i);
-#pragma unroll
-            for (int mi = 0; mi < kT / 2; mi++) {
-                const int ml = mh + 2 * mi;
+        const int col0 = it * kG;              // the step's first output column
+        const int ncol = min(kG, I - col0);
+        if (!int4) {
+            // complex double: four adjacent threads write one (spectrum,
+            // channel) row's 64 contiguous bytes, so each warp store fills
+            // whole sectors
+#pragma unroll 4
+            for (int e = 0; e < kT * kK * kG / kThreads; e++) {
+                const int idx = e * kThreads + tid;
+                const int r = idx & (kG - 1), kc = (idx / kG) % kK, ml = idx / (kG * kK);
                 const int m = m0 + ml;
-                if (m >= a.nspectra) continue;
+                if (r >= ncol || m >= a.nspectra) continue;
+                const float2 v = sm.buf[r * kT + ml][kc];
+                const float hi = imag_first ? v.y : v.x;
+                const float lo = imag_first ? v.x : v.y;
+                static_cast<double2 *>(a.out)[cc * a.out_cc + ((long long)m * kK + kc) * I + col0 + r] =
+                    make_double2((double)hi, (double)lo);
+            }
+            continue;
+        }
+#pragma unroll
+        for (int mi = 0; mi < kT / 2; mi++) {
+            const int ml = mh + 2 * mi;
+            const int m = m0 + ml;
+            if (m >= a.nspectra) continue;
+            const long long o = cc * a.out_cc + ((long long)m * kK + kp) * I + col0;
+            uint32_t word = 0;
+#pragma unroll
+            for (int r = 0; r < kG; r++) {
+                if (r >= ncol) break;
                 // buf holds (im, re)/K: the reference's default output order
                 const float2 v = sm.buf[r * kT + ml][kp];
                 const float hi = imag_first ? v.y : v.x; // first (high / .x) component
                 const float lo = imag_first ? v.x : v.y;
-                const long long o = cc * a.out_cc + ((long long)m * kK + kp) * I + io;
-                if (int4) {
-                    const int h4 = (int)hi & 0xF, l4 = (int)lo & 0xF;
-                    static_cast<uint8_t *>(a.out)[o] = (uint8_t)((h4 << 4) | l4);
-                } else {
-                    static_cast<double2 *>(a.out)[o] = make_double2((double)hi, (double)lo);
-                }
+                const int h4 = (int)hi & 0xF, l4 = (int)lo & 0xF;
+                const uint32_t b = (uint32_t)((h4 << 4) | l4);
+                if (a.word_stores) word |= b << (8 * r);
+                else static_cast<uint8_t *>(a.out)[o + r] = (uint8_t)b;
+            }
+            if (a.vec_stores) {
+                // I is a multiple of 16, so the steps come in whole groups of
+                // four and every fourth step completes 16 aligned columns
+                held[mi] = make_uint4(held[mi].y, held[mi].z, held[mi].w, word);
+                if ((it & 3) == 3) *reinterpret_cast<uint4 *>(static_cast<uint8_t *>(a.out) + o - 12) = held[mi];
+            } else if (a.word_stores) {
+                *reinterpret_cast<uint32_t *>(static_cast<uint8_t *>(a.out) + o) = word;
             }
         }
     }
@@ -608,9 +662,12 @@ template <bool A, bool B, bool C> struct BeamSel {
 template <bool A, bool B, bool C> struct PackSel {
     static int run(const PackArgs &a, dim3 grid, cudaStream_t st)
     {
-        int rc = prep<kG>(pack_kernel<A, B, C>);
+        const size_t smem = front_smem<kG>() + sizeof(int) * (size_t)kPackMaxInputs;
+        int rc = check_cuda(cudaFuncSetAttribute(pack_kernel<A, B, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem),
+                            "cudaFuncSetAttribute(pack smem)");
         if (rc) return rc;
-        pack_kernel<A, B, C><<<grid, kThreads, front_smem<kG>(), st>>>(a);
+        pack_kernel<A, B, C><<<grid, kThreads, smem, st>>>(a);
         return check_launch("pack_kernel");
     }
 };

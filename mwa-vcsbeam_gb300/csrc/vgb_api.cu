@@ -153,7 +153,8 @@ int vgb_check_device_status(void *stream, unsigned *flags_out)
         return set_error(VGB_ERR_DEVICE, "kernel status 0x%x%s%s%s", h,
                          (h & kErrWaitTimeout) ? " (bounded wait expired)" : "",
                          (h & kErrBadFrame) ? " (frame outside the voltage buffers)" : "",
-                         (h & kErrBadInput) ? " (polQ/polP input index outside the voltage row)" : "");
+                         (h & kErrBadInput) ? " (an input index outside the voltage row, or an input map that is not a permutation)"
+                                              : "");
     return VGB_SUCCESS;
 }
 
@@ -233,8 +234,12 @@ int vgb_fpfb(const vgb_voltages *v, int ncc, int nspectra, const int32_t *filter
     if ((rc = to_view(v, ncc, nspectra, a.vv))) return rc;
     if (ncc <= 0) return set_error(VGB_ERR_INVALID, "ncc must be positive");
     if (!filter || !i_idx || !out) return set_error(VGB_ERR_INVALID, "filter, i_idx and out must not be NULL");
+    if (v->ninputs > kPackMaxInputs)
+        return set_error(VGB_ERR_UNSUPPORTED, "fpfb: at most %d inputs (got %d)", kPackMaxInputs, v->ninputs);
     a.filter = filter;
     a.i_idx = i_idx;
+    a.word_stores = v->ninputs % 4 == 0 && (reinterpret_cast<uintptr_t>(out) & 3) == 0;
+    a.vec_stores = v->ninputs % 16 == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
     a.nspectra = nspectra;
     a.flags = pfb_flags;
     a.out = out;

@@ -37,8 +37,13 @@ struct PackArgs {
     unsigned flags;         // PFB_COMPLEX_INT4 / PFB_IMAG_PART_FIRST
     void *out;              // [cc][s][K][I] uint8 or double2
     long long out_cc;       // elements between coarse channels
-    unsigned *status;
+    unsigned *status;       // kErrBadInput when i_idx is not a permutation of the inputs
+    bool word_stores;       // 4-bit mode: out and I allow one aligned 4-byte store per 4 columns
+    bool vec_stores;        // ... and one aligned 16-byte store per 16 columns
 };
+// Largest input count of the packing PFB (its inverse input map lives in
+// shared memory).
+constexpr int kPackMaxInputs = 1024;
 
 struct RenormArgs {
     const float *S;        // [cc][p][nstep][nstokes][nchan]

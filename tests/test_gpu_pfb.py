@@ -166,3 +166,12 @@ def test_rejects_bad_arguments(vgb_mod, torch, golden):
     v = vgb_mod.reference_buffer_voltages(d, I_IN, 1)
     with pytest.raises(vgb_mod.VGBError, match="nspectra"):
         vgb_mod.fpfb(v, 1, 501, dev(golden["filter"]), dev(golden["i_idx"]), vgb_mod.PFB_SMART, out)
+    # an input map that repeats a column is not a permutation: flagged, nothing written
+    bad = np.array(golden["i_idx"], dtype=np.int32)
+    bad[5] = bad[6]
+    out.fill_(0x5A)
+    vgb_mod.fpfb(v, 1, 64, dev(golden["filter"]), dev(bad), vgb_mod.PFB_SMART, out)
+    torch.cuda.synchronize()
+    with pytest.raises(vgb_mod.VGBError, match="permutation"):
+        vgb_mod.check_device_status()
+    assert (host(out) == 0x5A).all()
