@@ -319,6 +319,39 @@ def gb300_arm(args, rank, local_rank, world):
                   "stage_ms": {"pfb_beam": bstage[0], "renormalise": bstage[1], "ipfb_vdif": bstage[2],
                                "history": bstage[3]}}
 
+    # ---- the PFB alone (fine_pfb_offline: vmExecuteForwardPFB's packed
+    # legacy-order output), 8 coarse channels from the reference's read
+    # buffer layout, both output types --------------------------------------
+    pfb_only = None
+    if args.pfb_only:
+        npc = min(8, ncc)
+        blk = NI * 64000 * 2
+        rbuf = torch.randint(-127, 128, (npc, (NBLK + 1) * blk), dtype=torch.int8, device="cuda")
+        rv = vgb.reference_buffer_voltages(rbuf, NI, NBLK, npc, (NBLK + 1) * blk)
+        dfilt = torch.from_numpy(h.astype(np.int32)).cuda()
+        didx = torch.from_numpy(SY.legacy_input_order(NANT).astype(np.int32)).cuda()
+        pfb_only = {"workload": f"{npc} coarse channels x 1 s, 128 tiles, packed to the legacy order "
+                                "(vgb_fpfb; the reference's fine_pfb_offline)"}
+        for name, flags, dt, per in (("smart_int4", vgb.PFB_SMART | vgb.WOLA_FP32, torch.uint8, 1),
+                                     ("full_precision_complex_double", vgb.PFB_FULL_PRECISION | vgb.WOLA_FP32,
+                                      torch.float64, 2)):
+            pout = torch.empty(npc * NSPEC * K * NI * per, dtype=dt, device="cuda")
+            for _ in range(2):
+                vgb.fpfb(rv, npc, NSPEC, dfilt, didx, flags, pout, stream=stream)
+            e0p, e1p = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0p.record(stream)
+            for _ in range(3):
+                vgb.fpfb(rv, npc, NSPEC, dfilt, didx, flags, pout, stream=stream)
+            e1p.record(stream)
+            e1p.synchronize()
+            ms = e0p.elapsed_time(e1p) / 3 / npc
+            nbytes = pout.numel() * pout.element_size() / npc
+            pfb_only[name] = {"ms_per_cc_s": ms, "rtf_24cc": 1e3 / (ms * NCC),
+                              "write_gbs": nbytes / (ms * 1e-3) / 1e9}
+            del pout
+        del rbuf
+        torch.cuda.empty_cache()
+
     # ---- end to end through the host API ------------------------------------
     psr_b, vdif_b, stat_b = out_bytes(ncc)
     e2e = None
@@ -393,6 +426,8 @@ def gb300_arm(args, rank, local_rank, world):
                                       "and second parity); stage_ms from a separate eager pass with events"},
             "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
             "smart_mode": smart_mode, "int32_wola": int32_wola}
+    if pfb_only is not None:
+        line["pfb_only"] = pfb_only
     if mb_section is not None:
         mb_section["gpu_launches"] = mb_launches
         line["multibeam"] = mb_section
@@ -742,6 +777,8 @@ def main():
     ap.add_argument("--mb-modes", default=None, help="profiling: comma-separated precision modes")
     ap.add_argument("--mb-nfine", type=int, default=K, help="profiling: fine channels per case")
     ap.add_argument("--mb-stream-iters", type=int, default=3, help="many-beam host-streaming calls timed (0: skip)")
+    ap.add_argument("--no-pfb-only", dest="pfb_only", action="store_false",
+                    help="skip the PFB-only (fine_pfb_offline) section")
     ap.add_argument("--pfb-variant", type=int, default=0, choices=[0, 4, 8],
                     help="profiling: force the fused front end's inputs per step (0 = timed choice)")
     ap.add_argument("--beam-sweep", action="store_true",
