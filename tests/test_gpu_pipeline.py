@@ -284,3 +284,32 @@ def test_pipeline_nan_channel(vgb_mod, torch, oracle_mod, setup):
             assert np.array_equal(off[cc], o[0], equal_nan=True) and np.array_equal(sc[cc], s[0], equal_nan=True)
         assert np.isnan(off[0, :, 17]).all()
     p.close()
+
+
+def test_pipeline_stokes_i_only(vgb_mod, torch, oracle_mod, setup):
+    """Stokes I only (nstokes = 1): the gathered extremes and the spliced
+    PSRFITS rows use the one-parameter layout; bytes, offsets and scales equal
+    the oracle's renormalise of the device's own Stokes, and the Stokes equal
+    the full-Stokes pipeline's I."""
+    from helpers import weights_on_device
+
+    volt, filt, syn, tabs = setup
+    W = torch.cat([weights_on_device(J, phi) for J, phi in tabs])
+    S = {}
+    for nst in (1, 4):
+        p = vgb_mod.Pipeline(NCC, NANT, NBLK, nstokes=nst, pfb_flags=0, do_ipfb=False, invw=1.0 / NI)
+        p.set_filters(filt, syn)
+        p.set_weights(W, on_device=True)
+        p.run_device(dev(volt[0].reshape(-1).view(np.uint8)))
+        ps = np.empty((NS, nst, NCC * K), np.uint8)
+        off = np.empty((NCC, nst, K), np.float32)
+        sc = np.empty((NCC, nst, K), np.float32)
+        p.fetch(ps, off, sc, None)
+        S[nst] = np.empty((NCC, NS, nst, K), np.float32)
+        p.fetch_raw(S[nst], None)
+        p.close()
+        for cc in range(NCC):
+            o, s, u = oracle_mod.renormalise(S[nst][cc][None])
+            assert np.array_equal(ps[:, :, cc * K:(cc + 1) * K], u[0]), (nst, cc)
+            assert np.array_equal(off[cc], o[0]) and np.array_equal(sc[cc], s[0]), (nst, cc)
+    assert np.array_equal(S[1][:, :, 0], S[4][:, :, 0])
