@@ -3,7 +3,7 @@
 Each CUDA translation unit in csrc/ is compiled for sm_103a only, in
 parallel, and linked into ``mwa-vcsbeam_gb300/lib/libvcsbeam_gb300.so``
 (git-ignored). Plain nvcc, no cmake, no torch extension machinery: the
-library exposes a C ABI (include/vcsbeam_gb300.h, include/vcsbeam.h).
+library exposes a C ABI (include/vcsbeam_gb300.h).
 """
 from __future__ import annotations
 
