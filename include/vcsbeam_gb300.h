@@ -305,8 +305,15 @@ int vgb_vdif_advance(uint32_t *d_hdr, int njobs, int nframes, void *stream);
  * with VGB_ERR_INVALID.
  *   out      [ncc][nspectra][nstokes][128] bytes (C_IDX per channel)
  *   offsets, scales  [ncc][nstokes][128]
- * The first call on each device looks up the array's device address (with
- * that device current); make that first call before any stream capture.
+ * The array is placed on a device when the library's module holding it is
+ * first used there, which (under CUDA's default lazy module loading) is the
+ * first call on that device: make one call on each device before reserving
+ * the GPU's memory and before any stream capture. A call with nspectra = 0
+ * does only that set-up (its other pointers may be NULL). Setting
+ * CUDA_MODULE_LOADING=EAGER places the array when the library loads instead.
+ * The first call for each new shape also times the fused front end's two
+ * tile shapes once (extra launches and a wait on CUDA events, see
+ * vgb_pfb_variant); force one with vgb_pfb_variant(4) to skip that.
  * All calls share the one array, which keeps the last call's contents.
  * Nothing in it needs to start at zero, because each call writes every
  * value it reads. Calls that overlap on the GPU (e.g. on different streams)
@@ -545,8 +552,38 @@ int vgb_pipeline_create(const vgb_pipeline_config *cfg, vgb_pipeline **out);
 int vgb_pipeline_destroy(vgb_pipeline *p);
 /* Analysis taps (K*P int32) and, when do_ipfb, synthesis taps (K*P float). */
 int vgb_pipeline_set_filters(vgb_pipeline *p, const int32_t *analysis, const float *synthesis);
-/* W [ncc][nant][128][2][2] complex float on the host or device. */
+/* W [ncc][nant][128][2][2] complex float on the host or device (fixed
+ * weights; turns per-second tracking off). */
 int vgb_pipeline_set_weights(vgb_pipeline *p, const void *W, int on_device);
+/*
+ * Per-second tracking: every second, before its beamformer, the pipeline
+ * rebuilds W on the device from these tables, as vmCalcJonesAndDelays does
+ * on the host each second (jones.c:170-188, called from
+ * app/make_mwa_tied_array_beam.c:256-262): the second's pointing (the
+ * per-second az/za the caller derives from RA/Dec, e.g. with calc_beam_geom,
+ * geometry.c:226-286; the unit vector is formed from az and el = pi/2 - za
+ * as there), B = vgb_primary_beam at each coarse channel's beam frequency,
+ * J^-1 = inv(norm_F(D B)) (vmCalcJ), phi at the fine-channel frequencies
+ * (vmCalcPhi) and W = phi J^-1, all FP64 with the arithmetic of vgb_phase /
+ * vgb_jones / vgb_weights, W rounded to FP32. Five small launches inside each
+ * captured second. Second s of the pipeline (counting from 0, including
+ * seconds restored by vgb_pipeline_load_state) uses entry min(s, nseconds-1).
+ * All pointers are device pointers that must stay valid while tracking is
+ * on; NULL `t` turns tracking off (so does vgb_pipeline_set_weights).
+ */
+typedef struct vgb_tracking {
+    const double *D;             /* [ncc][nant][128][2][2] complex double (D_IDX per coarse channel) */
+    const uint32_t *delays;      /* [nant][16] dipole delays 0..31, 32 = dead dipole */
+    const double *east, *north, *height, *cable;  /* [nant] metres */
+    const double *chan_freqs_hz; /* [ncc][128] fine-channel frequencies for phi (geometry.c:152-163) */
+    const double *beam_freqs_hz; /* [ncc] frequency B is evaluated at (the coarse channel's, primary_beam.c:224) */
+    const double *az, *za;       /* [nseconds] pointing of each second, radians */
+    int nseconds;
+    int pa_correction;           /* parallactic-angle rotation of B (primary_beam.c:436-456) */
+    double href;                 /* array reference height, metres */
+    double latitude;             /* array latitude, radians */
+} vgb_tracking;
+int vgb_pipeline_set_tracking(vgb_pipeline *p, const vgb_tracking *t);
 /* VDIF header template of the next second's first frame, [ncc][8] uint32 on
  * the host (optional; zeros by default). After every second the pipeline
  * advances the templates by that second's frames (vgb_vdif_advance), so the
@@ -604,7 +641,8 @@ long long vgb_pipeline_state_bytes(const vgb_pipeline *p);
 int vgb_pipeline_save_state(vgb_pipeline *p, void *host, long long bytes);
 int vgb_pipeline_load_state(vgb_pipeline *p, const void *host, long long bytes);
 /* Milliseconds per stage of the last second: [0] fused PFB + beamformer,
- * [1] renormalise, [2] inverse PFB + VDIF, [3] history carry. Synchronises. */
+ * [1] renormalise, [2] inverse PFB + VDIF, [3] history carry, [4] tracking
+ * tables (n = 5; 0 when tracking is off). Synchronises. */
 int vgb_pipeline_stage_ms(vgb_pipeline *p, float *ms, int n);
 
 #ifdef __cplusplus

@@ -116,12 +116,15 @@ __global__ void beam_expand_kernel(const PbArgs a, const int *rep)
     dst[3] = src[3];
 }
 
-int launch_beam_model(const PbArgs &a, cudaStream_t st)
+int launch_beam_model(const PbArgs &a, cudaStream_t st, int *given)
 {
     const long long n = (long long)a.nfreq * a.npointing * a.ntile;
     if (n <= 0) return VGB_SUCCESS;
-    int *scratch = nullptr; // rep [ntile], list [ntile], count
-    int rc = check_cuda(cudaMallocAsync(reinterpret_cast<void **>(&scratch), (2 * (size_t)a.ntile + 1) * sizeof(int), st),
+    int *scratch = given; // rep [ntile], list [ntile], count
+    int rc = VGB_SUCCESS;
+    if (!given)
+        rc = check_cuda(cudaMallocAsync(reinterpret_cast<void **>(&scratch), (2 * (size_t)a.ntile + 1) * sizeof(int),
+                                        st),
                         "cudaMallocAsync(beam configurations)");
     if (rc) return rc;
     int *rep = scratch, *list = scratch + a.ntile, *count = scratch + 2 * a.ntile;
@@ -135,6 +138,7 @@ int launch_beam_model(const PbArgs &a, cudaStream_t st)
         beam_expand_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a, rep);
         rc = check_launch("beam_expand_kernel");
     }
+    if (given) return rc;
     const int rf = check_cuda(cudaFreeAsync(scratch, st), "cudaFreeAsync(beam configurations)");
     return rc ? rc : rf;
 }

@@ -27,7 +27,21 @@ __device__ __forceinline__ double2 zadd(double2 a, double2 b) { return make_doub
 __device__ __forceinline__ double2 zsub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 
 // geometry.c:40-101 for one (pointing, tile, channel): phase terms use the
-// reference's order of operations, 2*pi*dt*f.
+// reference's order of operations, 2*pi*dt*f. `u` is the pointing's (E, N, H)
+// unit vector; the frequency is cast to whole Hz as the reference's is.
+__device__ __forceinline__ double2 geometric_phase(const double *u, double east, double north, double height,
+                                                   double cable, double href, double freq)
+{
+    const double L = cable - 0.0;
+    const double w = (east - 0.0) * u[0] + (north - 0.0) * u[1] + (height - href) * u[2];
+    const double dt = (w - L) / 299792458.0;
+    const double f = (double)(uint32_t)freq;
+    const double phase = 2.0 * 3.14159265358979323846 * dt * f;
+    double s, co;
+    sincos(phase, &s, &co);
+    return make_double2(co, s);
+}
+
 __global__ void phase_kernel(const double *unit, const double *east, const double *north, const double *height,
                              const double *cable, const double *freqs, int npointing, int nant, int nchan,
                              double href, double2 *phi)
@@ -38,15 +52,7 @@ __global__ void phase_kernel(const double *unit, const double *east, const doubl
     const int c = idx % nchan;
     const int a = (idx / nchan) % nant;
     const int p = idx / ((long long)nchan * nant);
-    const double L = cable[a] - 0.0;
-    const double w = (east[a] - 0.0) * unit[3 * p + 0] + (north[a] - 0.0) * unit[3 * p + 1] +
-                     (height[a] - href) * unit[3 * p + 2];
-    const double dt = (w - L) / 299792458.0;
-    const double f = (double)(uint32_t)freqs[c];
-    const double phase = 2.0 * 3.14159265358979323846 * dt * f;
-    double s, co;
-    sincos(phase, &s, &co);
-    phi[idx] = make_double2(co, s);
+    phi[idx] = geometric_phase(unit + 3 * p, east[a], north[a], height[a], cable[a], href, freqs[c]);
 }
 
 // geometry.c:440-467 (calc_array_factor; Eq. A4 of Meyers et al. 2017): the
@@ -98,16 +104,10 @@ int launch_array_factor(const double *look, const double *dirs, int npix, double
 }
 
 // jones.c:97-157: J = inv2x2S(D[a][c] B[p][a] / ||D B||_F), zero if the norm is 0.
-__global__ void jones_kernel(const double2 *D, const double2 *B, int npointing, int nant, int nchan, double2 *J)
+// jones.c:97-157 for one (pointing, tile, channel): J = D B normalised by
+// its Frobenius norm, then inverted (zero when the norm is zero).
+__device__ __forceinline__ void inverse_jones(const double2 *d, const double2 *b, double2 (&o)[4])
 {
-    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long n = (long long)npointing * nant * nchan;
-    if (idx >= n) return;
-    const int c = idx % nchan;
-    const int a = (idx / nchan) % nant;
-    const int p = idx / ((long long)nchan * nant);
-    const double2 *d = D + 4 * ((long long)a * nchan + c);
-    const double2 *b = B + 4 * ((long long)p * nant + a);
     double2 m[4];
     m[0] = zadd(zmul(d[0], b[0]), zmul(d[1], b[2]));
     m[1] = zadd(zmul(d[0], b[1]), zmul(d[1], b[3]));
@@ -116,7 +116,6 @@ __global__ void jones_kernel(const double2 *D, const double2 *B, int npointing, 
     double F = 0.0;
     for (int i = 0; i < 4; i++) F += zmul(m[i], make_double2(m[i].x, -m[i].y)).x;
     F = sqrt(F);
-    double2 *o = J + 4 * idx;
     if (F == 0.0) {
         for (int i = 0; i < 4; i++) o[i] = make_double2(0.0, 0.0);
         return;
@@ -132,18 +131,102 @@ __global__ void jones_kernel(const double2 *D, const double2 *B, int npointing, 
     o[3] = zmul(inv, m[0]);
 }
 
-// W[p][a][c] = phi[p][a][c] * J[p][a][c] in FP64, rounded to FP32 and stored
-// as two float4: (w00, w01), (w10, w11).
+// W = phi J in FP64, rounded to FP32 and stored as two float4:
+// (w00, w01), (w10, w11).
+__device__ __forceinline__ void store_weight(double2 ph, const double2 (&j)[4], float4 *W)
+{
+    double2 w[4];
+    for (int i = 0; i < 4; i++) w[i] = zmul(ph, j[i]);
+    W[0] = make_float4((float)w[0].x, (float)w[0].y, (float)w[1].x, (float)w[1].y);
+    W[1] = make_float4((float)w[2].x, (float)w[2].y, (float)w[3].x, (float)w[3].y);
+}
+
+__global__ void jones_kernel(const double2 *D, const double2 *B, int npointing, int nant, int nchan, double2 *J)
+{
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long n = (long long)npointing * nant * nchan;
+    if (idx >= n) return;
+    const int c = idx % nchan;
+    const int a = (idx / nchan) % nant;
+    const int p = idx / ((long long)nchan * nant);
+    double2 o[4];
+    inverse_jones(D + 4 * ((long long)a * nchan + c), B + 4 * ((long long)p * nant + a), o);
+    for (int i = 0; i < 4; i++) J[4 * idx + i] = o[i];
+}
+
+// W[p][a][c] = phi[p][a][c] * J[p][a][c].
 __global__ void weights_kernel(const double2 *J, const double2 *phi, long long n, float4 *W)
 {
     const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (idx >= n) return;
-    const double2 ph = phi[idx];
-    const double2 *j = J + 4 * idx;
-    double2 w[4];
-    for (int i = 0; i < 4; i++) w[i] = zmul(ph, j[i]);
-    W[2 * idx] = make_float4((float)w[0].x, (float)w[0].y, (float)w[1].x, (float)w[1].y);
-    W[2 * idx + 1] = make_float4((float)w[2].x, (float)w[2].y, (float)w[3].x, (float)w[3].y);
+    const double2 j[4] = {J[4 * idx], J[4 * idx + 1], J[4 * idx + 2], J[4 * idx + 3]};
+    store_weight(phi[idx], j, W + 2 * idx);
+}
+
+// ---------------------------------------------------------------------------
+// Per-second tracking (vmCalcJonesAndDelays, jones.c:170-188): the pointing
+// of the current second, then B (primary-beam kernel), then J^-1, phi and
+// W = phi J^-1 for every (coarse channel, tile, fine channel) in one pass.
+// ---------------------------------------------------------------------------
+
+// One thread: the second's pointing from the per-second table (the last entry
+// holds past its end), its (E, N, H) unit vector as calc_beam_geom sets it
+// (geometry.c:226-286, from az and el = pi/2 - za), and the counter stepped
+// for the next second.
+__global__ void track_select_kernel(const double *az_tab, const double *za_tab, int nseconds,
+                                    long long *counter, double *cur)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const long long s = *counter;
+    const int i = (int)(s < nseconds ? s : nseconds - 1);
+    const double az = az_tab[i], za = za_tab[i];
+    const double el = 0.5 * 3.14159265358979323846 - za;
+    double saz, caz, sel, cel;
+    sincos(az, &saz, &caz);
+    sincos(el, &sel, &cel);
+    cur[0] = az;
+    cur[1] = za;
+    cur[2] = cel * saz; // E
+    cur[3] = cel * caz; // N
+    cur[4] = sel;       // H
+    *counter = s + 1;
+}
+
+// One thread per (cc, tile, fine channel): D [cc][a][c][2][2], B [cc][a][2][2]
+// (one pointing, the coarse channel's beam frequency), freqs [cc][c].
+__global__ void track_weights_kernel(const double2 *D, const double2 *B, const double *unit, const double *east,
+                                     const double *north, const double *height, const double *cable,
+                                     const double *freqs, int ncc, int nant, int nchan, double href, float4 *W)
+{
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long n = (long long)ncc * nant * nchan;
+    if (idx >= n) return;
+    const int c = idx % nchan;
+    const int a = (idx / nchan) % nant;
+    const int cc = idx / ((long long)nchan * nant);
+    double2 j[4];
+    inverse_jones(D + 4 * idx, B + 4 * ((long long)cc * nant + a), j);
+    const double2 ph = geometric_phase(unit, east[a], north[a], height[a], cable[a], href,
+                                       freqs[(long long)cc * nchan + c]);
+    store_weight(ph, j, W + 2 * idx);
+}
+
+int launch_track_select(const double *az_tab, const double *za_tab, int nseconds, long long *counter, double *cur,
+                        cudaStream_t st)
+{
+    track_select_kernel<<<1, 32, 0, st>>>(az_tab, za_tab, nseconds, counter, cur);
+    return check_launch("track_select_kernel");
+}
+
+int launch_track_weights(const double2 *D, const double2 *B, const double *unit, const double *east,
+                         const double *north, const double *height, const double *cable, const double *freqs,
+                         int ncc, int nant, int nchan, double href, float4 *W, cudaStream_t st)
+{
+    const long long n = (long long)ncc * nant * nchan;
+    if (n == 0) return VGB_SUCCESS;
+    track_weights_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(D, B, unit, east, north, height, cable, freqs,
+                                                                      ncc, nant, nchan, href, W);
+    return check_launch("track_weights_kernel");
 }
 
 int launch_phase(const double *unit, const double *east, const double *north, const double *height,

@@ -466,9 +466,18 @@ struct vgb_pipeline {
     // asynchronous host outputs
     uint8_t *h_psrfits = nullptr, *h_vdif = nullptr;
     float *h_off = nullptr, *h_scl = nullptr;
-    // per-stage timing
+    // per-second tracking (vmCalcJonesAndDelays): caller's device tables and
+    // the pipeline's own second counter, pointing, B and beam-model scratch
+    bool tracking = false;
+    vgb_tracking trk{};
+    long long *d_trk_counter = nullptr;
+    double *d_trk_cur = nullptr;     // az, za, unit E, N, H of the current second
+    double2 *d_trk_B = nullptr;      // [cc][nant][2][2]
+    int *d_trk_scratch = nullptr;    // 2*nant + 1
+    // per-stage timing: events 0..4 bound the four stages, event 5 precedes
+    // the tracking tables
     bool timing = false;
-    cudaEvent_t ev_stage[5] = {};
+    cudaEvent_t ev_stage[6] = {};
     // CUDA graphs of one second, keyed by what the captured launches bake in
     struct Graph {
         const void *volt;
@@ -534,6 +543,23 @@ int pipeline_second(vgb_pipeline *p, const char2 *volt, long long cc_stride_byte
     auto mark = [&](int i) {
         return p->timing ? check_cuda(cudaEventRecord(p->ev_stage[i], p->s_comp), "stage event") : VGB_SUCCESS;
     };
+    if ((rc = mark(5))) return rc;
+    if (p->tracking) {
+        // the second's pointing, B at each coarse channel's beam frequency,
+        // then J^-1, phi and W for every (cc, tile, channel)
+        const vgb_tracking &t = p->trk;
+        rc = launch_track_select(t.az, t.za, t.nseconds, p->d_trk_counter, p->d_trk_cur, p->s_comp);
+        if (rc) return rc;
+        PbArgs pb{p->d_trk_cur, p->d_trk_cur + 1, 1, t.beam_freqs_hz, c.ncc, t.delays, c.nant, t.latitude,
+                  t.pa_correction, p->d_trk_B};
+        rc = launch_beam_model(pb, p->s_comp, p->d_trk_scratch);
+        if (rc) return rc;
+        rc = launch_track_weights(reinterpret_cast<const double2 *>(t.D), p->d_trk_B, p->d_trk_cur + 2, t.east,
+                                  t.north, t.height, t.cable, t.chan_freqs_hz, c.ncc, c.nant, kK, t.href, p->d_W,
+                                  p->s_comp);
+        if (rc) return rc;
+        p->launches += 5;
+    }
     if ((rc = mark(0))) return rc;
     rc = beamform_mwax_impl(&v, c.ncc, p->nspectra, p->d_filter, kP, kK, flags, p->d_W, c.nant, c.invw, c.nstokes,
                             p->d_S, p->d_e, p->d_incoh, p->d_rstat, p->s_comp);
@@ -670,7 +696,7 @@ int vgb_pipeline_create(const vgb_pipeline_config *cfg, vgb_pipeline **out)
     int rc = VGB_SUCCESS;
     rc = rc ? rc : check_cuda(cudaStreamCreateWithFlags(&p->s_comp, cudaStreamNonBlocking), "stream");
     rc = rc ? rc : check_cuda(cudaStreamCreateWithFlags(&p->s_copy, cudaStreamNonBlocking), "stream");
-    for (int i = 0; i < 5 && !rc; i++) rc = check_cuda(cudaEventCreate(&p->ev_stage[i]), "event");
+    for (int i = 0; i < 6 && !rc; i++) rc = check_cuda(cudaEventCreate(&p->ev_stage[i]), "event");
     for (int b = 0; b < 2 && !rc; b++) {
         rc = check_cuda(cudaEventCreateWithFlags(&p->ev_copied[b], cudaEventDisableTiming), "event");
         rc = rc ? rc : check_cuda(cudaEventCreateWithFlags(&p->ev_consumed[b], cudaEventDisableTiming), "event");
@@ -691,6 +717,10 @@ int vgb_pipeline_create(const vgb_pipeline_config *cfg, vgb_pipeline **out)
     if (cfg->do_ipfb) rc = rc ? rc : dalloc(&p->d_vdif, (size_t)ncc * ns * 544);
     rc = rc ? rc : dalloc(&p->d_hdr, sizeof(uint32_t) * 8 * ncc);
     rc = rc ? rc : dalloc(&p->d_rstat, sizeof(uint32_t) * 3 * ncc * cfg->nstokes * kK);
+    rc = rc ? rc : dalloc(&p->d_trk_counter, sizeof(long long));
+    rc = rc ? rc : dalloc(&p->d_trk_cur, sizeof(double) * 8);
+    rc = rc ? rc : dalloc(&p->d_trk_B, sizeof(double2) * 4 * ncc * cfg->nant);
+    rc = rc ? rc : dalloc(&p->d_trk_scratch, sizeof(int) * (2 * (size_t)cfg->nant + 1));
     if (!rc) {
         for (int b = 0; b < 2 && !rc; b++)
             rc = check_cuda(cudaMemsetAsync(p->d_hist[b], 0, (size_t)ncc * p->ninputs * kHistFrames * kK * 2,
@@ -698,6 +728,7 @@ int vgb_pipeline_create(const vgb_pipeline_config *cfg, vgb_pipeline **out)
                             "memset history");
         rc = rc ? rc : check_cuda(cudaMemsetAsync(p->d_hdr, 0, sizeof(uint32_t) * 8 * ncc, p->s_comp), "memset hdr");
         rc = rc ? rc : reset_rstat(p);
+        rc = rc ? rc : check_cuda(cudaMemsetAsync(p->d_trk_counter, 0, sizeof(long long), p->s_comp), "memset");
         rc = rc ? rc : check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
     }
     if (rc) {
@@ -721,10 +752,11 @@ int vgb_pipeline_destroy(vgb_pipeline *p)
     drop_graphs(p);
     void *bufs[] = {p->d_filter, p->d_coeffs, p->d_W, p->d_volt[0], p->d_volt[1], p->d_hist[0], p->d_hist[1],
                     p->d_S, p->d_e, p->d_incoh, p->d_ehist[0], p->d_ehist[1], p->d_psrfits, p->d_off, p->d_scl,
-                    p->d_vdif, p->d_hdr, p->d_rstat};
+                    p->d_vdif, p->d_hdr, p->d_rstat, p->d_trk_counter, p->d_trk_cur, p->d_trk_B,
+                    p->d_trk_scratch};
     for (void *b : bufs)
         if (b) cudaFree(b);
-    for (int i = 0; i < 5; i++)
+    for (int i = 0; i < 6; i++)
         if (p->ev_stage[i]) cudaEventDestroy(p->ev_stage[i]);
     for (int b = 0; b < 2; b++) {
         if (p->ev_copied[b]) cudaEventDestroy(p->ev_copied[b]);
@@ -751,9 +783,36 @@ int vgb_pipeline_set_filters(vgb_pipeline *p, const int32_t *analysis, const flo
     return rc ? rc : check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
 }
 
+int vgb_pipeline_set_tracking(vgb_pipeline *p, const vgb_tracking *t)
+{
+    if (!p) return set_error(VGB_ERR_INVALID, "NULL pipeline");
+    int rc = check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
+    if (rc) return rc;
+    drop_graphs(p); // the captured seconds did (or did not) rebuild W
+    if (!t) {
+        p->tracking = false;
+        return VGB_SUCCESS;
+    }
+    if (!t->D || !t->delays || !t->east || !t->north || !t->height || !t->cable || !t->chan_freqs_hz ||
+        !t->beam_freqs_hz || !t->az || !t->za)
+        return set_error(VGB_ERR_INVALID, "pipeline_set_tracking: NULL table");
+    if (t->nseconds <= 0) return set_error(VGB_ERR_INVALID, "pipeline_set_tracking: nseconds %d", t->nseconds);
+    if ((reinterpret_cast<uintptr_t>(t->delays) | reinterpret_cast<uintptr_t>(t->D)) & 15)
+        return set_error(VGB_ERR_INVALID, "pipeline_set_tracking: D and delays must be 16-byte aligned");
+    p->trk = *t;
+    p->tracking = true;
+    // the table index follows the pipeline's second counter
+    const long long s = p->second;
+    return check_cuda(cudaMemcpy(p->d_trk_counter, &s, sizeof(s), cudaMemcpyHostToDevice), "tracking counter");
+}
+
 int vgb_pipeline_set_weights(vgb_pipeline *p, const void *W, int on_device)
 {
     if (!p || !W) return set_error(VGB_ERR_INVALID, "NULL argument");
+    if (p->tracking) {
+        int rc = vgb_pipeline_set_tracking(p, nullptr);
+        if (rc) return rc;
+    }
     const size_t bytes = sizeof(float4) * 2 * p->cfg.ncc * p->cfg.nant * kK;
     return check_cuda(cudaMemcpyAsync(p->d_W, W, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                       p->s_comp),
@@ -849,6 +908,9 @@ int vgb_pipeline_load_state(vgb_pipeline *p, const void *host, long long bytes)
         rc = check_cuda(cudaMemcpy(p->d_hdr, in + sizeof(h) + state_hist_bytes(p) + state_ehist_bytes(p),
                                    state_hdr_bytes(p), cudaMemcpyHostToDevice),
                         "load VDIF headers");
+    if (!rc)
+        rc = check_cuda(cudaMemcpy(p->d_trk_counter, &h.second, sizeof(long long), cudaMemcpyHostToDevice),
+                        "load tracking counter");
     return rc;
 }
 
@@ -993,6 +1055,7 @@ int vgb_pipeline_stage_ms(vgb_pipeline *p, float *ms, int n)
     int rc = check_cuda(cudaEventSynchronize(p->ev_stage[4]), "sync stage events");
     for (int i = 0; i < n && i < 4 && !rc; i++)
         rc = check_cuda(cudaEventElapsedTime(&ms[i], p->ev_stage[i], p->ev_stage[i + 1]), "stage time");
+    if (!rc && n > 4) rc = check_cuda(cudaEventElapsedTime(&ms[4], p->ev_stage[5], p->ev_stage[0]), "stage time");
     return rc;
 }
 

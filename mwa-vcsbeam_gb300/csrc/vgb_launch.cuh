@@ -104,6 +104,14 @@ int launch_phase(const double *unit, const double *east, const double *north, co
 int launch_jones(const double2 *D, const double2 *B, int npointing, int nant, int nchan, double2 *J,
                  cudaStream_t st);
 int launch_weights(const double2 *J, const double2 *phi, long long n, float4 *W, cudaStream_t st);
+// Per-second tracking: the second's pointing cur[5] = (az, za, E, N, H) from
+// the per-second tables at *counter (then stepped), and W [cc][a][c] from
+// D [cc][a][c], B [cc][a] and freqs [cc][c].
+int launch_track_select(const double *az_tab, const double *za_tab, int nseconds, long long *counter, double *cur,
+                        cudaStream_t st);
+int launch_track_weights(const double2 *D, const double2 *B, const double *unit, const double *east,
+                         const double *north, const double *height, const double *cable, const double *freqs,
+                         int ncc, int nant, int nchan, double href, float4 *W, cudaStream_t st);
 int launch_renorm(const RenormArgs &a, int ncc, cudaStream_t st);
 int launch_incoh(const uint8_t *data, long long nrows, int ninput, float *incoh, cudaStream_t st);
 int launch_legacy_beam(const LegacyArgs &a, cudaStream_t st);
@@ -124,7 +132,9 @@ struct PbArgs { // primary-beam model evaluation
     int pa;                      // apply the parallactic-angle rotation
     double2 *B;                  // [nfreq][npointing][ntile][4]
 };
-int launch_beam_model(const PbArgs &a, cudaStream_t st);
+// `scratch` (nullable): 2*ntile + 1 ints of device memory for the
+// configuration lists; NULL takes them from the stream-ordered allocator.
+int launch_beam_model(const PbArgs &a, cudaStream_t st, int *scratch = nullptr);
 int launch_array_factor(const double *look, const double *dirs, int npix, double freq, const double *east,
                         const double *north, const double *height, const double *cable, double href, int nant,
                         double *af, cudaStream_t st);

@@ -119,6 +119,19 @@ def coarse_chan_start_hz(cc: int, first_rec_chan: int = 109) -> int:
     return centre - COARSE_CHAN_WIDTH_HZ // 2
 
 
+def tile_delays(az_deg: float, za_deg: float) -> np.ndarray:
+    """[16] analogue beamformer delays (units of 435 ps, 0..31) that point a
+    4 x 4 dipole tile (1.1 m pitch, row-major from the north-west corner, as
+    the device beam model lays it out) at (az, za)."""
+    i = np.arange(16)
+    x = ((i & 3) - 1.5) * 1.1
+    y = (1.5 - (i >> 2)) * 1.1
+    az, za = np.radians(az_deg), np.radians(za_deg)
+    tau = (x * np.sin(za) * np.sin(az) + y * np.sin(za) * np.cos(az)) / 299792458.0
+    d = np.round(tau / 435e-12)
+    return np.clip(d - d.min(), 0, 31).astype(np.uint32)
+
+
 def legacy_input_order(nant: int, seed: int = 3) -> np.ndarray:
     """i_idx[2*ant + pol] = vcs_order: a seeded permutation standing in for the
     metafits VCSOrder column (pfb.cpp:410-419)."""

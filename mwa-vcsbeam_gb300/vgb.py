@@ -87,6 +87,26 @@ class PipelineConfig(ctypes.Structure):
     ]
 
 
+class Tracking(ctypes.Structure):
+    """vgb_tracking: device tables the pipeline rebuilds W from every second."""
+    _fields_ = [
+        ("D", ctypes.c_void_p),
+        ("delays", ctypes.c_void_p),
+        ("east", ctypes.c_void_p),
+        ("north", ctypes.c_void_p),
+        ("height", ctypes.c_void_p),
+        ("cable", ctypes.c_void_p),
+        ("chan_freqs_hz", ctypes.c_void_p),
+        ("beam_freqs_hz", ctypes.c_void_p),
+        ("az", ctypes.c_void_p),
+        ("za", ctypes.c_void_p),
+        ("nseconds", ctypes.c_int),
+        ("pa_correction", ctypes.c_int),
+        ("href", ctypes.c_double),
+        ("latitude", ctypes.c_double),
+    ]
+
+
 _lib = None
 V = ctypes.c_void_p
 I = ctypes.c_int
@@ -166,6 +186,7 @@ _SIGS = {
     "vgb_pipeline_set_filters": (I, [V, V, V]),
     "vgb_pipeline_set_weights": (I, [V, V, I]),
     "vgb_pipeline_set_vdif_header": (I, [V, V]),
+    "vgb_pipeline_set_tracking": (I, [V, ctypes.POINTER(Tracking)]),
     "vgb_pipeline_run_device": (I, [V, V, LL]),
     "vgb_pipeline_run_host": (I, [V, V, LL]),
     "vgb_pipeline_fetch": (I, [V, V, V, V, V]),
@@ -694,6 +715,21 @@ class Pipeline:
     def set_weights(self, W, on_device: bool):
         check(lib().vgb_pipeline_set_weights(self.h, ptr(W), int(on_device)))
 
+    def set_tracking(self, D, delays, east, north, height, cable, chan_freqs_hz, beam_freqs_hz, az, za,
+                     href=0.0, latitude=0.0, pa_correction=True):
+        """Rebuild W on the device every second from these device tensors
+        (vgb_pipeline_set_tracking); az/za hold one pointing per second."""
+        self._tracking = (D, delays, east, north, height, cable, chan_freqs_hz, beam_freqs_hz, az, za)
+        t = Tracking(D=ptr(D), delays=ptr(delays), east=ptr(east), north=ptr(north), height=ptr(height),
+                     cable=ptr(cable), chan_freqs_hz=ptr(chan_freqs_hz), beam_freqs_hz=ptr(beam_freqs_hz),
+                     az=ptr(az), za=ptr(za), nseconds=int(az.numel()), pa_correction=int(pa_correction),
+                     href=float(href), latitude=float(latitude))
+        check(lib().vgb_pipeline_set_tracking(self.h, ctypes.byref(t)))
+
+    def clear_tracking(self):
+        check(lib().vgb_pipeline_set_tracking(self.h, None))
+        self._tracking = None
+
     def set_vdif_header(self, hdr: np.ndarray):
         hdr = np.ascontiguousarray(hdr, dtype=np.uint32)
         check(lib().vgb_pipeline_set_vdif_header(self.h, hdr.ctypes.data))
@@ -748,7 +784,8 @@ class Pipeline:
         buf = np.ascontiguousarray(buf, dtype=np.uint8)
         check(lib().vgb_pipeline_load_state(self.h, buf.ctypes.data, buf.size))
 
-    def stage_ms(self):
-        arr = (Fl * 4)()
-        check(lib().vgb_pipeline_stage_ms(self.h, arr, 4))
+    def stage_ms(self, n: int = 4):
+        """[PFB + beam, renormalise, IPFB + VDIF, history carry(, tracking tables)] ms."""
+        arr = (Fl * n)()
+        check(lib().vgb_pipeline_stage_ms(self.h, arr, n))
         return list(arr)

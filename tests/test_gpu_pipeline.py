@@ -313,3 +313,78 @@ def test_pipeline_stokes_i_only(vgb_mod, torch, oracle_mod, setup):
             assert np.array_equal(ps[:, :, cc * K:(cc + 1) * K], u[0]), (nst, cc)
             assert np.array_equal(off[cc], o[0]) and np.array_equal(sc[cc], s[0]), (nst, cc)
     assert np.array_equal(S[1][:, :, 0], S[4][:, :, 0])
+
+
+def test_pipeline_tracking_rebuilds_weights_every_second(vgb_mod, torch, oracle_mod, setup):
+    """Per-second tracking (vmCalcJonesAndDelays inside the captured second):
+    over three seconds with a different pointing each second, the pipeline
+    that rebuilds W itself equals, byte for byte, a pipeline given the W that
+    vgb_primary_beam -> vgb_jones / vgb_phase -> vgb_weights build for that
+    second; and its Stokes match the oracle chain (oracle primary beam, calc_j,
+    calc_phi, PFB, beamformer) within 1e-5 of the largest magnitude."""
+    import beam_model as BM
+
+    volt, filt, syn, _ = setup
+    nsec = 3
+    vol3 = np.concatenate([volt, volt[:1]], axis=0)[:nsec]
+    invw = 1.0 / NI
+    az = np.radians([45.0, 47.5, 50.0])
+    za = np.radians([20.0, 21.0, 22.5])
+    D = np.stack([SY.calibration_jones(NANT, K, seed=cc + 1) for cc in range(NCC)])
+    delays = np.zeros((NANT, 16), np.uint32)
+    delays[NANT // 2:] = np.arange(16, dtype=np.uint32) % 4          # a second dipole-delay set
+    delays[1, 3] = 32                                                # a dead dipole on one tile
+    east, north, height, cable = SY.tile_layout(NANT, seed=9)
+    href = 377.827  # the array reference height the oracle's calc_phi uses (MWA_ALTITUDE_METRES)
+    chan_f = np.stack([SY.fine_chan_freqs_hz(SY.coarse_chan_start_hz(cc)) for cc in range(NCC)])
+    beam_f = np.array([SY.coarse_chan_start_hz(cc) + 640000 for cc in range(NCC)], np.float64)
+    lat = BM.MWA_LATITUDE
+
+    d = {k: dev(v) for k, v in dict(D=D, delays=delays, east=east, north=north, height=height, cable=cable,
+                                      chan_f=chan_f, beam_f=beam_f, az=az, za=za).items()}
+    pt = vgb_mod.Pipeline(NCC, NANT, NBLK, nstokes=4, pfb_flags=0, do_ipfb=True, invw=invw)
+    pt.set_filters(filt, syn)
+    pt.set_tracking(d["D"], d["delays"], d["east"], d["north"], d["height"], d["cable"], d["chan_f"], d["beam_f"],
+                    d["az"], d["za"], href=href, latitude=lat, pa_correction=True)
+    pw = vgb_mod.Pipeline(NCC, NANT, NBLK, nstokes=4, pfb_flags=0, do_ipfb=True, invw=invw)
+    pw.set_filters(filt, syn)
+    for t in range(nsec):
+        # the fixed-weights pipeline gets this second's W from the separate table kernels
+        B = torch.empty((NCC, 1, NANT, 8), dtype=torch.float64, device="cuda")
+        vgb_mod.primary_beam(d["az"][t:t + 1], d["za"][t:t + 1], d["beam_f"], d["delays"], B, pa_correction=True,
+                             latitude=lat)
+        unit = dev(SY.unit_vectors(np.degrees(az[t]), np.degrees(za[t])))
+        Ws = []
+        for cc in range(NCC):
+            Jd = torch.empty((NANT * K, 8), dtype=torch.float64, device="cuda")
+            vgb_mod.jones(d["D"][cc], B[cc], 1, NANT, K, Jd)
+            ph = torch.empty((NANT * K, 2), dtype=torch.float64, device="cuda")
+            vgb_mod.phase(unit, d["east"], d["north"], d["height"], d["cable"], d["chan_f"][cc], 1, NANT, K, href, ph)
+            W = torch.empty((NANT * K, 8), dtype=torch.float32, device="cuda")
+            vgb_mod.weights(Jd, ph, NANT * K, W)
+            Ws.append(W)
+        pw.set_weights(torch.cat(Ws), on_device=True)
+        dv = dev(vol3[t].reshape(-1).view(np.uint8))
+        pt.run_device(dv)
+        pw.run_device(dv)
+        assert pt.launch_count() == pw.launch_count() + 5
+        outs = []
+        for p in (pt, pw):
+            ps = np.empty((NS, 4, NCC * K), np.uint8)
+            vd = np.empty((NCC, NS, 544), np.uint8)
+            S = np.empty((NCC, NS, 4, K), np.float32)
+            p.fetch(ps, None, None, vd)
+            p.fetch_raw(S)
+            outs.append((ps, vd, S))
+        for a, b in zip(*outs):
+            assert np.array_equal(a, b), t
+        # the oracle chain for this second
+        Bo = BM.primary_beam(az[t:t + 1], za[t:t + 1], beam_f, delays, pa=True, lat=lat)
+        unit_o = SY.unit_vectors(np.degrees(az[t]), np.degrees(za[t]))
+        for cc in range(NCC):
+            J = oracle_mod.calc_j(D[cc], np.ascontiguousarray(Bo[cc]))
+            phi = oracle_mod.calc_phi(unit_o, east, north, height, cable, chan_f[cc])
+            Sref, _ = oracle_second(oracle_mod, vol3, t, cc, filt, J, phi, invw)
+            assert rel_err(outs[0][2][cc], Sref[0]) < 1e-5, (t, cc)
+    pt.close()
+    pw.close()

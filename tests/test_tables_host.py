@@ -177,3 +177,21 @@ def test_filter_files(vgb_mod, ref, name, scale):
     assert np.array_equal(h, out[:n])
     if name == "FINEPFB":
         assert int(h.sum()) == 15106424   # documented checksum of the analysis filter
+
+
+def test_filter_fixture_is_the_reference_filters(vgb_mod):
+    """tests/golden/ref_filters.npz holds FINEPFB (analysis, int cast) and
+    LSQ12 x 15/7.2 (synthesis) as the reference's vmLoadFilter and
+    vmScaleFilterCoeffs loaded them (tests/golden/make_golden_filters.py);
+    the full-size GPU parity tests run on it. Where the filter files are
+    linked, this library's reader gives the same values."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_filters.npz"))
+    fine, lsq = g["finepfb"], g["lsq12_scaled"]
+    assert fine.shape == (1536,) and lsq.shape == (1536,)
+    assert int(fine.sum()) == 15106424 and int(fine.max()) == 117964   # documented checksum and peak tap
+    assert int(g["finepfb_ntaps"]) == 12 and int(g["lsq12_ntaps"]) == 12
+    for name, scale, want in (("FINEPFB", 1.0, fine.astype(np.float64)), ("LSQ12", 15.0 / 7.2, lsq)):
+        path = os.path.join(RUNTIME, f"{name}.dat")
+        if os.path.exists(path):
+            h, _ = vgb_mod.load_filter(path, 128, scale)
+            assert np.array_equal(h, want)
