@@ -84,3 +84,42 @@ def nibble_diff(a: np.ndarray, b: np.ndarray) -> int:
     hi = lambda x: ((x.astype(np.int16) >> 4) ^ 8) - 8
     lo = lambda x: ((x.astype(np.int16) & 15) ^ 8) - 8
     return int(max(np.abs(hi(a) - hi(b)).max(), np.abs(lo(a) - lo(b)).max()))
+
+
+def oracle_chain_second(htr, ninputs, filt, syn, J, phi, invw, blocks_per_chunk=4):
+    """The FP64 oracle chain over one whole second of MWAX voltages in the
+    reference's read-buffer layout (htr = margin block + the second's blocks):
+    forward PFB (identity VCS order, PFB_FULL_PRECISION), beamformer,
+    renormalise of the oracle's own Stokes, inverse PFB of the oracle's own
+    beam voltages (no history: a first second) and VDIF quantisation.
+    Processed a few blocks at a time so the complex-double fine channels stay
+    small. Returns S [ns][4][128], e [ns][128][2], (offsets, scales, bytes)
+    and the VDIF payload bytes [ns][512]."""
+    import oracle as O
+
+    K, P = 128, 12
+    nblk = htr.shape[0] - 1
+    i_idx = np.arange(ninputs, dtype=np.int32)
+    polQ, polP = pol_lists(i_idx)
+    S_parts, e_parts = [], []
+    for b in range(0, nblk, blocks_per_chunk):
+        k = min(blocks_per_chunk, nblk - b)
+        v = O.fpfb(np.ascontiguousarray(htr[b:b + k + 1]), ninputs, k * 500, filt, K, P, i_idx, 0)
+        S, e = O.beamform(v, J, phi, polQ, polP, invw)
+        S_parts.append(S[0])
+        e_parts.append(e[0])
+        del v
+    S = np.concatenate(S_parts)
+    e = np.concatenate(e_parts)
+    off, sc, u8 = O.renormalise(S[None])
+    x = np.concatenate([np.zeros((P, K, 2), np.complex128), e], axis=0)
+    out = O.ipfb(x, syn, P)
+    flt = np.stack([out.real, out.imag], axis=-1).astype(np.float32).reshape(S.shape[0], 512)
+    return S, e, (off[0], sc[0], u8[0]), O.vdif_quantise(flt)
+
+
+def byte_diff_stats(a, b):
+    """(largest |a - b|, fraction of samples differing by more than one LSB,
+    fraction differing at all) of two uint8 arrays."""
+    d = np.abs(np.asarray(a).astype(np.int16) - np.asarray(b).astype(np.int16))
+    return int(d.max()), float((d > 1).mean()), float((d > 0).mean())

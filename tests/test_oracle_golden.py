@@ -150,3 +150,32 @@ def test_table_builders_match_reference_host(oracle_mod):
         ref.refhost_calc_geometric_delays(*unit, int(freqs[c]), A, pp(east), pp(north), pp(height),
                                           pp(cable), pp(pr))
         assert np.array_equal(pr, phi[0, :, c])
+
+
+def test_oracle_chain_c1_against_reference_kernels():
+    """The FP64 oracle chain over one whole C1 second (128 tiles, FINEPFB,
+    LSQ12 x 15/7.2) against the reference's own CUDA kernels on the same
+    voltages (tests/golden/ref_golden_c1.npz): Stokes and beam voltages within
+    1e-5 norm-wise (cuFFT FP32 against FP64), PSRFITS bytes within one LSB on
+    <= 1e-4 of samples, VDIF frames (outside the reference's inverse-PFB tap
+    bug, the first 12 fine samples) within one LSB on <= 1e-4."""
+    import os
+    import sys
+
+    path = os.path.join(os.path.dirname(__file__), "golden", "ref_golden_c1.npz")
+    if not os.path.exists(path):
+        pytest.skip("C1 golden vectors not generated")
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import make_golden_c1 as G
+    from helpers import byte_diff_stats, oracle_chain_second, rel_err
+
+    g = dict(np.load(path))
+    htr, fine, lsq, J, phi = G.c1_inputs()
+    S, e, (off, sc, u8), vd = oracle_chain_second(htr, 256, fine, lsq, J, phi, 1.0 / 256)
+    assert rel_err(S[::G.SUB_S], g["S_sub"]) < 1e-5
+    assert rel_err(e[::G.SUB_S], g["e_sub"]) < 1e-5
+    assert byte_diff_stats(u8[::G.SUB_B], g["u8_sub"])[1] <= 1e-4
+    assert rel_err(off, g["offsets"]) < 1e-5 and rel_err(sc, g["scales"]) < 1e-5
+    keep = np.arange(0, 10000, G.SUB_B) >= 12
+    mx, _, frac = byte_diff_stats(vd[::G.SUB_B][keep], g["vdif_sub"][keep])
+    assert mx <= 1 and frac <= 1e-4
