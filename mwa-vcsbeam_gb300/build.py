@@ -77,5 +77,34 @@ def build(verbose: bool = False, force: bool = False, ptxas_v: bool = False) -> 
     return LIB
 
 
+COMPAT_SRC = os.path.join(CSRC, "compat", "vm_compat.cu")
+COMPAT_LIB = os.path.join(LIBDIR, "libvcsbeam_compat.so")
+
+
+def build_compat(include_dirs, verbose: bool = False) -> str:
+    """The VCSBeam-API library (lib/libvcsbeam_compat.so): csrc/compat/
+    vm_compat.cu compiled against a configured VCSBeam vcsbeam.h and the
+    dependency headers it includes (`include_dirs`, e.g. a VCSBeam build's
+    include directories), linked to libvcsbeam_gb300.so."""
+    lib = build(verbose=verbose)
+    obj = os.path.join(BUILD, "vm_compat.cu.o")
+    incs = []
+    for d in include_dirs:
+        incs += ["-I", d]
+    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-D__NVCC__", "-x", "cu",
+           *incs, "-I", os.path.join(ROOT, "include"), "-c", COMPAT_SRC, "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if verbose or r.returncode:
+        sys.stderr.write(r.stdout + r.stderr)
+    if r.returncode:
+        raise RuntimeError("nvcc failed: " + " ".join(cmd))
+    link = [nvcc(), *ARCH, "-shared", "-o", COMPAT_LIB, obj, "-L", LIBDIR, "-lvcsbeam_gb300",
+            "-Xlinker", "-rpath,$ORIGIN"]
+    r = subprocess.run(link, capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+    return COMPAT_LIB
+
+
 if __name__ == "__main__":
     print(build(verbose=True, force="--force" in sys.argv, ptxas_v="-v" in sys.argv))

@@ -5,7 +5,9 @@
 # /root/reference, override with VGB_REFERENCE_DIR) against the stand-in
 # headers in oracle/ref_stubs/, writing only into oracle/_ref/:
 #
-#   oracle/_ref/include/vcsbeam.h   configured from include/vcsbeam.h.in
+#   oracle/_ref/include/vcsbeam.h   configured from include/vcsbeam.h.in, with
+#                                   src/gpu_includes.h, gpu_macros.h and
+#                                   gpu_fft.hpp beside it
 #   oracle/_ref/ref_pfb.cubin       device code of src/pfb.cpp       (sm_103a)
 #   oracle/_ref/ref_form_beam.cubin device code of src/form_beam.cpp (sm_103a)
 #   oracle/_ref/libref_host.so      src/jones.c, src/filter.c, src/geometry.c,
@@ -13,6 +15,7 @@
 #                                   + oracle/ref_host_shim.c (host, this machine)
 #   oracle/_ref/runtime/            RUNTIME_DIR: links to the reference's
 #                                   pfb_filter/*.dat and pq_phase_correction.txt
+#   oracle/_ref/source_dir          the VCSBeam source tree's path (text)
 #
 # The cubins travel to a GPU machine with the repository; there
 # oracle/ref_harness.cu (built by __graft_entry__.build()) loads them with the
@@ -30,8 +33,19 @@ if [ ! -f "$REF/src/pfb.cpp" ]; then
     exit 0
 fi
 mkdir -p "$OUT/include" "$OUT/runtime"
+# where the source tree is, for CPU tests that compile the reference's own
+# programs against the configured header (a path, not a link, so that no
+# copy of the tree follows the build output anywhere)
+rm -f "$OUT/source"
+printf '%s\n' "$REF" > "$OUT/source_dir"
 for f in "$REF"/pfb_filter/*.dat "$REF/pq_phase_correction.txt"; do
     [ -f "$f" ] && ln -sf "$f" "$OUT/runtime/$(basename "$f")"
+done
+
+# the reference's GPU portability headers that vcsbeam.h includes, beside it,
+# so that code compiled against the configured header needs only _ref/include
+for f in gpu_includes.h gpu_macros.h gpu_fft.hpp; do
+    cp -f "$REF/src/$f" "$OUT/include/$f"
 done
 
 # include/vcsbeam.h.in -> vcsbeam.h (the three #cmakedefine lines only)

@@ -95,6 +95,8 @@ typedef struct MetafitsMetadata {
     size_t num_corr_fine_chans_per_coarse;
     uint32_t corr_fine_chan_width_hz;
     size_t num_volt_fine_chans_per_coarse;
+    double ra_tile_pointing_deg;
+    double dec_tile_pointing_deg;
 } MetafitsMetadata;
 
 typedef struct VoltageMetadata {
