@@ -18,6 +18,9 @@ flush is needed); two distinct seconds stay resident and alternate.
          1 ms integrations into 8-bit PSRFITS, one coarse channel-second per
          step, in four weight precisions: split BF16 and single FP16/BF16 on
          the tensor cores, FP32 on the CUDA cores (the plain baseline)
+  reference_cuda  the reference's own CUDA kernels (unmodified, compiled for
+         sm_103a) on one coarse channel-second of the same workload, timed on
+         the same GPU beside the product (a baseline, like the CPU one)
   --impl reference  the reference's CPU path timed on the host cores: the
          reference has no CPU implementation of its kernels, so this is the
          oracle's OpenMP FP32 transcription of them (oracle/oracle.c).
@@ -45,6 +48,13 @@ NI = 2 * NANT
 NSPEC = NBLK * 500
 SECOND_BYTES = NBLK * NI * 64000 * 2           # one coarse channel, one second
 BEAM_KERNEL_DRAM_BYTES_PER_CC = (1.322368e9 + 86.6944e6) / 2
+# Algorithmic FP32 flops of the fused PFB + beamformer per (RF input, fine
+# spectrum): the 12-tap weighted overlap-add of 128 complex samples
+# (12 x 2 x 2 x 128 = 6,144), a 128-point complex FFT counted as 5 N log2 N
+# (4,480), and the beam back end per input and fine channel -- half of a
+# tile's J^-1 v (32), its sums into ex / ey (4), the autocorrelation terms
+# (16) and the incoherent power (8) -- (60 / 2) x 128 = 3,840.
+BEAM_KERNEL_FLOPS_PER_INPUT_SPECTRUM = 6144 + 4480 + 3840
 
 
 def out_bytes(ncc):
@@ -238,6 +248,92 @@ def cpu_baseline_line(target_s: float = 12.0):
 
 
 # --------------------------------------------------------------------------
+# the reference's own CUDA build on the same GPU (a baseline, like the CPU one)
+# --------------------------------------------------------------------------
+def reference_cuda_section(smart: bool = False, reps: int = 3):
+    """The unmodified VCSBeam kernels (oracle/_ref/*.cubin, compiled from the
+    reference's pfb.cpp and form_beam.cpp by oracle/build_ref.sh) driven by
+    oracle/ref_harness.cu with the reference's launch shapes, memsets and
+    cuFFT calls, on one coarse channel-second of the bench workload (128
+    tiles, 1 beam, full Stokes): forward PFB (vmWOLAChunk..vmPackChunk),
+    beamformer (vmApplyJChunk + vmBeamformChunk), renormalise (the kernel of
+    vmSendSToFits) and inverse PFB (the kernel of cu_invert_pfb). Device time
+    between CUDA events only, the best of `reps` runs per stage (the
+    reference's host repacking loops and synchronous copies are left out,
+    which favours it). The reference runs one process per coarse channel, so
+    its real-time factor for the 24-channel band on one GPU is 1 / (24 t)."""
+    import ctypes
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    import synthetic as SY
+
+    path = os.path.join(ROOT, "oracle", "_ref", "libref_harness.so")
+    if not os.path.exists(path):
+        return {"unavailable": "oracle/_ref/libref_harness.so not built (needs the reference's cubins)"}
+    h = ctypes.CDLL(path)
+    h.refh_last_error.restype = ctypes.c_char_p
+    if h.refh_init(os.path.join(ROOT, "oracle", "_ref").encode()):
+        return {"unavailable": h.refh_last_error().decode()}
+    V, I = ctypes.c_void_p, ctypes.c_int
+    h.refh_fpfb.argtypes = [V, ctypes.c_size_t, I, I, V, I, I, V, I, V, V, V]
+    h.refh_beamform.argtypes = [V, I, I, I, I, V, V, V, V, I, ctypes.c_double, I, V, V, V]
+    h.refh_ipfb.argtypes = [V, V, V, V, I, I, I, I, V, V]
+    h.refh_renormalise_timed.argtypes = [V, I, I, I, I, V, V, V, V]
+    p = lambda a: a.ctypes.data_as(V)
+
+    def chk(rc):
+        if rc:
+            raise RuntimeError(h.refh_last_error().decode())
+
+    clocks = ClockSampler(0)
+    htr = O.mwax_buffer(7, NBLK + 1, NI)
+    filt = SY.analysis_filter_int16()
+    i_idx = SY.legacy_input_order(NANT)
+    flags = O.PFB_SMART if smart else O.PFB_FULL_PRECISION
+    out = np.empty((NSPEC, K, NI), dtype=np.uint8 if smart else np.complex128)
+    ms = ctypes.c_float()
+    times = {}
+
+    def best(call):
+        vals = []
+        for _ in range(reps + 1):          # the first run loads modules and plans cuFFT
+            chk(call())
+            vals.append(ms.value)
+        return min(vals[1:])
+
+    times["pfb"] = best(lambda: h.refh_fpfb(p(htr), htr.nbytes, NI, NSPEC, p(filt), K, P, p(i_idx), flags, None,
+                                            p(out), ctypes.byref(ms)))
+    J = O.calc_j(SY.calibration_jones(NANT, K, seed=11), SY.identity_beam(1, NANT))
+    e_, n_, h_, c_ = SY.tile_layout(NANT, seed=7)
+    phi = O.calc_phi(SY.unit_vectors(45.0, 20.0), e_, n_, h_, c_, SY.fine_chan_freqs_hz(SY.coarse_chan_start_hz(0)))
+    polQ = np.ascontiguousarray(i_idx[0::2].astype(np.uint32))
+    polP = np.ascontiguousarray(i_idx[1::2].astype(np.uint32))
+    S = np.empty((1, NSPEC, 4, K), dtype=np.float32)
+    e = np.empty((1, NSPEC, K, 2), dtype=np.complex128)
+    times["beamform"] = best(lambda: h.refh_beamform(p(out), 0 if smart else 1, NSPEC, K, NANT, p(J), p(phi),
+                                                     p(polQ), p(polP), 1, 1.0 / NI, 4, p(S), p(e), ctypes.byref(ms)))
+    off = np.empty((1, 4, K), np.float32)
+    sc = np.empty((1, 4, K), np.float32)
+    u8 = np.empty(S.shape, np.uint8)
+    times["renormalise"] = best(lambda: h.refh_renormalise_timed(p(S), 1, NSPEC, 4, K, p(off), p(sc), p(u8),
+                                                                 ctypes.byref(ms)))
+    coeffs = SY.synthesis_filter(scale=SY.synthesis_scale(filt))
+    ftr, fti = O.ipfb_table(coeffs, K)
+    x = np.concatenate([np.zeros((P, K, 2), np.complex128), e[0]], axis=0)
+    ir = np.ascontiguousarray(x.real.astype(np.float32))
+    ii = np.ascontiguousarray(x.imag.astype(np.float32))
+    vo = np.empty((NSPEC * K, 2, 2), dtype=np.float32)
+    times["ipfb"] = best(lambda: h.refh_ipfb(p(ir), p(ii), p(ftr), p(fti), P, NSPEC, K, 2, p(vo), ctypes.byref(ms)))
+    clk = clocks.stop()
+    t_cc = sum(times.values()) / 1e3
+    return {"what": "the reference's own CUDA kernels (unmodified, compiled for sm_103a), one coarse channel-second, "
+                    "128 tiles, 1 beam, full Stokes; device time only (host repacking and copies left out)",
+            "mode": "PFB_SMART" if smart else "PFB_FULL_PRECISION", "ms_per_cc_s": times,
+            "seconds_per_cc_second": t_cc, "value": 1.0 / (NCC * t_cc), "unit": UNIT, "clocks": clk}
+
+
+# --------------------------------------------------------------------------
 # arms
 # --------------------------------------------------------------------------
 def reference_arm(args, rank, world):
@@ -255,7 +351,7 @@ def reference_arm(args, rank, world):
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total_dt / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
             "config": config_dict(NCC),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port",
                              "sample": f"{args.ref_spectra} fine spectra of 1 of 24 coarse channels per step "
@@ -271,7 +367,7 @@ def gb300_arm(args, rank, local_rank, world):
     import synthetic as SY
     import vgb
 
-    from sharding import RankContext
+    from sharding import RankContext, gather_splice, shard
 
     torch.cuda.set_device(local_rank)
     ctx = RankContext()
@@ -285,7 +381,10 @@ def gb300_arm(args, rank, local_rank, world):
 
     max_over_ranks = ctx.max
 
-    ncc = args.ncc
+    # one data-second's coarse channels split over the ranks (the reference's
+    # one process per coarse channel); one rank takes --ncc of them
+    mine = shard(NCC, rank, world) if world > 1 else range(args.ncc)
+    ncc = len(mine)
     volt = make_voltages(torch, args.resident, ncc, seed=1234 + rank)
     W = make_weights(torch, vgb, SY, ncc)
     h = SY.analysis_filter_int16()
@@ -315,7 +414,8 @@ def gb300_arm(args, rank, local_rank, world):
     barrier()
     clk = clocks.stop()
     elapsed_s = max_over_ranks(ev0.elapsed_time(ev1) / 1e3)
-    value = world * args.steps * ncc / NCC / elapsed_s
+    ncc_all = ctx.sum(ncc)                  # channels all ranks process per step
+    value = args.steps * ncc_all / NCC / elapsed_s
     # per-stage CUDA-event times (eager launches with events between stages)
     pipe.enable_timing(True)
     stage = np.zeros(5)
@@ -411,23 +511,34 @@ def gb300_arm(args, rank, local_rank, world):
         scl = torch.empty(ncc * 4 * K, dtype=torch.float32, pin_memory=True)
         pipe.set_host_outputs(ps, off, scl, vd)
         del volt
-        for _ in range(min(args.warmup, 3)):
+        psv = ps.numpy().reshape(NSPEC, 4, ncc * K)
+        offv, sclv = off.numpy().reshape(ncc, 4, K), scl.numpy().reshape(ncc, 4, K)
+        vdv = vd.numpy().reshape(ncc, NSPEC, 544)
+
+        def e2e_step():
             pipe.run_host(hin)
+            if world > 1:                   # the channel splice at the writer rank, host-staged
+                pipe.sync()
+                gather_splice(ctx, NCC, psv, offv, sclv, vdv)
+
+        for _ in range(min(args.warmup, 3)):
+            e2e_step()
         pipe.sync()
         barrier()
         t0 = time.perf_counter()
         e2e_steps = max(1, min(args.steps, args.e2e_steps))
         for _ in range(e2e_steps):
-            pipe.run_host(hin)
+            e2e_step()
         pipe.sync()
         barrier()
         e2e_s = max_over_ranks(time.perf_counter() - t0)
-        e2e = {"value": world * e2e_steps * ncc / NCC / e2e_s, "unit": UNIT,
+        e2e = {"value": e2e_steps * ncc_all / NCC / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": ncc * SECOND_BYTES,
                "d2h_bytes_per_step": psr_b + vdif_b + stat_b,
                "steps": e2e_steps, "ms_per_step": 1e3 * e2e_s / e2e_steps,
                "path": "vgb_pipeline_run_host from pinned host memory, products back to pinned host buffers; "
-                       "next second's copy overlaps this second's compute"}
+                       "next second's copy overlaps this second's compute" +
+                       ("; each rank's rows gathered and spliced at rank 0 (gloo, host-staged)" if world > 1 else "")}
     pipe.close()
 
     # ---- roofline of the dominant kernel (fused PFB + beamformer) -----------
@@ -444,6 +555,21 @@ def gb300_arm(args, rank, local_rank, world):
     # written once
     traffic = args.traffic if args.traffic is not None else ncc * BEAM_KERNEL_DRAM_BYTES_PER_CC
     achieved = alg_bytes / (stage[0] / 1e3) / 1e9
+    # the compute side: FP32 flops of the launch against this GPU's measured
+    # FP32 FMA throughput (scalar FFMA and packed FFMA2, the better of both)
+    alg_flops = ncc * NI * NSPEC * BEAM_KERNEL_FLOPS_PER_INPUT_SPECTRUM
+    try:
+        fp32_ffma = vgb.fp32_peak(False)
+        fp32_ffma2 = vgb.fp32_peak(True)
+    except Exception:
+        fp32_ffma = fp32_ffma2 = None
+    fp32_peak = max(fp32_ffma or 0.0, fp32_ffma2 or 0.0) or None
+    fp32_achieved = alg_flops / (stage[0] / 1e3) / 1e12
+    compute = {"bound": "fp32 (CUDA cores)", "alg_flops_per_launch": alg_flops,
+               "alg_flops_per_input_spectrum": {"wola": 6144, "fft_5nlog2n": 4480, "beam_back_end": 3840},
+               "achieved": fp32_achieved, "unit": "TFLOP/s",
+               "peak_ffma": fp32_ffma, "peak_ffma2": fp32_ffma2, "peak_source": "measured (vgb_fp32_peak)",
+               "frac": (fp32_achieved / fp32_peak) if fp32_peak else None}
     roofline = {"kernel": "beam_kernel (fused PFB + tied-array/incoherent beam + Stokes)", "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
@@ -454,7 +580,8 @@ def gb300_arm(args, rank, local_rank, world):
                            "(ncu of a 2-channel launch: issue 61.0 %, FMA pipe 58.8 %, shared-memory wavefronts "
                            "59.3 % of peak; DRAM 9.4 %)",
                 "stage_ms": {"pfb_beam": stage[0], "renormalise": stage[1], "ipfb_vdif": stage[2],
-                             "history": stage[3], "tracking_tables": stage[4]}}
+                             "history": stage[3], "tracking_tables": stage[4]},
+                "compute": compute}
 
     mb_section = None
     if rank == 0 and not args.no_multibeam:
@@ -462,9 +589,11 @@ def gb300_arm(args, rank, local_rank, world):
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed_s / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config_dict(ncc),
-            "run": {"step": "one data-second (24 coarse channels x 1 s)", "resident_seconds": args.resident,
+            "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_dict(NCC if world > 1 else ncc),
+            "run": {"step": "one data-second (24 coarse channels x 1 s)" +
+                            (f"; rank r processes coarse channels shard(24, r, {world})" if world > 1 else ""),
+                    "resident_seconds": args.resident,
                     "pfb_inputs_per_step": vgb.pfb_variant_last(),
                     "cuda_graphs": "each second replayed from a captured CUDA graph (one per resident buffer "
                                    "and second parity), the per-second tracking tables inside it; stage_ms from "
@@ -480,6 +609,16 @@ def gb300_arm(args, rank, local_rank, world):
         line["surrogate"] = surrogate_section(torch, vgb, SY, args.sur_steps)
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_line(args.cpu_seconds)
+    if rank == 0 and world == 1 and not args.no_ref_cuda:
+        try:
+            rc = reference_cuda_section()
+        except Exception as exc:  # the baseline leg must not lose the product's line
+            rc = {"unavailable": f"{type(exc).__name__}: {exc}"}
+        line["reference_cuda"] = rc
+        if "value" in rc:
+            # the target: >= 2x the reference's own CUDA build for 1 beam at FP32 accuracy
+            line["vs_reference_cuda"] = {"value": value / rc["value"], "e2e": (e2e["value"] / rc["value"]) if e2e
+                                         else None, "target": 2.0}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -812,6 +951,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=40)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ref-cuda", action="store_true", help="skip timing the reference's own CUDA build")
     ap.add_argument("--ref-spectra", type=int, default=400, help="reference arm: spectra per step")
     ap.add_argument("--no-multibeam", action="store_true", help="skip the many-beam (C3/C4) section")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the beam-surrogate section")

@@ -640,6 +640,22 @@ int vgb_pipeline_enable_graphs(vgb_pipeline *p, int on);
 long long vgb_pipeline_state_bytes(const vgb_pipeline *p);
 int vgb_pipeline_save_state(vgb_pipeline *p, void *host, long long bytes);
 int vgb_pipeline_load_state(vgb_pipeline *p, const void *host, long long bytes);
+/* Diagnostic (no reference counterpart): this GPU's FP32 FMA throughput in
+ * TFLOP/s (2 flops per FMA), from independent FMA chains on every SM timed
+ * with CUDA events; packed != 0 issues them as FFMA2. The compute
+ * denominator of the fused PFB + beamformer's roofline. */
+int vgb_fp32_peak(int packed, int iters, double *tflops, void *stream);
+
+/* The PSRFITS channel splice across processes (the reference's MPI_Igather
+ * into the spliced sub-integration, beam_psrfits.c:608-628), host memory:
+ * one process's spliced rows part [nspectra][nstokes][ncc_part*nchan] (its
+ * pipeline's vgb_pipeline_fetch output) placed at coarse channels
+ * [cc_offset, cc_offset + ncc_part) of the full rows out
+ * [nspectra][nstokes][ncc_total*nchan]. The offsets and scales
+ * ([ncc][nstokes][nchan]) and VDIF frames ([ncc][...]) of consecutive
+ * channels are contiguous and join by concatenation. */
+int vgb_splice_psrfits(const uint8_t *part, int nspectra, int nstokes, int nchan, int ncc_part, int cc_offset,
+                       int ncc_total, uint8_t *out);
 /* Milliseconds per stage of the last second: [0] fused PFB + beamformer,
  * [1] renormalise, [2] inverse PFB + VDIF, [3] history carry, [4] tracking
  * tables (n = 5; 0 when tracking is off). Synchronises. */

@@ -187,6 +187,8 @@ _SIGS = {
     "vgb_pipeline_set_weights": (I, [V, V, I]),
     "vgb_pipeline_set_vdif_header": (I, [V, V]),
     "vgb_pipeline_set_tracking": (I, [V, ctypes.POINTER(Tracking)]),
+    "vgb_splice_psrfits": (I, [V, I, I, I, I, I, I, V]),
+    "vgb_fp32_peak": (I, [I, I, ctypes.POINTER(ctypes.c_double), V]),
     "vgb_pipeline_run_device": (I, [V, V, LL]),
     "vgb_pipeline_run_host": (I, [V, V, LL]),
     "vgb_pipeline_fetch": (I, [V, V, V, V, V]),
@@ -681,6 +683,24 @@ class Multibeam:
         ms = (ctypes.c_float * 5)()
         check(lib().vgb_multibeam_stage_ms(self.h, ms, 5))
         return dict(zip(self.STAGES, [float(x) for x in ms]))
+
+
+def fp32_peak(packed: bool, iters: int = 20000, stream=None) -> float:
+    """This GPU's FP32 FMA throughput in TFLOP/s (FFMA2 when packed)."""
+    t = ctypes.c_double()
+    check(lib().vgb_fp32_peak(int(packed), iters, ctypes.byref(t), stream_ptr(stream)))
+    return t.value
+
+
+def splice_psrfits(part: np.ndarray, cc_offset: int, ncc_total: int, out: np.ndarray):
+    """Place one process's spliced PSRFITS rows part [ns][nstokes][ncc_part*128]
+    (uint8, host) at coarse channel cc_offset of out [ns][nstokes][ncc_total*128]."""
+    part = np.ascontiguousarray(part, dtype=np.uint8)
+    ns, nst, w = part.shape
+    if out.shape != (ns, nst, ncc_total * NCHAN) or out.dtype != np.uint8 or not out.flags.c_contiguous:
+        raise VGBError("splice_psrfits: out must be contiguous uint8 [ns][nstokes][ncc_total*128]")
+    check(lib().vgb_splice_psrfits(part.ctypes.data, ns, nst, NCHAN, w // NCHAN, cc_offset, ncc_total,
+                                   out.ctypes.data))
 
 
 class Pipeline:

@@ -273,6 +273,37 @@ extern "C" int refh_renormalise(const float *S, int npointing, int nstep, int ns
     return 0;
 }
 
+/* refh_renormalise with the kernel's device time (CUDA events around the
+ * launch) in *elapsed_ms. */
+extern "C" int refh_renormalise_timed(const float *S, int npointing, int nstep, int nstokes, int nchan,
+                                      float *offsets, float *scales, uint8_t *out, float *elapsed_ms)
+{
+    const size_t n = (size_t)npointing * nstep * nstokes * nchan;
+    DevBuf<float> d_S, d_off, d_sc;
+    DevBuf<uint8_t> d_out;
+    if (d_S.alloc(n) || d_off.alloc((size_t)npointing * nstokes * nchan) ||
+        d_sc.alloc((size_t)npointing * nstokes * nchan) || d_out.alloc(n))
+        return 1;
+    RT(cudaMemcpy(d_S.p, S, sizeof(float) * n, cudaMemcpyHostToDevice));
+    void *a0 = d_S.p, *a2 = d_off.p, *a3 = d_sc.p, *a4 = d_out.p;
+    int ns = nstep;
+    void *args[] = {&a0, &ns, &a2, &a3, &a4};
+    cudaEvent_t e0, e1;
+    RT(cudaEventCreate(&e0));
+    RT(cudaEventCreate(&e1));
+    RT(cudaEventRecord(e0));
+    if (launch(g_renorm, dim3(npointing), dim3(nchan, nstokes), 0, args)) return 1;
+    RT(cudaEventRecord(e1));
+    RT(cudaEventSynchronize(e1));
+    if (elapsed_ms) RT(cudaEventElapsedTime(elapsed_ms, e0, e1));
+    RT(cudaMemcpy(offsets, d_off.p, sizeof(float) * npointing * nstokes * nchan, cudaMemcpyDeviceToHost));
+    RT(cudaMemcpy(scales, d_sc.p, sizeof(float) * npointing * nstokes * nchan, cudaMemcpyDeviceToHost));
+    RT(cudaMemcpy(out, d_out.p, n, cudaMemcpyDeviceToHost));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return 0;
+}
+
 /* cu_form_incoh_beam's first kernel (form_beam.cpp:487-490):
  * incoh_beam <<<(nchan, nsample), ninput>>>. */
 extern "C" int refh_incoh(const uint8_t *data, int nsample, int nchan, int ninput, float *incoh)

@@ -86,3 +86,64 @@ def test_training_validation_and_fallback(vgb_mod):
     assert np.all(err[~exact] <= 2 * tol)      # network answers (rotated by P, a unitary)
     assert (~exact).any()                      # ... and there are some
     s.close()
+
+
+def test_what_the_trained_network_gains(vgb_mod):
+    """The surrogate against the method without it (the plain beam model) on
+    a C5-shaped query set: 1024 pointings on a 32 x 32 grid of 0.4 deg around
+    the tiles' analogue pointing x 128 tiles sharing one trained delay set x
+    24 frequencies, after a short training run (24,000 steps of 8,192
+    samples; the network trains on the analytic tile model that stands in
+    for the FEE model, whose parity is unpinned here).
+
+    The relation this build documents, asserted:
+      * at the required 1e-3 Jones tolerance no sky cell qualifies, every
+        query falls back, and B equals the plain model's exactly: no error,
+        and no gain;
+      * at a loose 0.1 tolerance the network answers queries, each within
+        twice the validated tolerance of the plain model;
+      * the surrogate path is slower than the plain model either way (the
+        analytic stand-in is a 16-term sum; the network would pay only
+        against a model as costly as the FEE one).
+    The measured numbers are printed."""
+    torch = torch_cuda()
+    nsets, nfreq = 16, 24
+    delays, set_az, set_za = SY.tile_delay_sets(nsets, seed=11, return_dirs=True)
+    freqs = np.linspace(80e6, 300e6, nfreq)
+    s = vgb_mod.Surrogate(nsets, batch=8192, seed=1)
+    s.set_training(delays, freqs, ndir=65536)
+    s.train(24000, lr_max=2e-3, lr_min=1e-4)
+    npnt, ntile = 1024, 128
+    gaz, gza = SY.grid_pointings(32, 0.4, np.degrees(set_az[0]), np.degrees(set_za[0]))
+    az, za, f = dev(np.radians(gaz)), dev(np.radians(gza)), dev(freqs)
+    ts = dev(np.zeros(ntile, np.int32))
+    td = dev(np.broadcast_to(delays[0], (ntile, 16)).astype(np.uint32))
+    Bs = torch.empty(nfreq * npnt * ntile * 8, dtype=torch.float64, device="cuda")
+    Bp = torch.empty_like(Bs)
+    nq = nfreq * npnt * ntile
+
+    def timed(fn, n=3):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            r = fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) / n, r
+
+    ms_plain, _ = timed(lambda: vgb_mod.primary_beam(az, za, f, td, Bp))
+    out = {}
+    for tol in (1e-3, 0.1):
+        mx, frac = s.validate(1_000_000, tol=tol)
+        ms_sur, nfb = timed(lambda: s.beam(az, za, f, ts, td, Bs))
+        err = (Bs - Bp).abs().max().item()
+        out[tol] = dict(cells_within=frac, max_validation_error=mx, fallback_fraction=nfb / nq, max_B_error=err,
+                        surrogate_ms=ms_sur, plain_ms=ms_plain)
+    print("surrogate vs plain model:", out)
+    strict, loose = out[1e-3], out[0.1]
+    assert strict["cells_within"] == 0.0 and strict["fallback_fraction"] == 1.0 and strict["max_B_error"] == 0.0
+    assert loose["fallback_fraction"] < 1.0 and loose["max_B_error"] <= 2 * 0.1
+    assert strict["surrogate_ms"] > ms_plain and loose["surrogate_ms"] > ms_plain
+    s.close()
