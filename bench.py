@@ -58,12 +58,13 @@ BEAM_KERNEL_FLOPS_PER_INPUT_SPECTRUM = 6144 + 4480 + 3840
 
 
 def out_bytes(ncc):
-    """PSRFITS bytes, VDIF bytes and scale/offset bytes per data-second."""
-    return NSPEC * 4 * ncc * K, ncc * NSPEC * 544, 2 * ncc * 4 * K * 4
+    """PSRFITS bytes (the tied-array beam's four Stokes and the incoherent
+    beam's Stokes I), VDIF bytes and scale/offset bytes per data-second."""
+    return NSPEC * 5 * ncc * K, ncc * NSPEC * 544, 2 * ncc * 5 * K * 4
 
 
 WORKLOAD = ("full band: 24 coarse channels x 128 tiles x 2 pols, 8-bit MWAX voltages (sigma 16), "
-            "fine PFB 12x128 -> 1 tied-array beam + incoherent, full Stokes 100 us -> 8-bit PSRFITS; "
+            "fine PFB 12x128 -> 1 tied-array beam (full Stokes) + incoherent beam (Stokes I), 100 us -> 8-bit PSRFITS; "
             "inverse PFB -> 8-bit VDIF; FP32")
 
 
@@ -505,22 +506,42 @@ def gb300_arm(args, rank, local_rank, world):
     if args.e2e_steps > 0:
         hin = torch.empty(ncc * SECOND_BYTES, dtype=torch.int8, pin_memory=True)
         hin.copy_(volt[0].reshape(-1))
-        ps = torch.empty(psr_b, dtype=torch.uint8, pin_memory=True)
+        ps = torch.empty(NSPEC * 4 * ncc * K, dtype=torch.uint8, pin_memory=True)
         vd = torch.empty(vdif_b, dtype=torch.uint8, pin_memory=True)
         off = torch.empty(ncc * 4 * K, dtype=torch.float32, pin_memory=True)
         scl = torch.empty(ncc * 4 * K, dtype=torch.float32, pin_memory=True)
+        ips = torch.empty(NSPEC * ncc * K, dtype=torch.uint8, pin_memory=True)
+        ioff = torch.empty(ncc * K, dtype=torch.float32, pin_memory=True)
+        iscl = torch.empty(ncc * K, dtype=torch.float32, pin_memory=True)
         pipe.set_host_outputs(ps, off, scl, vd)
+        pipe.set_host_incoh(ips, ioff, iscl)
         del volt
         psv = ps.numpy().reshape(NSPEC, 4, ncc * K)
         offv, sclv = off.numpy().reshape(ncc, 4, K), scl.numpy().reshape(ncc, 4, K)
         vdv = vd.numpy().reshape(ncc, NSPEC, 544)
+        ipsv = ips.numpy().reshape(NSPEC, 1, ncc * K)
+        ioffv, isclv = ioff.numpy().reshape(ncc, 1, K), iscl.numpy().reshape(ncc, 1, K)
 
         def e2e_step():
             pipe.run_host(hin)
             if world > 1:                   # the channel splice at the writer rank, host-staged
                 pipe.sync()
                 gather_splice(ctx, NCC, psv, offv, sclv, vdv)
+                gather_splice(ctx, NCC, ipsv, ioffv, isclv)
 
+        # the host link's own rate on this machine: one second of voltages
+        # pinned -> device with a single copy, beside the pipeline's numbers
+        dst = torch.empty(ncc * SECOND_BYTES, dtype=torch.int8, device="cuda")
+        dst.copy_(hin, non_blocking=True)
+        torch.cuda.synchronize()
+        l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0.record()
+        dst.copy_(hin, non_blocking=True)
+        l1.record()
+        l1.synchronize()
+        link_gbs = hin.numel() / (l0.elapsed_time(l1) / 1e3) / 1e9
+        del dst
+        torch.cuda.empty_cache()
         for _ in range(min(args.warmup, 3)):
             e2e_step()
         pipe.sync()
@@ -536,7 +557,10 @@ def gb300_arm(args, rank, local_rank, world):
                "h2d_bytes_per_step": ncc * SECOND_BYTES,
                "d2h_bytes_per_step": psr_b + vdif_b + stat_b,
                "steps": e2e_steps, "ms_per_step": 1e3 * e2e_s / e2e_steps,
-               "path": "vgb_pipeline_run_host from pinned host memory, products back to pinned host buffers; "
+               "h2d_link_gbs": link_gbs,
+               "link_bound": link_gbs * 1e9 / (ncc * SECOND_BYTES) * ncc_all / NCC,
+               "path": "vgb_pipeline_run_host from pinned host memory, products (tied-array PSRFITS rows, "
+                       "incoherent PSRFITS rows, VDIF frames, offsets, scales) back to pinned host buffers; "
                        "next second's copy overlaps this second's compute" +
                        ("; each rank's rows gathered and spliced at rank 0 (gloo, host-staged)" if world > 1 else "")}
     pipe.close()

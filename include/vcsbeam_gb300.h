@@ -9,8 +9,10 @@
  * wait that expired, a frame outside the described buffers, an input index
  * outside the voltage row).
  *
- * The VCSBeam library API (include/vcsbeam.h in this project, mirroring the
- * reference's include/vcsbeam.h.in) is implemented on top of these calls.
+ * VCSBeam's own GPU API (the vm* / cu_* functions of its src/pfb.cpp and
+ * src/form_beam.cpp, over its vcsbeam_context) is implemented on top of these
+ * calls in mwa-vcsbeam_gb300/csrc/compat/vm_compat.cu (libvcsbeam_compat.so),
+ * compiled against the VCSBeam build's own configured vcsbeam.h.
  * Each entry point below names the reference routine(s) it replaces;
  * file:line references are to the VCSBeam source tree.
  *
@@ -602,6 +604,16 @@ int vgb_pipeline_run_host(vgb_pipeline *p, const void *h_voltages, long long cur
  * psrfits [nspectra][nstokes][ncc*128] bytes (channel-spliced rows),
  * offsets/scales [ncc][nstokes][128], vdif [ncc][nspectra][544]. */
 int vgb_pipeline_fetch(vgb_pipeline *p, uint8_t *psrfits, float *offsets, float *scales, uint8_t *vdif);
+/* The incoherent beam of the last completed second as 8-bit PSRFITS rows
+ * (Stokes I; each coarse channel's incoherent sum renormalised per channel
+ * as cu_form_incoh_beam does, form_beam.cpp:463-505): psrfits
+ * [nspectra][ncc*128] bytes (channel-spliced), offsets/scales [ncc][128]
+ * (each nullable). Synchronises. */
+int vgb_pipeline_fetch_incoh(vgb_pipeline *p, uint8_t *psrfits, float *offsets, float *scales);
+/* Host buffers (each nullable) every following vgb_pipeline_run_* fills
+ * asynchronously with the incoherent beam's rows, offsets and scales, as
+ * vgb_pipeline_set_host_outputs does for the tied-array beam. */
+int vgb_pipeline_set_host_incoh(vgb_pipeline *p, uint8_t *psrfits, float *offsets, float *scales);
 /* Copy the last second's unquantised products to host buffers (each
  * nullable), as vmPullS / vmPullE do (form_beam.cpp:632-644):
  * S [ncc][nspectra][nstokes][128] float, e [ncc][nspectra][128][2] complex

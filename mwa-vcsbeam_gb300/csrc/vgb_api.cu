@@ -457,6 +457,8 @@ struct vgb_pipeline {
     float4 *d_ehist[2] = {};         // [cc][12][128]
     uint8_t *d_psrfits = nullptr;    // [ns][nstokes][ncc*128]
     float *d_off = nullptr, *d_scl = nullptr;
+    uint8_t *d_ipsr = nullptr;       // incoherent beam, Stokes I: [ns][ncc*128]
+    float *d_ioff = nullptr, *d_iscl = nullptr; // [ncc][128]
     uint8_t *d_vdif = nullptr;       // [cc][ns][544]
     uint32_t *d_hdr = nullptr;
     uint32_t *d_rstat = nullptr;     // [3][cc][stokes][128]: Stokes min / max keys, first-value NaN flags
@@ -466,6 +468,8 @@ struct vgb_pipeline {
     // asynchronous host outputs
     uint8_t *h_psrfits = nullptr, *h_vdif = nullptr;
     float *h_off = nullptr, *h_scl = nullptr;
+    uint8_t *h_ipsr = nullptr;
+    float *h_ioff = nullptr, *h_iscl = nullptr;
     // per-second tracking (vmCalcJonesAndDelays): caller's device tables and
     // the pipeline's own second counter, pointing, B and beam-model scratch
     bool tracking = false;
@@ -572,6 +576,12 @@ int pipeline_second(vgb_pipeline *p, const char2 *volt, long long cc_stride_byte
                           (long long)c.ncc * kK, p->d_off, p->d_scl, p->d_rstat, p->s_comp);
     if (rc) return rc;
     p->launches++;
+    // the incoherent beam's 8-bit rows (Stokes I, spliced the same way; its
+    // renormalise as cu_form_incoh_beam's, form_beam.cpp:495-497)
+    rc = renormalise_impl(p->d_incoh, c.ncc, 1, p->nspectra, 1, kK, p->d_ipsr, kK, 0, (long long)c.ncc * kK,
+                          (long long)c.ncc * kK, p->d_ioff, p->d_iscl, nullptr, p->s_comp);
+    if (rc) return rc;
+    p->launches++;
     // the next second's extremes start empty
     rc = reset_rstat(p);
     if (rc) return rc;
@@ -620,6 +630,17 @@ int pipeline_second(vgb_pipeline *p, const char2 *volt, long long cc_stride_byte
         rc = check_cuda(cudaMemcpyAsync(p->h_vdif, p->d_vdif, (size_t)c.ncc * ns * 544, cudaMemcpyDeviceToHost,
                                         p->s_comp),
                         "D2H vdif");
+    if (!rc && p->h_ipsr)
+        rc = check_cuda(cudaMemcpyAsync(p->h_ipsr, p->d_ipsr, ns * c.ncc * kK, cudaMemcpyDeviceToHost, p->s_comp),
+                        "D2H incoherent psrfits");
+    if (!rc && p->h_ioff)
+        rc = check_cuda(cudaMemcpyAsync(p->h_ioff, p->d_ioff, sizeof(float) * c.ncc * kK, cudaMemcpyDeviceToHost,
+                                        p->s_comp),
+                        "D2H incoherent offsets");
+    if (!rc && p->h_iscl)
+        rc = check_cuda(cudaMemcpyAsync(p->h_iscl, p->d_iscl, sizeof(float) * c.ncc * kK, cudaMemcpyDeviceToHost,
+                                        p->s_comp),
+                        "D2H incoherent scales");
     return rc;
 }
 
@@ -636,7 +657,8 @@ int pipeline_second_graph(vgb_pipeline *p, const char2 *volt, long long cc_strid
     if (!p->use_graphs || p->timing) return pipeline_second(p, volt, cc_stride_bytes);
     const int parity = (int)(p->second & 1);
     const bool first = p->second == 0;
-    const void *hout = p->h_psrfits ? (const void *)p->h_psrfits : (const void *)p->h_vdif;
+    const void *hout = p->h_psrfits ? (const void *)p->h_psrfits
+                                    : p->h_vdif ? (const void *)p->h_vdif : (const void *)p->h_ipsr;
     for (auto &g : p->graphs)
         if (g.volt == volt && g.stride == cc_stride_bytes && g.parity == parity && g.first == first && g.hout == hout) {
             int rc = check_cuda(cudaGraphLaunch(g.exec, p->s_comp), "cudaGraphLaunch");
@@ -712,6 +734,9 @@ int vgb_pipeline_create(const vgb_pipeline_config *cfg, vgb_pipeline **out)
     rc = rc ? rc : dalloc(&p->d_e, sizeof(float4) * ncc * ns * kK);
     rc = rc ? rc : dalloc(&p->d_incoh, sizeof(float) * ncc * ns * kK);
     rc = rc ? rc : dalloc(&p->d_psrfits, (size_t)ns * cfg->nstokes * ncc * kK);
+    rc = rc ? rc : dalloc(&p->d_ipsr, (size_t)ns * ncc * kK);
+    rc = rc ? rc : dalloc(&p->d_ioff, sizeof(float) * ncc * kK);
+    rc = rc ? rc : dalloc(&p->d_iscl, sizeof(float) * ncc * kK);
     rc = rc ? rc : dalloc(&p->d_off, sizeof(float) * ncc * cfg->nstokes * kK);
     rc = rc ? rc : dalloc(&p->d_scl, sizeof(float) * ncc * cfg->nstokes * kK);
     if (cfg->do_ipfb) rc = rc ? rc : dalloc(&p->d_vdif, (size_t)ncc * ns * 544);
@@ -753,7 +778,7 @@ int vgb_pipeline_destroy(vgb_pipeline *p)
     void *bufs[] = {p->d_filter, p->d_coeffs, p->d_W, p->d_volt[0], p->d_volt[1], p->d_hist[0], p->d_hist[1],
                     p->d_S, p->d_e, p->d_incoh, p->d_ehist[0], p->d_ehist[1], p->d_psrfits, p->d_off, p->d_scl,
                     p->d_vdif, p->d_hdr, p->d_rstat, p->d_trk_counter, p->d_trk_cur, p->d_trk_B,
-                    p->d_trk_scratch};
+                    p->d_trk_scratch, p->d_ipsr, p->d_ioff, p->d_iscl};
     for (void *b : bufs)
         if (b) cudaFree(b);
     for (int i = 0; i < 6; i++)
@@ -980,6 +1005,38 @@ int vgb_pipeline_fetch(vgb_pipeline *p, uint8_t *psrfits, float *offsets, float 
     rc = check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
     if (rc) return rc;
     return vgb_check_device_status(p->s_comp, nullptr);
+}
+
+int vgb_pipeline_fetch_incoh(vgb_pipeline *p, uint8_t *psrfits, float *offsets, float *scales)
+{
+    if (!p) return set_error(VGB_ERR_INVALID, "NULL pipeline");
+    const size_t ns = p->nspectra, ncc = p->cfg.ncc;
+    int rc = VGB_SUCCESS;
+    if (psrfits)
+        rc = check_cuda(cudaMemcpyAsync(psrfits, p->d_ipsr, ns * ncc * kK, cudaMemcpyDeviceToHost, p->s_comp),
+                        "D2H incoherent psrfits");
+    if (!rc && offsets)
+        rc = check_cuda(cudaMemcpyAsync(offsets, p->d_ioff, sizeof(float) * ncc * kK, cudaMemcpyDeviceToHost,
+                                        p->s_comp),
+                        "D2H incoherent offsets");
+    if (!rc && scales)
+        rc = check_cuda(cudaMemcpyAsync(scales, p->d_iscl, sizeof(float) * ncc * kK, cudaMemcpyDeviceToHost,
+                                        p->s_comp),
+                        "D2H incoherent scales");
+    if (rc) return rc;
+    return check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
+}
+
+int vgb_pipeline_set_host_incoh(vgb_pipeline *p, uint8_t *psrfits, float *offsets, float *scales)
+{
+    if (!p) return set_error(VGB_ERR_INVALID, "NULL pipeline");
+    int rc = check_cuda(cudaStreamSynchronize(p->s_comp), "sync");
+    if (rc) return rc;
+    drop_graphs(p); // graphs captured the previous destinations
+    p->h_ipsr = psrfits;
+    p->h_ioff = offsets;
+    p->h_iscl = scales;
+    return VGB_SUCCESS;
 }
 
 int vgb_pipeline_fetch_raw(vgb_pipeline *p, float *S_, void *e, float *incoh)

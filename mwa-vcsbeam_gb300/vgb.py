@@ -193,6 +193,8 @@ _SIGS = {
     "vgb_pipeline_run_host": (I, [V, V, LL]),
     "vgb_pipeline_fetch": (I, [V, V, V, V, V]),
     "vgb_pipeline_fetch_raw": (I, [V, V, V, V]),
+    "vgb_pipeline_fetch_incoh": (I, [V, V, V, V]),
+    "vgb_pipeline_set_host_incoh": (I, [V, V, V, V]),
     "vgb_pipeline_device_products": (I, [V, ctypes.POINTER(V), ctypes.POINTER(V), ctypes.POINTER(V),
                                          ctypes.POINTER(V), ctypes.POINTER(V)]),
     "vgb_pipeline_launch_count": (I, [V]),
@@ -762,6 +764,14 @@ class Pipeline:
 
     def fetch(self, psrfits=None, offsets=None, scales=None, vdif=None):
         check(lib().vgb_pipeline_fetch(self.h, ptr(psrfits), ptr(offsets), ptr(scales), ptr(vdif)))
+
+    def fetch_incoh(self, psrfits=None, offsets=None, scales=None):
+        """The incoherent beam's 8-bit rows [ns][ncc*128], offsets and scales [ncc][128]."""
+        check(lib().vgb_pipeline_fetch_incoh(self.h, ptr(psrfits), ptr(offsets), ptr(scales)))
+
+    def set_host_incoh(self, psrfits=None, offsets=None, scales=None):
+        self._host_incoh = (psrfits, offsets, scales)  # keep them alive
+        check(lib().vgb_pipeline_set_host_incoh(self.h, ptr(psrfits), ptr(offsets), ptr(scales)))
 
     def fetch_raw(self, S=None, e=None, incoh=None):
         check(lib().vgb_pipeline_fetch_raw(self.h, ptr(S), ptr(e), ptr(incoh)))

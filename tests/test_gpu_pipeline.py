@@ -161,7 +161,7 @@ def test_pipeline_graph_replay_equals_eager(vgb_mod, torch, setup):
             vd = np.empty((NCC, NS, 544), np.uint8)
             p.fetch(ps, None, None, vd)
             res.append((ps, vd))
-            assert p.launch_count() == 5      # beam, renormalise, inverse PFB, VDIF headers, history
+            assert p.launch_count() == 6      # beam, renormalise x2 (tied-array, incoherent), inverse PFB, VDIF headers, history
         p.close()
         outs.append(res)
     for (a, b), (c, d) in zip(outs[0], outs[1]):
@@ -388,3 +388,41 @@ def test_pipeline_tracking_rebuilds_weights_every_second(vgb_mod, torch, oracle_
             assert rel_err(outs[0][2][cc], Sref[0]) < 1e-5, (t, cc)
     pt.close()
     pw.close()
+
+
+def test_pipeline_incoherent_beam_psrfits(vgb_mod, torch, oracle_mod, setup):
+    """The incoherent beam's 8-bit rows (Stokes I, spliced across the two
+    coarse channels) over two seconds: bit for bit the oracle's renormalise
+    of the device's incoherent sums, and within one LSB on <= 1e-4 of samples
+    of the oracle's renormalise of the oracle's own incoherent sums (the sum
+    of |v|^2 over the RF inputs of the oracle's fine channels); the same rows
+    land in host buffers given to vgb_pipeline_set_host_incoh."""
+    volt, filt, syn, tabs = setup
+    invw = 1.0 / NI
+    p = make_pipeline(vgb_mod, torch, filt, syn, tabs, invw)
+    hps = np.zeros((NS, NCC * K), np.uint8)
+    hoff = np.zeros((NCC, K), np.float32)
+    hsc = np.zeros((NCC, K), np.float32)
+    p.set_host_incoh(hps, hoff, hsc)
+    for t in range(2):
+        p.run_device(dev(volt[t].reshape(-1).view(np.uint8)))
+        ps = np.empty((NS, NCC * K), np.uint8)
+        off = np.empty((NCC, K), np.float32)
+        sc = np.empty((NCC, K), np.float32)
+        p.fetch_incoh(ps, off, sc)
+        p.sync()
+        assert np.array_equal(hps, ps) and np.array_equal(hoff, off) and np.array_equal(hsc, sc)
+        inc = np.empty((NCC, NS, K), np.float32)
+        p.fetch_raw(incoh=inc)
+        for cc in range(NCC):
+            o, s_, u = oracle_mod.renormalise(inc[cc][None, :, None, :])
+            assert np.array_equal(ps[:, cc * K:(cc + 1) * K], u[0][:, 0])
+            assert np.array_equal(off[cc], o[0][0]) and np.array_equal(sc[cc], s_[0][0])
+            margin = np.zeros((1, NI, 64000, 2), np.int8) if t == 0 else volt[t - 1, cc, NBLK - 1:]
+            buf = np.ascontiguousarray(np.concatenate([margin, volt[t, cc]], axis=0))
+            v = oracle_mod.fpfb(buf, NI, NS, filt, K, P, np.arange(NI, dtype=np.int32), 0)
+            iref = (np.abs(v) ** 2).sum(axis=-1).astype(np.float32)
+            _, _, uref = oracle_mod.renormalise(iref[None, :, None, :])
+            d8 = np.abs(ps[:, cc * K:(cc + 1) * K].astype(np.int16) - uref[0][:, 0].astype(np.int16))
+            assert (d8 > 1).mean() <= 1e-4 and (d8 > 0).mean() <= 1e-3, (t, cc)
+    p.close()
