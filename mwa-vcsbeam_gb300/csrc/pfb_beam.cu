@@ -129,6 +129,47 @@ __device__ __forceinline__ void produce(FrontSmemT<G> &sm, const VoltView &vv, i
     }
 }
 
+// Producer of the beamformer kernel, spread over warps so that no warp
+// carries all of a step's copy set-up (every warp meets at the step's block
+// barriers, where the most loaded one sets the pace): lane 0 of warp li
+// (li < G) copies input it * G + li's frames, lane 0 of warp G the two Jones
+// rows of the step's tiles, and lane 0 of warp 0 posts the step's expected
+// byte count first. Each issuer completes its own shortfall when frames fell
+// outside the buffers (the status word records that). The transaction count
+// may be consumed before it is posted; the phase still cannot complete before
+// warp 0's arrival. Called by every thread after the step's first block
+// barrier, as produce() is.
+template <int G>
+__device__ __forceinline__ void produce_spread(FrontSmemT<G> &sm, const VoltView &vv, int cc, int it, int m0,
+                                              int nspectra, const CUtensorMap *wmap, unsigned *status)
+{
+    if ((threadIdx.x & 31) != 0) return;
+    const int warp = threadIdx.x >> 5;
+    const int s = it & 1;
+    const int w_end = min(m0 + kWin, nspectra + kP - 1);
+    const uint32_t per_input = (w_end - m0) * kFrameBytes;
+    constexpr uint32_t kWBytes = (G / 2) * kK * 16;   // one Jones row of G/2 tiles
+    if (warp == 0) {
+        uint32_t total = 2 * kWBytes;
+        for (int li = 0; li < G; li++)
+            if (it * G + li < vv.ninputs) total += per_input;
+        mbar_arrive_expect_tx(&sm.bar[s], total);
+    }
+    if (warp < G) {
+        const int pos = it * G + warp;
+        if (pos < vv.ninputs) {
+            const uint32_t issued = issue_frames(vv, cc, pos, m0, w_end, sm.stage[s][warp][0], &sm.bar[s], status);
+            if (issued != per_input)
+                asm volatile("mbarrier.complete_tx.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&sm.bar[s])),
+                             "r"(per_input - issued)
+                             : "memory");
+        }
+    } else if (warp == G) {
+        tma_load_5d(sm.wst[s][0][0], wmap, 0, 0, 0, (G / 2) * it, cc, &sm.bar[s]);
+        tma_load_5d(sm.wst[s][1][0], wmap, 0, 1, 0, (G / 2) * it, cc, &sm.bar[s]);
+    }
+}
+
 // Four int8 values (two char2) -> packed floats (re0, re1), (im0, im1), exact,
 // via the 2^23 magic number: bytes are offset to unsigned, placed under the
 // exponent of 2^23 and the 2^23 + 128 bias subtracted.
@@ -353,7 +394,7 @@ __global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1)
     const int li = tid >> 6, n0 = 2 * (tid & 63);
     load_taps(a.filter, n0, hc);
     __syncthreads();
-    if (tid < 32) produce(sm, a.vv, cc, 0, m0, a.nspectra, &wmap, a.status);
+    produce_spread(sm, a.vv, cc, 0, m0, a.nspectra, &wmap, a.status);
 
     // beam accumulators for (k', m = mh + kMh mi)
     const int kp = tid & (kK - 1), mh = tid >> 7;
@@ -369,7 +410,7 @@ __global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1)
             return;
         }
         // everyone has finished step it-1, so its buffers may be refilled
-        if (tid < 32 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, &wmap, a.status);
+        if (it + 1 < nsteps) produce_spread(sm, a.vv, cc, it + 1, m0, a.nspectra, &wmap, a.status);
         wola_step<kInt32, kFpga>(sm, it & 1, li, n0, hc);
         input_barrier(li);
         fft_step<kDemote, kFpga>(sm, tid);
