@@ -938,7 +938,9 @@ def surrogate_section(torch, vgb, SY, steps: int):
         return e0.elapsed_time(e1) / n, r
 
     out = {"workload": "MLP 6 -> 4 x 256 GELU -> 8, BF16 weights, FP32 accumulate; trained on the analytic tile "
-                       "model (16 delay sets x 24 frequencies 80-300 MHz x 65,536 directions above 10 deg); "
+                       "model that stands in for the FEE model (FEE parity unpinned: mwa_hyperbeam and its HDF5 "
+                       "table are not available) (16 delay sets x 24 frequencies 80-300 MHz x 65,536 directions "
+                       "above 10 deg); "
                        "queries: 1024 beams (32 x 32 grid, 0.4 deg, around the tiles' pointing) x 128 tiles "
                        "(trained delay set 0) x 24 frequencies, re-pointed every second for 10 s",
            "train_steps": steps, "train_s": train_s, "ms_per_train_step": 1e3 * train_s / max(steps, 1),
@@ -988,8 +990,9 @@ def main():
     ap.add_argument("--mb-stream-iters", type=int, default=3, help="many-beam host-streaming calls timed (0: skip)")
     ap.add_argument("--no-pfb-only", dest="pfb_only", action="store_false",
                     help="skip the PFB-only (fine_pfb_offline) section")
-    ap.add_argument("--pfb-variant", type=int, default=0, choices=[0, 4, 8],
-                    help="profiling: force the fused front end's inputs per step (0 = timed choice)")
+    ap.add_argument("--pfb-variant", type=int, default=0, choices=[0, 3, 4, 8],
+                    help="profiling: force the fused front end's variant (4 or 8 inputs per step, 3 the "
+                         "warp-specialised kernel; 0 = timed choice)")
     ap.add_argument("--beam-sweep", action="store_true",
                     help="time 1..1024 beams per coarse channel-second on both beamformers and print their JSON")
     ap.add_argument("--traffic", type=float, default=None,

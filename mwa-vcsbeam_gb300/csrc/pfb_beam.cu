@@ -203,10 +203,12 @@ __device__ __forceinline__ float fpga_round(float X)
 // ---------------------------------------------------------------------------
 // Steps 2-3: weighted overlap-add for thread (li, n0..n0+1) into buf rows.
 // ---------------------------------------------------------------------------
-template <bool kInt32, bool kFpga, int G>
-__device__ __forceinline__ void wola_step(FrontSmemT<G> &sm, int s, int li, int n0, const int (&hc)[2][kP])
+// stage_in: the input's kWin staged frames [w][kK]; rows: its kT output rows.
+template <bool kInt32, bool kFpga>
+__device__ __forceinline__ void wola_rows(const char2 *stage_in, float2 (*rows)[kFftRow], int n0,
+                                          const int (&hc)[2][kP])
 {
-    const uint32_t *x = reinterpret_cast<const uint32_t *>(sm.stage[s][li][0] + n0);
+    const uint32_t *x = reinterpret_cast<const uint32_t *>(stage_in + n0);
     if (kInt32) {
         int ar[kT][2], ai[kT][2];
 #pragma unroll
@@ -240,7 +242,7 @@ __device__ __forceinline__ void wola_step(FrontSmemT<G> &sm, int s, int li, int 
                 b = make_float4((float)ar[m][0] * sc, (float)ai[m][0] * sc, (float)ar[m][1] * sc,
                                 (float)ai[m][1] * sc);
             }
-            *reinterpret_cast<float4 *>(&sm.buf[li * kT + m][n0]) = b;
+            *reinterpret_cast<float4 *>(&rows[m][n0]) = b;
         }
     } else {
         // Without FPGA rounding the output scale 2^-14 / K (a power of two)
@@ -274,9 +276,15 @@ __device__ __forceinline__ void wola_step(FrontSmemT<G> &sm, int s, int li, int 
             } else {
                 b = make_float4(ar[m].x, ai[m].x, ar[m].y, ai[m].y);
             }
-            *reinterpret_cast<float4 *>(&sm.buf[li * kT + m][n0]) = b;
+            *reinterpret_cast<float4 *>(&rows[m][n0]) = b;
         }
     }
+}
+
+template <bool kInt32, bool kFpga, int G>
+__device__ __forceinline__ void wola_step(FrontSmemT<G> &sm, int s, int li, int n0, const int (&hc)[2][kP])
+{
+    wola_rows<kInt32, kFpga>(sm.stage[s][li][0], &sm.buf[li * kT], n0, hc);
 }
 
 // vcsbeam.h.in:453-456: (int)round(x) clipped to [-8, 7].
@@ -291,12 +299,12 @@ __device__ __forceinline__ float demote4(float x)
 // kScale: apply the 1/K here (after FPGA rounding); without FPGA rounding the
 // WOLA output already carries it (scaling by a power of two commutes exactly
 // with the FFT's arithmetic).
-template <bool kDemote, bool kScale, int G>
-__device__ __forceinline__ void fft_step(FrontSmemT<G> &sm, int tid)
+template <bool kDemote, bool kScale>
+__device__ __forceinline__ void fft_rows(float2 (*buf)[kFftRow], const float2 *tw, int tid)
 {
     const int g = tid >> 3, j = tid & 7;
-    float2 *row = sm.buf[g];
-    fft128_pass1<-1>(row, sm.tw, j);
+    float2 *row = buf[g];
+    fft128_pass1<-1>(row, tw, j);
     __syncwarp();
     float2 out[2][8];
     fft128_pass2<-1>(row, j, out);
@@ -317,14 +325,26 @@ __device__ __forceinline__ void fft_step(FrontSmemT<G> &sm, int tid)
         }
 }
 
-template <int G> __device__ __forceinline__ void init_front(FrontSmemT<G> &sm, int tid)
+template <bool kDemote, bool kScale, int G>
+__device__ __forceinline__ void fft_step(FrontSmemT<G> &sm, int tid)
+{
+    fft_rows<kDemote, kScale>(sm.buf, sm.tw, tid);
+}
+
+// W128 twiddles at fft128_tw_slot(k1, j), by threads 0..127.
+__device__ __forceinline__ void init_twiddles(float2 *tw, int tid)
 {
     if (tid < 128) {
         const int k1 = tid >> 3, j = tid & 7;
         double sn, cs;
         sincospi((double)(j * k1) / 64.0, &sn, &cs);
-        sm.tw[fft128_tw_slot(k1, j)] = make_float2((float)cs, (float)sn);
+        tw[fft128_tw_slot(k1, j)] = make_float2((float)cs, (float)sn);
     }
+}
+
+template <int G> __device__ __forceinline__ void init_front(FrontSmemT<G> &sm, int tid)
+{
+    init_twiddles(sm.tw, tid);
     if (tid == 0) {
         mbar_init(&sm.bar[0], 1);
         mbar_init(&sm.bar[1], 1);
@@ -365,6 +385,82 @@ template <int G> __device__ __forceinline__ void drain(FrontSmemT<G> &sm, int it
 {
     if (threadIdx.x == 0) mbar_wait_bounded(&sm.bar[it & 1], (it >> 1) & 1, 1u << 20);
     __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Beamformer back end, shared by both beamformer kernels so that they give
+// identical results.
+// ---------------------------------------------------------------------------
+// One tile's contribution to (k', spectrum) (form_beam.cpp:174-177, 295-315):
+// ex / ey = the two Jones rows wa = (w00, w01), wb = (w10, w11) times the
+// tile's (Q, P) voltages; c[0..3] += ex, ey; c[4..7] += |ex|^2, |ey|^2, ex ey*;
+// c[8] += |vq|^2 + |vp|^2 (the incoherent sum).
+__device__ __forceinline__ void beam_accumulate(float *c, float4 wa, float4 wb, float2 vq, float2 vp)
+{
+    const float exr = wa.x * vq.x - wa.y * vq.y + wa.z * vp.x - wa.w * vp.y;
+    const float exi = wa.x * vq.y + wa.y * vq.x + wa.z * vp.y + wa.w * vp.x;
+    const float eyr = wb.x * vq.x - wb.y * vq.y + wb.z * vp.x - wb.w * vp.y;
+    const float eyi = wb.x * vq.y + wb.y * vq.x + wb.z * vp.y + wb.w * vp.x;
+    c[0] += exr;
+    c[1] += exi;
+    c[2] += eyr;
+    c[3] += eyi;
+    c[4] = fmaf(exr, exr, fmaf(exi, exi, c[4]));
+    c[5] = fmaf(eyr, eyr, fmaf(eyi, eyi, c[5]));
+    c[6] = fmaf(exr, eyr, fmaf(exi, eyi, c[6]));
+    c[7] = fmaf(exi, eyr, fmaf(-exr, eyi, c[7]));
+    c[8] = fmaf(vq.x, vq.x, fmaf(vq.y, vq.y, fmaf(vp.x, vp.x, fmaf(vp.y, vp.y, c[8]))));
+}
+
+// form_beam.cpp:322-338: Stokes of spectrum m (skipped past the second's
+// end), e, the incoherent sum, and the running extremes for the 8-bit stage.
+__device__ __forceinline__ void beam_store(const BeamArgs &a, int cc, int m, int kp, const float *c, uint32_t (&kmn)[4],
+                                           uint32_t (&kmx)[4])
+{
+    if (m >= a.nspectra) return;
+    const float bnXX = c[0] * c[0] + c[1] * c[1] - c[4];
+    const float bnYY = c[2] * c[2] + c[3] * c[3] - c[5];
+    const float bxr = c[0] * c[2] + c[1] * c[3] - c[6];
+    const float bxi = c[1] * c[2] - c[0] * c[3] - c[7];
+    float *S = a.S + cc * a.S_cc + ((long long)m * a.nstokes) * kK + kp;
+    const float sv[4] = {a.invw * (bnXX + bnYY), a.invw * (bnXX - bnYY), 2.0f * a.invw * bxr,
+                         -2.0f * a.invw * bxi};
+    S[0] = sv[0];
+    if (a.nstokes == 4) {
+        S[kK] = sv[1];
+        S[2 * kK] = sv[2];
+        S[3 * kK] = sv[3];
+    }
+    if (a.st_mn) {
+#pragma unroll
+        for (int st = 0; st < 4; st++) {
+            if (st >= a.nstokes) break;
+            if (isnan(sv[st])) {
+                if (m == 0) a.st_nan0[(long long)(cc * a.nstokes + st) * kK + kp] = 1u;
+            } else {
+                const uint32_t k = fkey(sv[st]);
+                kmn[st] = min(kmn[st], k);
+                kmx[st] = max(kmx[st], k);
+            }
+        }
+    }
+    if (a.e) a.e[cc * a.e_cc + (long long)m * kK + kp] = make_float4(c[0], c[1], c[2], c[3]);
+    if (a.incoh) a.incoh[cc * a.inc_cc + (long long)m * kK + kp] = c[8];
+}
+
+// The row extremes for the 8-bit stage (min and max are idempotent, so a
+// repeated launch over the same data leaves them unchanged).
+__device__ __forceinline__ void beam_store_extremes(const BeamArgs &a, int cc, int kp, const uint32_t (&kmn)[4],
+                                                    const uint32_t (&kmx)[4])
+{
+    if (!a.st_mn) return;
+#pragma unroll
+    for (int st = 0; st < 4; st++) {
+        if (st >= a.nstokes) break;
+        const long long r = (long long)(cc * a.nstokes + st) * kK + kp;
+        if (kmn[st] != ~0u) atomicMin(&a.st_mn[r], kmn[st]);
+        if (kmx[st] != 0u) atomicMax(&a.st_mx[r], kmx[st]);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -424,73 +520,200 @@ __global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1)
 #pragma unroll
             for (int mi = 0; mi < kMi; mi++) {
                 const int m = mh + kMh * mi;
-                const float2 vq = sm.buf[(2 * aa) * kT + m][kp];
-                const float2 vp = sm.buf[(2 * aa + 1) * kT + m][kp];
-                const float exr = wa.x * vq.x - wa.y * vq.y + wa.z * vp.x - wa.w * vp.y;
-                const float exi = wa.x * vq.y + wa.y * vq.x + wa.z * vp.y + wa.w * vp.x;
-                const float eyr = wb.x * vq.x - wb.y * vq.y + wb.z * vp.x - wb.w * vp.y;
-                const float eyi = wb.x * vq.y + wb.y * vq.x + wb.z * vp.y + wb.w * vp.x;
-                float *c = acc[mi];
-                c[0] += exr;
-                c[1] += exi;
-                c[2] += eyr;
-                c[3] += eyi;
-                c[4] = fmaf(exr, exr, fmaf(exi, exi, c[4]));
-                c[5] = fmaf(eyr, eyr, fmaf(eyi, eyi, c[5]));
-                c[6] = fmaf(exr, eyr, fmaf(exi, eyi, c[6]));
-                c[7] = fmaf(exi, eyr, fmaf(-exr, eyi, c[7]));
-                c[8] = fmaf(vq.x, vq.x, fmaf(vq.y, vq.y, fmaf(vp.x, vp.x, fmaf(vp.y, vp.y, c[8]))));
+                beam_accumulate(acc[mi], wa, wb, sm.buf[(2 * aa) * kT + m][kp], sm.buf[(2 * aa + 1) * kT + m][kp]);
             }
         }
     }
 
-    // form_beam.cpp:322-338
     uint32_t kmn[4] = {~0u, ~0u, ~0u, ~0u}, kmx[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
-    for (int mi = 0; mi < kMi; mi++) {
-        const int m = m0 + mh + kMh * mi;
-        if (m >= a.nspectra) continue;
-        const float *c = acc[mi];
-        const float bnXX = c[0] * c[0] + c[1] * c[1] - c[4];
-        const float bnYY = c[2] * c[2] + c[3] * c[3] - c[5];
-        const float bxr = c[0] * c[2] + c[1] * c[3] - c[6];
-        const float bxi = c[1] * c[2] - c[0] * c[3] - c[7];
-        float *S = a.S + cc * a.S_cc + ((long long)m * a.nstokes) * kK + kp;
-        const float sv[4] = {a.invw * (bnXX + bnYY), a.invw * (bnXX - bnYY), 2.0f * a.invw * bxr,
-                             -2.0f * a.invw * bxi};
-        S[0] = sv[0];
-        if (a.nstokes == 4) {
-            S[kK] = sv[1];
-            S[2 * kK] = sv[2];
-            S[3 * kK] = sv[3];
+    for (int mi = 0; mi < kMi; mi++) beam_store(a, cc, m0 + mh + kMh * mi, kp, acc[mi], kmn, kmx);
+    beam_store_extremes(a, cc, kp, kmn, kmx);
+}
+
+// ---------------------------------------------------------------------------
+// Warp-specialised beamformer kernel (variant 3, selected only when forced
+// with vgb_pfb_variant(3): on a GB300 it took 26.0 ms per data-second of the
+// full band against beam_kernel<..., 4>'s 21.5 ms -- one 416-thread CTA per
+// SM, about three warps per scheduler, hides the WOLA's and FFT's latencies
+// worse than two 256-thread CTAs do, and the double-buffered rows leave no
+// shared memory for a second CTA). The same arithmetic as
+// beam_kernel<..., 4> with the roles split across warps and no block-wide
+// barrier inside the loop. One CTA per SM of 416 threads:
+//   warps 0-7  front: WOLA + FFT of the step's four inputs (two warps per
+//              input, as in beam_kernel), rows into a double-buffered array;
+//   warps 8-11 back: one fine channel per thread and all 8 spectra, summing
+//              tiles in order as beam_kernel does (identical results);
+//   warp 12    producer: lane 0 issues the frames and the weights.
+// Six mbarrier rings of two coordinate them: frames full (TMA) / empty
+// (front), weights full (TMA) / empty (back), rows full (front) / empty
+// (back), so the front works on step it while the back sums step it - 1.
+// Every wait is bounded; a wait that gives up raises the status word and an
+// abort flag the other roles see at their next wait; the two warps of an
+// input agree before either leaves (they share a named barrier), and the
+// producer lets its last copies land before the CTA exits.
+// ---------------------------------------------------------------------------
+constexpr int kWsFront = 64 * kG;               // 256
+constexpr int kWsBack = kK;                     // 128
+constexpr int kWsThreads = kWsFront + kWsBack + 32;
+
+struct WsSmem {
+    char2 stage[2][kG][kWin][kK];               // frames (TMA)
+    float4 wst[2][2][kG / 2][kK];               // weights (TMA): [stage][row][tile][k']
+    float2 buf[2][kG * kT][kFftRow];            // rows: front -> back, double-buffered
+    float2 tw[128];
+    uint64_t ffull[2], fempty[2], wfull[2], wempty[2], rfull[2], rempty[2];
+    int abort;
+};
+static_assert(offsetof(WsSmem, wst) % 128 == 0 && offsetof(WsSmem, tw) % 16 == 0, "TMA / vector alignment");
+
+__device__ __forceinline__ bool ws_wait(volatile int *abort, uint64_t *bar, uint32_t parity, unsigned *status)
+{
+    if (*abort) return false;
+    if (mbar_wait_bounded(bar, parity, 1u << 22)) return true;
+    *abort = 1;
+    atomicOr(status, kErrWaitTimeout);
+    return false;
+}
+
+// True on all 64 threads of input li's two warps if `pred` holds on any.
+__device__ __forceinline__ bool pair_any(int li, bool pred)
+{
+    uint32_t r;
+    asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, %2, 64, p;\n"
+                 " selp.u32 %0, 1, 0, q;\n}\n"
+                 : "=r"(r)
+                 : "r"((uint32_t)pred), "r"(1 + li)
+                 : "memory");
+    return r != 0;
+}
+
+template <bool kInt32, bool kFpga, bool kDemote>
+__global__ void __launch_bounds__(kWsThreads, 1)
+    beam_ws_kernel(const BeamArgs a, const __grid_constant__ CUtensorMap wmap)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    WsSmem &sm = *reinterpret_cast<WsSmem *>(smem_raw);
+    volatile int *abort = &sm.abort;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int cc = blockIdx.y;
+    const int m0 = blockIdx.x * kT;
+    const int nsteps = (a.vv.ninputs + kG - 1) / kG;
+
+    init_twiddles(sm.tw, tid);
+    if (tid == 0) {
+        for (int s = 0; s < 2; s++) {
+            mbar_init(&sm.ffull[s], 1);
+            mbar_init(&sm.wfull[s], 1);
+            mbar_init(&sm.fempty[s], kWsFront / 32);
+            mbar_init(&sm.rfull[s], kWsFront / 32);
+            mbar_init(&sm.rempty[s], kWsBack / 32);
+            mbar_init(&sm.wempty[s], kWsBack / 32);
         }
-        if (a.st_mn) {
-#pragma unroll
-            for (int st = 0; st < 4; st++) {
-                if (st >= a.nstokes) break;
-                if (isnan(sv[st])) {
-                    if (m == 0) a.st_nan0[(long long)(cc * a.nstokes + st) * kK + kp] = 1u;
-                } else {
-                    const uint32_t k = fkey(sv[st]);
-                    kmn[st] = min(kmn[st], k);
-                    kmx[st] = max(kmx[st], k);
+        sm.abort = 0;
+        fence_mbar_init();
+    }
+    if (tid == kWsFront + kWsBack) prefetch_tmap(&wmap);
+    __syncthreads();
+
+    if (tid >= kWsFront + kWsBack) {
+        // ---- producer ----
+        int last_it_f = -1, last_it_w = -1; // the last steps whose frames / weights were issued
+        if (lane == 0) {
+            constexpr uint32_t kWBytes = (kG / 2) * kK * 16;
+            for (int it = 0; it < nsteps; it++) {
+                const int s = it & 1, k = it >> 1;
+                if (k > 0 && !ws_wait(abort, &sm.fempty[s], (k - 1) & 1, a.status)) break;
+                const int w_end = min(m0 + kWin, a.nspectra + kP - 1);
+                const uint32_t per_input = (w_end - m0) * kFrameBytes;
+                uint32_t total = 0;
+                for (int li = 0; li < kG; li++)
+                    if (it * kG + li < a.vv.ninputs) total += per_input;
+                mbar_arrive_expect_tx(&sm.ffull[s], total);
+                for (int li = 0; li < kG; li++) {
+                    const int pos = it * kG + li;
+                    if (pos >= a.vv.ninputs) break;
+                    const uint32_t got =
+                        issue_frames(a.vv, cc, pos, m0, w_end, sm.stage[s][li][0], &sm.ffull[s], a.status);
+                    if (got != per_input)
+                        asm volatile("mbarrier.complete_tx.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&sm.ffull[s])),
+                                     "r"(per_input - got)
+                                     : "memory");
                 }
+                last_it_f = it;
+                if (k > 0 && !ws_wait(abort, &sm.wempty[s], (k - 1) & 1, a.status)) break;
+                mbar_arrive_expect_tx(&sm.wfull[s], 2 * kWBytes);
+                tma_load_5d(sm.wst[s][0][0], &wmap, 0, 0, 0, (kG / 2) * it, cc, &sm.wfull[s]);
+                tma_load_5d(sm.wst[s][1][0], &wmap, 0, 1, 0, (kG / 2) * it, cc, &sm.wfull[s]);
+                last_it_w = it;
             }
         }
-        if (a.e) a.e[cc * a.e_cc + (long long)m * kK + kp] = make_float4(c[0], c[1], c[2], c[3]);
-        if (a.incoh) a.incoh[cc * a.inc_cc + (long long)m * kK + kp] = c[8];
+        __syncthreads();
+        // after an abort, let the copies this CTA issued land before it exits
+        // (the two most recent steps' copies, one per stage, may be in flight)
+        if (lane == 0 && *abort) {
+            for (int it = max(0, last_it_f - 1); it <= last_it_f; it++)
+                mbar_wait_bounded(&sm.ffull[it & 1], (it >> 1) & 1, 1u << 20);
+            for (int it = max(0, last_it_w - 1); it <= last_it_w; it++)
+                mbar_wait_bounded(&sm.wfull[it & 1], (it >> 1) & 1, 1u << 20);
+        }
+        return;
     }
-    // the row extremes for the 8-bit stage (min and max are idempotent, so a
-    // repeated launch over the same data leaves them unchanged)
-    if (a.st_mn) {
+    if (tid < kWsFront) {
+        // ---- front: WOLA + FFT of input li ----
+        int hc[2][kP];
+        const int li = tid >> 6, n0 = 2 * (tid & 63);
+        load_taps(a.filter, n0, hc);
+        for (int it = 0; it < nsteps; it++) {
+            const int s = it & 1, k = it >> 1;
+            bool ok = ws_wait(abort, &sm.ffull[s], k & 1, a.status);
+            if (ok && k > 0) ok = ws_wait(abort, &sm.rempty[s], (k - 1) & 1, a.status);
+            if (pair_any(li, !ok)) break;
+            wola_rows<kInt32, kFpga>(sm.stage[s][li][0], &sm.buf[s][li * kT], n0, hc);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&sm.fempty[s]);
+            input_barrier(li);
+            fft_rows<kDemote, kFpga>(sm.buf[s], sm.tw, tid);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&sm.rfull[s]);
+        }
+        __syncthreads();
+        return;
+    }
+    // ---- back: fine channel kp, all kT spectra ----
+    const int kp = tid - kWsFront;
+    float acc[kT][9];
 #pragma unroll
-        for (int st = 0; st < 4; st++) {
-            if (st >= a.nstokes) break;
-            const long long r = (long long)(cc * a.nstokes + st) * kK + kp;
-            if (kmn[st] != ~0u) atomicMin(&a.st_mn[r], kmn[st]);
-            if (kmx[st] != 0u) atomicMax(&a.st_mx[r], kmx[st]);
+    for (int m = 0; m < kT; m++)
+#pragma unroll
+        for (int q = 0; q < 9; q++) acc[m][q] = 0.f;
+    for (int it = 0; it < nsteps; it++) {
+        const int s = it & 1, k = it >> 1;
+        bool ok = ws_wait(abort, &sm.rfull[s], k & 1, a.status);
+        if (ok) ok = ws_wait(abort, &sm.wfull[s], k & 1, a.status);
+        if (!__all_sync(0xffffffffu, ok)) break; // the warp leaves together (it meets at __syncwarp below)
+#pragma unroll
+        for (int aa = 0; aa < kG / 2; aa++) {
+            const int ant = it * (kG / 2) + aa;
+            if (ant >= a.nant) break;
+            const float4 wa = sm.wst[s][0][aa][kp];
+            const float4 wb = sm.wst[s][1][aa][kp];
+#pragma unroll
+            for (int m = 0; m < kT; m++)
+                beam_accumulate(acc[m], wa, wb, sm.buf[s][(2 * aa) * kT + m][kp], sm.buf[s][(2 * aa + 1) * kT + m][kp]);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            mbar_arrive(&sm.rempty[s]);
+            mbar_arrive(&sm.wempty[s]);
         }
     }
+    __syncthreads();
+    if (*abort) return;
+    uint32_t kmn[4] = {~0u, ~0u, ~0u, ~0u}, kmx[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int m = 0; m < kT; m++) beam_store(a, cc, m0 + m, kp, acc[m], kmn, kmx);
+    beam_store_extremes(a, cc, kp, kmn, kmx);
 }
 
 // ---------------------------------------------------------------------------
@@ -639,10 +862,17 @@ template <bool A, bool B, bool C> struct BeamSel {
     static int run_g(const BeamArgs &a, dim3 grid, cudaStream_t st, int g)
     {
         CUtensorMap wmap;
-        int rc = make_tmap_beam_weights(&wmap, a.W, a.nant, (int)grid.y, a.W_cc, g / 2);
+        int rc = make_tmap_beam_weights(&wmap, a.W, a.nant, (int)grid.y, a.W_cc, g == 3 ? kG / 2 : g / 2);
         if (rc) return rc;
         g_pfb_last = g;
-        if (g == 8) {
+        if (g == 3) {
+            auto kern = beam_ws_kernel<A, B, C>;
+            if ((rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      (int)sizeof(WsSmem)),
+                                 "cudaFuncSetAttribute(ws smem)")))
+                return rc;
+            kern<<<grid, kWsThreads, sizeof(WsSmem), st>>>(a, wmap);
+        } else if (g == 8) {
             if ((rc = prep<8>(beam_kernel<A, B, C, 8>))) return rc;
             beam_kernel<A, B, C, 8><<<grid, 512, front_smem<8>(), st>>>(a, wmap);
         } else {
@@ -675,7 +905,7 @@ template <bool A, bool B, bool C> struct BeamSel {
         if (!rc) rc = check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
         float best = 0.f;
         int pick = 4;
-        for (int g : {4, 8}) {
+        for (int g : {4, 8}) { // variant 3 measured slower on every shape tried; forced only
             if (rc) break;
             rc = run_g(a, grid, st, g);
             if (!rc) rc = check_cuda(cudaEventRecord(e0, st), "cudaEventRecord");
@@ -717,7 +947,7 @@ int pfb_variant_last() { return g_pfb_last; }
 
 int pfb_variant(int g)
 {
-    if (g != 0 && g != 4 && g != 8) return -1;
+    if (g != 0 && g != 3 && g != 4 && g != 8) return -1;
     return g_pfb_variant.exchange(g);
 }
 
