@@ -74,13 +74,14 @@ def test_exports_the_loop_helpers_weak(lib):
     assert all(lib[f] == "W" for f in WEAK_HELPERS)
 
 
-def test_program_loop_compiles_and_links(lib, tmp_path):
+@pytest.mark.parametrize("prog", ["app_loop", "legacy_loop"])
+def test_program_loop_compiles_and_links(lib, tmp_path, prog):
     if not shutil.which("gcc"):
         pytest.skip("no gcc")
-    exe = tmp_path / "app_loop"
+    exe = tmp_path / prog
     subprocess.run(["gcc", "-O2", "-D__NVCC__", "-Wall", "-Werror", "-Wno-unused-function",
                     "-I", REF_INC, "-I", STUBS, "-I", os.path.join(CUDA, "include"),
-                    os.path.join(ROOT, "tests", "compat", "app_loop.c"), "-o", str(exe), "-L", LIBDIR,
+                    os.path.join(ROOT, "tests", "compat", f"{prog}.c"), "-o", str(exe), "-L", LIBDIR,
                     "-lvcsbeam_compat", "-lvcsbeam_gb300", "-L", os.path.join(CUDA, "lib64"), "-lcudart",
                     f"-Wl,-rpath,{LIBDIR}"], check=True)
     assert exe.exists()

@@ -13,7 +13,13 @@ linked to this library's vm* / cu_* entry points. It runs as a child process
     of the inverse PFB's output;
   * one whole C1 second (128 tiles, FINEPFB / LSQ12 x 15/7.2): against the
     reference's own kernels (tests/golden/ref_golden_c1.npz) with the bounds
-    of the C1 parity test.
+    of the C1 parity test;
+  * tests/compat/legacy_loop.c: legacy recombined 4+4-bit input, three
+    pointings, two seconds in two chunks each (vmPushChunk, vmApplyJChunk,
+    vmBeamformChunk): every pointing's Stokes, beam voltages and PSRFITS
+    bytes, offsets and scales equal this library's vgb_beamform_legacy and
+    vgb_renormalise on the same inputs bit for bit, and its Stokes match the
+    oracle's beamformer within 1e-5 (norm-wise).
 """
 import os
 import subprocess
@@ -23,7 +29,7 @@ import numpy as np
 import pytest
 
 import synthetic as SY
-from helpers import byte_diff_stats, dev, rel_err, tables, torch_cuda, weights_on_device
+from helpers import byte_diff_stats, dev, host, rel_err, tables, torch_cuda, weights_on_device
 
 pytestmark = pytest.mark.gpu
 
@@ -35,20 +41,29 @@ K, P = 128, 12
 sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
 
 
-@pytest.fixture(scope="module")
-def app(tmp_path_factory):
+def build_program(tmp_path_factory, name):
     torch_cuda()
     if not os.path.exists(os.path.join(REF_INC, "vcsbeam.h")):
         pytest.skip("no configured vcsbeam.h")
     if not os.path.exists(os.path.join(LIBDIR, "libvcsbeam_compat.so")):
         pytest.fail("libvcsbeam_compat.so was not built although vcsbeam.h is configured")
-    exe = str(tmp_path_factory.mktemp("app") / "app_loop")
+    exe = str(tmp_path_factory.mktemp(name) / name)
     cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
     subprocess.run(["gcc", "-O2", "-D__NVCC__", "-w", "-I", REF_INC, "-I", STUBS, "-I", os.path.join(cuda, "include"),
-                    os.path.join(ROOT, "tests", "compat", "app_loop.c"), "-o", exe, "-L", LIBDIR, "-lvcsbeam_compat",
+                    os.path.join(ROOT, "tests", "compat", f"{name}.c"), "-o", exe, "-L", LIBDIR, "-lvcsbeam_compat",
                     "-lvcsbeam_gb300", "-L", os.path.join(cuda, "lib64"), "-lcudart", f"-Wl,-rpath,{LIBDIR}"],
                    check=True)
     return exe
+
+
+@pytest.fixture(scope="module")
+def legacy_app(tmp_path_factory):
+    return build_program(tmp_path_factory, "legacy_loop")
+
+
+@pytest.fixture(scope="module")
+def app(tmp_path_factory):
+    return build_program(tmp_path_factory, "app_loop")
 
 
 def run_app(exe, tmp, nant, nsec, nchunks, volt, ana, syn, i_idx, J, phi):
@@ -136,3 +151,57 @@ def test_compat_loop_c1_against_reference_kernels(app, tmp_path):
     keep = np.arange(0, 10000, G.SUB_B) >= P
     mx, _, frac = byte_diff_stats(vq[keep], g["vdif_sub"][keep])
     assert mx <= 1 and frac <= 1e-4
+
+
+def test_compat_legacy_pointings_equal_library_calls(legacy_app, tmp_path, oracle_mod):
+    torch = torch_cuda()
+    import vgb
+
+    nant, npnt, nsec, ns = 16, 3, 2, 10000
+    ni = 2 * nant
+    volt = oracle_mod.gen_int4_bytes(777, nsec * ns * K * ni).reshape(nsec, ns, K, ni)
+    i_idx = SY.legacy_input_order(nant)
+    polQ = np.ascontiguousarray(i_idx[0::2].astype(np.uint32))
+    polP = np.ascontiguousarray(i_idx[1::2].astype(np.uint32))
+    tabs = [tables(nant, seed=3 + t, npointing=npnt) for t in range(nsec)]
+    ind, outd = tmp_path / "in", tmp_path / "out"
+    ind.mkdir()
+    outd.mkdir()
+    volt.tofile(ind / "volt.bin")
+    np.asarray(i_idx, np.int32).tofile(ind / "i_idx.bin")
+    np.stack([tb[0] for tb in tabs]).astype(np.complex128).tofile(ind / "J.bin")
+    np.stack([tb[1] for tb in tabs]).astype(np.complex128).tofile(ind / "phi.bin")
+    r = subprocess.run([legacy_app, str(nant), str(npnt), str(nsec), "2", str(ind), str(outd)], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    invw = 1.0 / ni
+    for t in range(nsec):
+        S_c = np.fromfile(outd / f"S_{t}.bin", np.float32).reshape(npnt, ns, 4, K)
+        e_c = np.fromfile(outd / f"e_{t}.bin", np.complex128).reshape(npnt, ns, K, 2)
+        J, phi = tabs[t]
+        W = weights_on_device(J, phi)
+        dv = dev(volt[t].reshape(-1))
+        S = torch.empty(npnt * ns * 4 * K, dtype=torch.float32, device="cuda")
+        e = torch.empty(npnt * ns * K * 4, dtype=torch.float32, device="cuda")
+        vgb.beamform_legacy(dv, vgb.INT4, ns, K, nant, dev(polQ), dev(polP), W, npnt, invw, 4, S, e)
+        out = torch.empty(npnt * ns * 4 * K, dtype=torch.uint8, device="cuda")
+        off = torch.empty(npnt * 4 * K, dtype=torch.float32, device="cuda")
+        sc = torch.empty_like(off)
+        vgb.renormalise(S, 1, npnt, ns, 4, K, out, 0, ns * 4 * K, 4 * K, K, off, sc)
+        torch.cuda.synchronize()
+        S_l = host(S).reshape(npnt, ns, 4, K)
+        e_l = host(e).view(np.complex64).reshape(npnt, ns, K, 2)
+        assert np.array_equal(S_c, S_l), t
+        assert np.array_equal(e_c, e_l.astype(np.complex128)), t
+        out_l = host(out).reshape(npnt, ns, 4, K)
+        off_l = host(off).reshape(npnt, 4, K)
+        sc_l = host(sc).reshape(npnt, 4, K)
+        for p in range(npnt):
+            ps = np.fromfile(outd / f"psrfits_{p}_{t}.bin", np.uint8).reshape(ns, 4, K)
+            assert np.array_equal(ps, out_l[p]), (t, p)
+            assert np.array_equal(np.fromfile(outd / f"offsets_{p}_{t}.bin", np.float32).reshape(4, K), off_l[p])
+            assert np.array_equal(np.fromfile(outd / f"scales_{p}_{t}.bin", np.float32).reshape(4, K), sc_l[p])
+        if t == 0:
+            Sref, _ = oracle_mod.beamform(volt[t], J, phi, polQ, polP, invw)
+            for p in range(npnt):
+                assert rel_err(S_c[p], Sref[p]) < 1e-5, p
