@@ -446,26 +446,35 @@ def gb300_arm(args, rank, local_rank, world):
                   "stage_ms": {"pfb_beam": sstage[0], "renormalise": sstage[1], "ipfb_vdif": sstage[2],
                                "history": sstage[3]}}
 
-    # a filter as large as the reference's FINEPFB (peak tap 117,964): its
-    # partial sums can pass 2^24, so the weighted overlap-add runs in int32
+    # a filter as large as the reference's FINEPFB (peak tap 117,964): one
+    # FP32 sum could pass 2^24, so the weighted overlap-add takes the exact
+    # even/odd split sums the library picks for it; the int32 sums beside it
     hbig = (h.astype(np.int64) * 117964 // int(np.abs(h).max())).astype(np.int32)
-    assert not vgb.filter_fp32_exact(hbig)
-    big = vgb.Pipeline(ncc, NANT, NBLK, nstokes=4, pfb_flags=0, do_ipfb=True, invw=1.0 / NI)
-    big.set_filters(hbig, syn)
-    big.set_weights(W, on_device=True)
-    big.enable_timing(True)
-    bstage = np.zeros(4)
-    for i in range(nstage + 1):
-        big.run_device(volt[i % args.resident])
-        if i:
-            bstage += np.array(big.stage_ms())
-    big.close()
-    bstage /= nstage
-    int32_wola = {"filter": "the int16 prototype scaled to a peak tap of 117,964 (the reference's FINEPFB range): "
-                            "exact int32 weighted overlap-add",
-                  "rtf_device_eager": (ncc / NCC) / (bstage.sum() / 1e3),
-                  "stage_ms": {"pfb_beam": bstage[0], "renormalise": bstage[1], "ipfb_vdif": bstage[2],
-                               "history": bstage[3]}}
+    assert vgb.filter_wola_flags(hbig) == vgb.WOLA_FP32_SPLIT
+
+    def eager_stages(pfb_flags):
+        pl = vgb.Pipeline(ncc, NANT, NBLK, nstokes=4, pfb_flags=pfb_flags, do_ipfb=True, invw=1.0 / NI)
+        pl.set_filters(hbig, syn)
+        pl.set_weights(W, on_device=True)
+        pl.enable_timing(True)
+        st = np.zeros(4)
+        for i in range(nstage + 1):
+            pl.run_device(volt[i % args.resident])
+            if i:
+                st += np.array(pl.stage_ms())
+        pl.close()
+        return st / nstage
+
+    bstage = eager_stages(0)
+    istage = eager_stages(vgb.WOLA_INT32)
+    finepfb_sized = {"filter": "the int16 prototype scaled to a peak tap of 117,964 (the reference's FINEPFB "
+                               "range): one FP32 sum is not exact, the even/odd split sums are",
+                     "wola": "FP32, even and odd taps summed apart and added once (exact)",
+                     "rtf_device_eager": (ncc / NCC) / (bstage.sum() / 1e3),
+                     "stage_ms": {"pfb_beam": bstage[0], "renormalise": bstage[1], "ipfb_vdif": bstage[2],
+                                  "history": bstage[3]},
+                     "int32_wola": {"rtf_device_eager": (ncc / NCC) / (istage.sum() / 1e3),
+                                    "pfb_beam_ms": istage[0]}}
 
     # ---- the PFB alone (fine_pfb_offline: vmExecuteForwardPFB's packed
     # legacy-order output), 8 coarse channels from the reference's read
@@ -623,7 +632,7 @@ def gb300_arm(args, rank, local_rank, world):
                                    "and second parity), the per-second tracking tables inside it; stage_ms from "
                                    "a separate eager pass with events"},
             "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
-            "smart_mode": smart_mode, "int32_wola": int32_wola}
+            "smart_mode": smart_mode, "finepfb_sized": finepfb_sized}
     if pfb_only is not None:
         line["pfb_only"] = pfb_only
     if mb_section is not None:

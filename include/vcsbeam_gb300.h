@@ -49,10 +49,21 @@ extern "C" {
 #define VGB_PFB_IMAG_PART_FIRST 0x100
 #define VGB_PFB_EMULATE_FPGA 0x200
 
-/* Not a reference bit: accumulate the weighted overlap-add in FP32 instead of
- * int32. Exact (identical results) only when every partial sum of the filter
- * times int8 voltages stays below 2^24; vgb_filter_fp32_exact() checks that. */
+/* Not reference bits: the arithmetic of the weighted overlap-add. Neither
+ * bit: int32 sums (any filter). VGB_WOLA_FP32: one FP32 sum, exact (identical
+ * results) only when every partial sum of the filter times int8 voltages
+ * stays within 2^24; vgb_filter_fp32_exact() checks that. VGB_WOLA_FP32_SPLIT:
+ * the even and the odd taps summed apart in FP32 and added once, exact when
+ * each half's partial sums stay within 2^24 (the reference's FINEPFB filter,
+ * peak tap 117,964, is such a filter); ignored with VGB_PFB_EMULATE_FPGA,
+ * whose rounding takes the int32 sums. vgb_filter_wola_flags() picks the
+ * fastest exact one for a filter. */
 #define VGB_WOLA_FP32 0x10000
+#define VGB_WOLA_FP32_SPLIT 0x20000
+/* Force the int32 sums (takes precedence over the two bits above). In a
+ * pipeline's configured pfb_flags any of the three WOLA bits overrides the
+ * choice it derives from the filter. */
+#define VGB_WOLA_INT32 0x40000
 
 /* ---- vcsbeam_datatype (include/vcsbeam.h.in:346-350) ---- */
 #define VGB_INT4 0
@@ -69,6 +80,11 @@ int vgb_version(void);
 /* 1 if FP32 accumulation of the weighted overlap-add is exact for this
  * host-side filter (K*P taps) and int8 voltages, else 0. */
 int vgb_filter_fp32_exact(const int32_t *filter, int ntaps, int nchan);
+/* VGB_WOLA_FP32 when one FP32 sum is exact for this host-side filter (K*P
+ * taps) and int8 voltages, else VGB_WOLA_FP32_SPLIT when the even/odd split
+ * sums are, else 0 (int32). The pipeline and the VCSBeam API layer apply it
+ * to the filter they are given. */
+unsigned vgb_filter_wola_flags(const int32_t *filter, int ntaps, int nchan);
 /* Copies and clears the device status word of the current device (after
  * synchronising `stream`). Returns VGB_ERR_DEVICE if any bit was set. */
 int vgb_check_device_status(void *stream, unsigned *flags_out);
@@ -108,7 +124,8 @@ typedef struct vgb_voltages {
  *   filter      K*P int32 analysis taps (pfb.cpp:459-460 cast)
  *   pfb_flags   VGB_PFB_EMULATE_FPGA and/or VGB_PFB_COMPLEX_INT4 select the
  *               rounding (pfb.cpp:602-616) and the 4-bit demotion the
- *               reference's beamformer input carries (pfb.cpp:325-332)
+ *               reference's beamformer input carries (pfb.cpp:325-332);
+ *               a VGB_WOLA_* bit the overlap-add arithmetic (none: int32)
  *   W           [ncc][nant][128][2][2] complex float: phi * J^-1
  *               (vgb_weights)
  *   invw        1 / number of unflagged RF inputs (metadata.c:1554-1561)
@@ -550,7 +567,9 @@ typedef struct vgb_pipeline_config {
     int nant;                /* tiles; ninputs = 2*nant */
     int nblocks;             /* MWAX voltage blocks per second (20) */
     int nstokes;             /* 1 or 4 */
-    unsigned pfb_flags;      /* rounding / demotion of the beamformer input */
+    unsigned pfb_flags;      /* rounding / demotion of the beamformer input;
+                                no VGB_WOLA_* bit: the exact arithmetic
+                                vgb_filter_wola_flags() picks for the filter */
     int do_ipfb;             /* inverse PFB + VDIF */
     float invw;              /* 1 / unflagged RF inputs */
 } vgb_pipeline_config;

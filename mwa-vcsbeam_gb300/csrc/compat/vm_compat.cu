@@ -79,7 +79,7 @@ struct CtxState {
     size_t W_n = 0;
     float4 *d_ef = nullptr;          // complex float beam voltages of one chunk, [s][c][pol]
     size_t ef_bytes = 0;
-    bool fp32_wola = false;
+    unsigned wola_flags = 0; // VGB_WOLA_FP32 / VGB_WOLA_FP32_SPLIT for the loaded filter
     unsigned stages = 0;             // forward-PFB / ApplyJ stages recorded since the last pass
 };
 struct IpfbState {
@@ -242,7 +242,7 @@ void vmInitForwardPFB(vcsbeam_context *vm, int M, pfb_flags flags)
     f->ninputs_per_cufft_batch = 32;
     f->cufft_batch_size = f->nspectra_per_chunk * f->ninputs_per_cufft_batch;
     std::memset(&f->plan, 0, sizeof(f->plan));
-    state(vm).fp32_wola = vgb_filter_fp32_exact(f->filter_coeffs, kP, kK) != 0;
+    state(vm).wola_flags = vgb_filter_wola_flags(f->filter_coeffs, kP, kK);
 
     vm->fine_sample_rate = f->nspectra;
     vm->nfine_chan = f->K;
@@ -291,7 +291,7 @@ void vmPackChunk(vcsbeam_context *vm)
     const vgb_voltages v = chunk_view(f->d_htr_data, f->I, (int)(f->nspectra_per_chunk / kFrames));
     const unsigned fl = ((unsigned)f->flags & (VGB_PFB_COMPLEX_INT4 | VGB_PFB_COMPLEX_FLOAT64 |
                                                VGB_PFB_IMAG_PART_FIRST | VGB_PFB_EMULATE_FPGA)) |
-                        (s.fp32_wola ? VGB_WOLA_FP32 : 0u);
+                        s.wola_flags;
     vk(vgb_fpfb(&v, 1, f->nspectra_per_chunk, f->d_filter_coeffs, kP, kK, f->d_i_output_idx, fl, f->d_vcs_data,
                 nullptr),
        fn);
@@ -543,7 +543,7 @@ void vmBeamformSecond(vcsbeam_context *vm)
     ensure_ef(s, (size_t)nsc * K * 2 * sizeof(float2), fn);
     const float invw = inverse_weight(vm, fn);
     const unsigned fl = ((unsigned)f->flags & (VGB_PFB_COMPLEX_INT4 | VGB_PFB_EMULATE_FPGA)) |
-                        (s.fp32_wola ? VGB_WOLA_FP32 : 0u);
+                        s.wola_flags;
     for (unsigned chunk = 0; chunk < vm->chunks_per_second; chunk++) {
         vmUploadForwardPFBChunk(vm);
         const vgb_voltages v = chunk_view(f->d_htr_data, f->I, nsc / kFrames);

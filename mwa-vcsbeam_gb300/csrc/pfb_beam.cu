@@ -10,7 +10,8 @@
 //      with mbarriers: step i+1 lands while step i computes;
 //   2. weighted overlap-add, exactly (pfb.cpp:121-179): one thread per
 //      (input, pair of adjacent samples), the pair's 12 taps in registers,
-//      packed FP32x2 FMAs (or int32 when FP32 would not be exact);
+//      packed FP32x2 FMAs (the even and odd taps summed apart, or int32,
+//      when one FP32 sum would not be exact);
 //   3. the FPGA rounding (pfb.cpp:202-242) or the 2^-14 scaling
 //      (pfb.cpp:256-268);
 //   4. a 128-point FFT (16 x 8, eight threads per transform, in place);
@@ -203,13 +204,26 @@ __device__ __forceinline__ float fpga_round(float X)
 // ---------------------------------------------------------------------------
 // Steps 2-3: weighted overlap-add for thread (li, n0..n0+1) into buf rows.
 // ---------------------------------------------------------------------------
+// Arithmetic of the sum of 12 products h x (int taps, int8 voltages), each
+// giving the exact integer sum rounded once to FP32 -- what the reference's
+// int32 sum converted to float gives (pfb.cpp:153-160, 256-268):
+//   kWolaFp32   one FP32 sum; exact when every partial sum of the filter
+//               times |x| <= 128 stays within 2^24 (vgb_filter_fp32_exact);
+//   kWolaSplit  the even and the odd taps summed apart in FP32, each exact
+//               within 2^24, and added once (one rounding of the exact sum);
+//               the reference's FINEPFB filter (peak tap 117,964) is such a
+//               filter. Without FPGA rounding only (that needs the integer);
+//   kWolaInt32  int32 sums, any filter.
+constexpr int kWolaFp32 = 0, kWolaSplit = 1, kWolaInt32 = 2;
+
 // stage_in: the input's kWin staged frames [w][kK]; rows: its kT output rows.
-template <bool kInt32, bool kFpga>
+template <int kW, bool kFpga>
 __device__ __forceinline__ void wola_rows(const char2 *stage_in, float2 (*rows)[kFftRow], int n0,
                                           const int (&hc)[2][kP])
 {
+    static_assert(kW != kWolaSplit || !kFpga, "the split sum is for the unrounded mode");
     const uint32_t *x = reinterpret_cast<const uint32_t *>(stage_in + n0);
-    if (kInt32) {
+    if (kW == kWolaInt32) {
         int ar[kT][2], ai[kT][2];
 #pragma unroll
         for (int m = 0; m < kT; m++) ar[m][0] = ar[m][1] = ai[m][0] = ai[m][1] = 0;
@@ -243,6 +257,47 @@ __device__ __forceinline__ void wola_rows(const char2 *stage_in, float2 (*rows)[
                                 (float)ai[m][1] * sc);
             }
             *reinterpret_cast<float4 *>(&rows[m][n0]) = b;
+        }
+    } else if (kW == kWolaSplit) {
+        // Two passes of kT / 2 spectra each keep the even and odd sums within
+        // the FP32 path's registers; each pass reads the kT / 2 + kP - 1
+        // frames its spectra need. The output scale rides on the taps, as in
+        // the single-sum path (a power of two: every product and partial sum
+        // is the exact one scaled).
+        constexpr int kH = kT / 2;
+        const float tsc = 1.0f / (16384.0f * kK);
+        float2 h2[kP];
+#pragma unroll
+        for (int p = 0; p < kP; p++) h2[p] = make_float2((float)hc[0][p] * tsc, (float)hc[1][p] * tsc);
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+            const int mb = half * kH;
+            float2 er[kH], ei[kH], od_r[kH], od_i[kH];
+#pragma unroll
+            for (int m = 0; m < kH; m++) er[m] = ei[m] = od_r[m] = od_i[m] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int w = mb; w < mb + kH + kP - 1; w++) {
+                float2 xr, xi;
+                c4_to_f(x[w * (kK / 2)], xr, xi);
+#pragma unroll
+                for (int p = 0; p < kP; p++) {
+                    const int m = w - p - mb;
+                    if (m >= 0 && m < kH) {
+                        if (p & 1) {
+                            od_r[m] = __ffma2_rn(h2[p], xr, od_r[m]);
+                            od_i[m] = __ffma2_rn(h2[p], xi, od_i[m]);
+                        } else {
+                            er[m] = __ffma2_rn(h2[p], xr, er[m]);
+                            ei[m] = __ffma2_rn(h2[p], xi, ei[m]);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < kH; m++) {
+                const float2 r = padd(er[m], od_r[m]), i = padd(ei[m], od_i[m]);
+                *reinterpret_cast<float4 *>(&rows[mb + m][n0]) = make_float4(r.x, i.x, r.y, i.y);
+            }
         }
     } else {
         // Without FPGA rounding the output scale 2^-14 / K (a power of two)
@@ -281,10 +336,10 @@ __device__ __forceinline__ void wola_rows(const char2 *stage_in, float2 (*rows)[
     }
 }
 
-template <bool kInt32, bool kFpga, int G>
+template <int kW, bool kFpga, int G>
 __device__ __forceinline__ void wola_step(FrontSmemT<G> &sm, int s, int li, int n0, const int (&hc)[2][kP])
 {
-    wola_rows<kInt32, kFpga>(sm.stage[s][li][0], &sm.buf[li * kT], n0, hc);
+    wola_rows<kW, kFpga>(sm.stage[s][li][0], &sm.buf[li * kT], n0, hc);
 }
 
 // vcsbeam.h.in:453-456: (int)round(x) clipped to [-8, 7].
@@ -470,7 +525,7 @@ __device__ __forceinline__ void beam_store_extremes(const BeamArgs &a, int cc, i
 // G = 8 (one CTA of 512 threads, half the steps and block barriers per
 // input). Every (k', m) is summed by one thread over the tiles in the same
 // order either way, so both give identical results; the host picks by timing.
-template <bool kInt32, bool kFpga, bool kDemote, int G>
+template <int kW, bool kFpga, bool kDemote, int G>
 __global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1)
     beam_kernel(const BeamArgs a, const __grid_constant__ CUtensorMap wmap)
 {
@@ -507,7 +562,7 @@ __global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1)
         }
         // everyone has finished step it-1, so its buffers may be refilled
         if (it + 1 < nsteps) produce_spread(sm, a.vv, cc, it + 1, m0, a.nspectra, &wmap, a.status);
-        wola_step<kInt32, kFpga>(sm, it & 1, li, n0, hc);
+        wola_step<kW, kFpga>(sm, it & 1, li, n0, hc);
         input_barrier(li);
         fft_step<kDemote, kFpga>(sm, tid);
         __syncthreads();
@@ -588,7 +643,7 @@ __device__ __forceinline__ bool pair_any(int li, bool pred)
     return r != 0;
 }
 
-template <bool kInt32, bool kFpga, bool kDemote>
+template <int kW, bool kFpga, bool kDemote>
 __global__ void __launch_bounds__(kWsThreads, 1)
     beam_ws_kernel(const BeamArgs a, const __grid_constant__ CUtensorMap wmap)
 {
@@ -669,7 +724,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             bool ok = ws_wait(abort, &sm.ffull[s], k & 1, a.status);
             if (ok && k > 0) ok = ws_wait(abort, &sm.rempty[s], (k - 1) & 1, a.status);
             if (pair_any(li, !ok)) break;
-            wola_rows<kInt32, kFpga>(sm.stage[s][li][0], &sm.buf[s][li * kT], n0, hc);
+            wola_rows<kW, kFpga>(sm.stage[s][li][0], &sm.buf[s][li * kT], n0, hc);
             __syncwarp();
             if (lane == 0) mbar_arrive(&sm.fempty[s]);
             input_barrier(li);
@@ -719,7 +774,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 // ---------------------------------------------------------------------------
 // PFB-only kernel: packed legacy-order output (pfb.cpp:297-343).
 // ---------------------------------------------------------------------------
-template <bool kInt32, bool kFpga, bool kDemote>
+template <int kW, bool kFpga, bool kDemote>
 __global__ void __launch_bounds__(kThreads, 2) pack_kernel(const PackArgs a)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -771,7 +826,7 @@ __global__ void __launch_bounds__(kThreads, 2) pack_kernel(const PackArgs a)
             return;
         }
         if (tid < 32 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, nullptr, a.status, inv);
-        wola_step<kInt32, kFpga>(sm, it & 1, li, n0, hc);
+        wola_step<kW, kFpga>(sm, it & 1, li, n0, hc);
         input_barrier(li);
         fft_step<kDemote, kFpga>(sm, tid);
         __syncthreads();
@@ -837,20 +892,30 @@ template <int G = kG, class K> static int prep(K kern)
                       "cudaFuncSetAttribute(front smem)");
 }
 
-// Pick the template instance for (int32 WOLA, FPGA rounding, 4-bit demotion).
-template <template <bool, bool, bool> class Sel, class Args>
-static int dispatch(const Args &a, dim3 grid, bool i32, bool fpga, bool demote, cudaStream_t st)
+// Pick the template instance for (WOLA arithmetic, FPGA rounding, 4-bit
+// demotion). The split sum is built for the unrounded mode only; a request
+// for it with FPGA rounding takes the int32 sums (identical results).
+template <template <int, bool, bool> class Sel, class Args>
+static int dispatch(const Args &a, dim3 grid, int wola, bool fpga, bool demote, cudaStream_t st)
 {
-    const int sel = (i32 ? 4 : 0) | (fpga ? 2 : 0) | (demote ? 1 : 0);
+    if (wola == kWolaSplit && fpga) wola = kWolaInt32;
+    if (wola == kWolaFp32) {
+        const int sel = (fpga ? 2 : 0) | (demote ? 1 : 0);
+        switch (sel) {
+        case 0: return Sel<kWolaFp32, false, false>::run(a, grid, st);
+        case 1: return Sel<kWolaFp32, false, true>::run(a, grid, st);
+        case 2: return Sel<kWolaFp32, true, false>::run(a, grid, st);
+        default: return Sel<kWolaFp32, true, true>::run(a, grid, st);
+        }
+    }
+    if (wola == kWolaSplit)
+        return demote ? Sel<kWolaSplit, false, true>::run(a, grid, st) : Sel<kWolaSplit, false, false>::run(a, grid, st);
+    const int sel = (fpga ? 2 : 0) | (demote ? 1 : 0);
     switch (sel) {
-    case 0: return Sel<false, false, false>::run(a, grid, st);
-    case 1: return Sel<false, false, true>::run(a, grid, st);
-    case 2: return Sel<false, true, false>::run(a, grid, st);
-    case 3: return Sel<false, true, true>::run(a, grid, st);
-    case 4: return Sel<true, false, false>::run(a, grid, st);
-    case 5: return Sel<true, false, true>::run(a, grid, st);
-    case 6: return Sel<true, true, false>::run(a, grid, st);
-    default: return Sel<true, true, true>::run(a, grid, st);
+    case 0: return Sel<kWolaInt32, false, false>::run(a, grid, st);
+    case 1: return Sel<kWolaInt32, false, true>::run(a, grid, st);
+    case 2: return Sel<kWolaInt32, true, false>::run(a, grid, st);
+    default: return Sel<kWolaInt32, true, true>::run(a, grid, st);
     }
 }
 
@@ -858,7 +923,7 @@ static int dispatch(const Args &a, dim3 grid, bool i32, bool fpga, bool demote, 
 static std::atomic<int> g_pfb_variant{0}; // 0: autotuned; else forced inputs per step (4 or 8)
 static std::atomic<int> g_pfb_last{0};    // inputs per step of the last fused launch
 
-template <bool A, bool B, bool C> struct BeamSel {
+template <int A, bool B, bool C> struct BeamSel {
     static int run_g(const BeamArgs &a, dim3 grid, cudaStream_t st, int g)
     {
         CUtensorMap wmap;
@@ -930,7 +995,7 @@ template <bool A, bool B, bool C> struct BeamSel {
     }
 };
 
-template <bool A, bool B, bool C> struct PackSel {
+template <int A, bool B, bool C> struct PackSel {
     static int run(const PackArgs &a, dim3 grid, cudaStream_t st)
     {
         const size_t smem = front_smem<kG>() + sizeof(int) * (size_t)kPackMaxInputs;
@@ -951,18 +1016,30 @@ int pfb_variant(int g)
     return g_pfb_variant.exchange(g);
 }
 
-int launch_beam(const BeamArgs &a, int ncc, bool int32_wola, bool fpga, bool demote, cudaStream_t st)
+// WOLA arithmetic requested by the pfb_flags bits: VGB_WOLA_INT32, else
+// VGB_WOLA_FP32, else VGB_WOLA_FP32_SPLIT, else int32.
+static int wola_mode(unsigned flags)
 {
-    if (a.nspectra <= 0 || ncc <= 0) return VGB_SUCCESS;
-    dim3 grid((a.nspectra + kT - 1) / kT, ncc);
-    return dispatch<BeamSel>(a, grid, int32_wola, fpga, demote, st);
+    if (flags & VGB_WOLA_INT32) return kWolaInt32;
+    if (flags & VGB_WOLA_FP32) return kWolaFp32;
+    if (flags & VGB_WOLA_FP32_SPLIT) return kWolaSplit;
+    return kWolaInt32;
 }
 
-int launch_pack(const PackArgs &a, int ncc, bool int32_wola, bool fpga, bool demote, cudaStream_t st)
+int launch_beam(const BeamArgs &a, int ncc, unsigned flags, cudaStream_t st)
 {
     if (a.nspectra <= 0 || ncc <= 0) return VGB_SUCCESS;
     dim3 grid((a.nspectra + kT - 1) / kT, ncc);
-    return dispatch<PackSel>(a, grid, int32_wola, fpga, demote, st);
+    return dispatch<BeamSel>(a, grid, wola_mode(flags), (flags & VGB_PFB_EMULATE_FPGA) != 0,
+                             (flags & VGB_PFB_COMPLEX_INT4) != 0, st);
+}
+
+int launch_pack(const PackArgs &a, int ncc, unsigned flags, cudaStream_t st)
+{
+    if (a.nspectra <= 0 || ncc <= 0) return VGB_SUCCESS;
+    dim3 grid((a.nspectra + kT - 1) / kT, ncc);
+    return dispatch<PackSel>(a, grid, wola_mode(flags), (flags & VGB_PFB_EMULATE_FPGA) != 0,
+                             (flags & VGB_PFB_COMPLEX_INT4) != 0, st);
 }
 
 // Gather the last P frames of a second into the compact history layout

@@ -96,19 +96,36 @@ const char *vgb_last_error(void) { return t_err; }
 
 int vgb_version(void) { return 1; }
 
-int vgb_filter_fp32_exact(const int32_t *filter, int ntaps, int nchan)
+// Largest sum of |h| over the taps p = first, first + step, ... of one
+// sample position n (the taps h[p * nchan + n] that one output sums).
+static long long worst_tap_sum(const int32_t *filter, int ntaps, int nchan, int first, int step)
 {
-    if (!filter || ntaps <= 0 || nchan <= 0) return 0;
     long long worst = 0;
     for (int n = 0; n < nchan; n++) {
         long long s = 0;
-        for (int p = 0; p < ntaps; p++) {
-            long long h = filter[p * nchan + n];
+        for (int p = first; p < ntaps; p += step) {
+            const long long h = filter[p * nchan + n];
             s += h < 0 ? -h : h;
         }
         if (s > worst) worst = s;
     }
-    return worst * 127 < (1LL << 24) ? 1 : 0;
+    return worst;
+}
+
+// |x| <= 128 for int8 voltages: a sum is exact in FP32 when the largest
+// possible partial sum stays within 2^24.
+int vgb_filter_fp32_exact(const int32_t *filter, int ntaps, int nchan)
+{
+    if (!filter || ntaps <= 0 || nchan <= 0) return 0;
+    return worst_tap_sum(filter, ntaps, nchan, 0, 1) * 128 <= (1LL << 24) ? 1 : 0;
+}
+
+unsigned vgb_filter_wola_flags(const int32_t *filter, int ntaps, int nchan)
+{
+    if (!filter || ntaps <= 0 || nchan <= 0) return 0u;
+    if (vgb_filter_fp32_exact(filter, ntaps, nchan)) return VGB_WOLA_FP32;
+    const long long even = worst_tap_sum(filter, ntaps, nchan, 0, 2), odd = worst_tap_sum(filter, ntaps, nchan, 1, 2);
+    return (even > odd ? even : odd) * 128 <= (1LL << 24) ? VGB_WOLA_FP32_SPLIT : 0u;
 }
 
 // A wait on an mbarrier that nothing arrives on, limited to `polls` polls:
@@ -200,8 +217,7 @@ int beamform_mwax_impl(const vgb_voltages *v, int ncc, int nspectra, const int32
         a.st_mx = rstat + n;
         a.st_nan0 = rstat + 2 * n;
     }
-    return launch_beam(a, ncc, !(pfb_flags & VGB_WOLA_FP32), (pfb_flags & VGB_PFB_EMULATE_FPGA) != 0,
-                       (pfb_flags & VGB_PFB_COMPLEX_INT4) != 0, S(stream));
+    return launch_beam(a, ncc, pfb_flags, S(stream));
 }
 
 } // namespace
@@ -246,8 +262,7 @@ int vgb_fpfb(const vgb_voltages *v, int ncc, int nspectra, const int32_t *filter
     a.out_cc = (long long)nspectra * kK * v->ninputs;
     a.status = status_word();
     if (!a.status) return set_error(VGB_ERR_CUDA, "device status word unavailable");
-    return launch_pack(a, ncc, !(pfb_flags & VGB_WOLA_FP32), (pfb_flags & VGB_PFB_EMULATE_FPGA) != 0,
-                       (pfb_flags & VGB_PFB_COMPLEX_INT4) != 0, S(stream));
+    return launch_pack(a, ncc, pfb_flags, S(stream));
 }
 
 int vgb_wola(const vgb_voltages *v, int nspectra, const int32_t *filter, int ntaps, int nchan, int32_t *b,
@@ -443,7 +458,7 @@ struct vgb_pipeline {
     vgb_pipeline_config cfg{};
     int ninputs = 0, nspectra = 0;
     long long second_bytes = 0;      // one coarse channel's second, bytes
-    bool fp32_wola = false;
+    unsigned wola_flags = 0;         // VGB_WOLA_FP32 / VGB_WOLA_FP32_SPLIT for the loaded filter
     cudaStream_t s_comp = nullptr, s_copy = nullptr;
     cudaEvent_t ev_copied[2] = {}, ev_consumed[2] = {};
     int32_t *d_filter = nullptr;
@@ -497,6 +512,14 @@ struct vgb_pipeline {
     bool front_timed = false; // the fused front end's inputs-per-step choice has been timed
 };
 
+// The configured pfb_flags with the WOLA arithmetic: the configuration's own
+// WOLA bits if it has any, else the exact choice derived from the filter.
+static unsigned pipeline_pfb_flags(const vgb_pipeline *p)
+{
+    constexpr unsigned kWolaBits = VGB_WOLA_FP32 | VGB_WOLA_FP32_SPLIT | VGB_WOLA_INT32;
+    return p->cfg.pfb_flags | ((p->cfg.pfb_flags & kWolaBits) ? 0u : p->wola_flags);
+}
+
 namespace {
 
 template <class T> int dalloc(T **p, size_t bytes)
@@ -543,7 +566,7 @@ int pipeline_second(vgb_pipeline *p, const char2 *volt, long long cc_stride_byte
     int rc;
     p->launches = 0;
     const vgb_voltages v = pipeline_voltages(p, volt, cc_stride_bytes);
-    const unsigned flags = c.pfb_flags | (p->fp32_wola ? VGB_WOLA_FP32 : 0u);
+    const unsigned flags = pipeline_pfb_flags(p);
     auto mark = [&](int i) {
         return p->timing ? check_cuda(cudaEventRecord(p->ev_stage[i], p->s_comp), "stage event") : VGB_SUCCESS;
     };
@@ -678,7 +701,7 @@ int pipeline_second_graph(vgb_pipeline *p, const char2 *volt, long long cc_strid
         const vgb_pipeline_config &c = p->cfg;
         const vgb_voltages v = pipeline_voltages(p, volt, cc_stride_bytes);
         rc = vgb_beamform_mwax(&v, c.ncc, p->nspectra, p->d_filter, kP, kK,
-                               c.pfb_flags | (p->fp32_wola ? VGB_WOLA_FP32 : 0u), p->d_W, c.nant, c.invw, c.nstokes,
+                               pipeline_pfb_flags(p), p->d_W, c.nant, c.invw, c.nstokes,
                                p->d_S, p->d_e, p->d_incoh, p->s_comp);
         if (rc) return rc;
         p->front_timed = true; // one shape per pipeline
@@ -797,7 +820,7 @@ int vgb_pipeline_set_filters(vgb_pipeline *p, const int32_t *analysis, const flo
 {
     if (!p || !analysis) return set_error(VGB_ERR_INVALID, "NULL argument");
     if (p->cfg.do_ipfb && !synthesis) return set_error(VGB_ERR_INVALID, "synthesis filter required for the IPFB");
-    p->fp32_wola = vgb_filter_fp32_exact(analysis, kP, kK) != 0;
+    p->wola_flags = vgb_filter_wola_flags(analysis, kP, kK);
     int rc = check_cuda(cudaMemcpyAsync(p->d_filter, analysis, sizeof(int32_t) * kK * kP, cudaMemcpyHostToDevice,
                                         p->s_comp),
                         "upload analysis filter");

@@ -88,7 +88,9 @@ struct IpfbArgs {
     int frame_offset;
 };
 
-int launch_beam(const BeamArgs &a, int ncc, bool int32_wola, bool fpga, bool demote, cudaStream_t st);
+// flags: the pfb_flags bits (FPGA rounding, 4-bit demotion) and the WOLA
+// arithmetic bits VGB_WOLA_FP32 / VGB_WOLA_FP32_SPLIT (neither: int32).
+int launch_beam(const BeamArgs &a, int ncc, unsigned flags, cudaStream_t st);
 // VDIF frames per second (the MWA fine sample rate, 1.28 MHz / 128): where a
 // header's frame number rolls over to the next second.
 constexpr int kVdifFramesPerSecond = 10000;
@@ -97,7 +99,7 @@ int launch_vdif_advance(uint32_t *hdr, int njobs, int nframes, cudaStream_t st);
 // choice; returns the previous setting, -1 for a bad value.
 int pfb_variant_last();
 int pfb_variant(int g);
-int launch_pack(const PackArgs &a, int ncc, bool int32_wola, bool fpga, bool demote, cudaStream_t st);
+int launch_pack(const PackArgs &a, int ncc, unsigned flags, cudaStream_t st);
 int launch_phase(const double *unit, const double *east, const double *north, const double *height,
                  const double *cable, const double *freqs, int npointing, int nant, int nchan, double href,
                  double2 *phi, cudaStream_t st);

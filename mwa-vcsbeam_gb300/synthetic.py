@@ -54,10 +54,17 @@ def synthesis_scale(analysis: np.ndarray) -> float:
 
 def wola_fp32_exact(h: np.ndarray, ntaps: int = NTAPS, nchan: int = NCHAN) -> bool:
     """True when every partial sum of the weighted overlap-add of int8
-    voltages (|x| <= 127) with filter h stays below 2^24, so FP32
+    voltages (|x| <= 128) with filter h stays within 2^24, so FP32
     accumulation reproduces the int32 result exactly."""
     hh = np.abs(np.asarray(h, dtype=np.int64)).reshape(ntaps, nchan)
-    return int(hh.sum(axis=0).max()) * 127 < (1 << 24)
+    return int(hh.sum(axis=0).max()) * 128 <= (1 << 24)
+
+
+def wola_split_exact(h: np.ndarray, ntaps: int = NTAPS, nchan: int = NCHAN) -> bool:
+    """True when the even-tap and the odd-tap sums are each exact in FP32
+    (the split weighted overlap-add)."""
+    hh = np.abs(np.asarray(h, dtype=np.int64)).reshape(ntaps, nchan)
+    return max(int(hh[0::2].sum(axis=0).max()), int(hh[1::2].sum(axis=0).max())) * 128 <= (1 << 24)
 
 
 def tile_layout(nant: int, seed: int = 7, radius_m: float = 1500.0):

@@ -28,6 +28,8 @@ PFB_EMULATE_FPGA = 0x200
 PFB_SMART = 0x21D
 PFB_FULL_PRECISION = 0x2D
 WOLA_FP32 = 0x10000
+WOLA_FP32_SPLIT = 0x20000
+WOLA_INT32 = 0x40000
 INT4 = 0
 DBL = 1
 
@@ -119,6 +121,7 @@ _SIGS = {
     "vgb_last_error": (ctypes.c_char_p, []),
     "vgb_version": (I, []),
     "vgb_filter_fp32_exact": (I, [V, I, I]),
+    "vgb_filter_wola_flags": (U, [V, I, I]),
     "vgb_check_device_status": (I, [V, ctypes.POINTER(U)]),
     "vgb_beamform_mwax": (I, [ctypes.POINTER(Voltages), I, I, V, I, I, U, V, I, Fl, I, V, V, V, V]),
     "vgb_fpfb": (I, [ctypes.POINTER(Voltages), I, I, V, I, I, V, U, V, V]),
@@ -478,6 +481,13 @@ def check_device_status(stream=None) -> int:
 def filter_fp32_exact(h: np.ndarray) -> bool:
     h = np.ascontiguousarray(h, dtype=np.int32)
     return bool(lib().vgb_filter_fp32_exact(h.ctypes.data, NTAPS, NCHAN))
+
+
+def filter_wola_flags(h: np.ndarray) -> int:
+    """WOLA_FP32, WOLA_FP32_SPLIT or 0 (int32): the fastest exact weighted
+    overlap-add arithmetic for analysis filter h."""
+    h = np.ascontiguousarray(h, dtype=np.int32)
+    return int(lib().vgb_filter_wola_flags(h.ctypes.data, NTAPS, NCHAN))
 
 
 # --------------------------------------------------------------------------

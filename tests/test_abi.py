@@ -79,3 +79,19 @@ def test_filter_exactness_rule(vgb_mod):
     h = SY.analysis_filter_int16()
     assert vgb_mod.filter_fp32_exact(h)
     assert not vgb_mod.filter_fp32_exact(h * 4)
+    # the arithmetic the library picks per filter: one FP32 sum for the
+    # prototype, the even/odd split for the reference's FINEPFB (its worst
+    # half-sum 129,763 x 128 < 2^24), int32 beyond that
+    finepfb = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_filters.npz"))["finepfb"]
+    assert vgb_mod.filter_wola_flags(h) == vgb_mod.WOLA_FP32
+    assert vgb_mod.filter_wola_flags(finepfb) == vgb_mod.WOLA_FP32_SPLIT
+    assert not SY.wola_fp32_exact(finepfb) and SY.wola_split_exact(finepfb)
+    assert vgb_mod.filter_wola_flags(finepfb * 2) == 0 and not SY.wola_split_exact(finepfb * 2)
+    # the bound counts |x| = 128 (int8 -128): a filter exactly at the limit
+    # passes, one tap more does not
+    edge = np.zeros(12 * 128, np.int32)
+    edge[0] = 1 << 17                                  # 2^17 x 128 = 2^24
+    assert vgb_mod.filter_fp32_exact(edge) and SY.wola_fp32_exact(edge)
+    edge[128] = 1                                      # same sample position, another tap
+    assert not vgb_mod.filter_fp32_exact(edge) and not SY.wola_fp32_exact(edge)
+    assert vgb_mod.filter_wola_flags(edge) == vgb_mod.WOLA_FP32_SPLIT

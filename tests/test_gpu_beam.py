@@ -5,6 +5,8 @@ Tolerances: Stokes and beam voltages within 1e-5 of the largest magnitude
 (FP32 accumulation against the reference's FP64); the incoherent sum of
 4-bit voltages bit-exact (integer sums); tables within 1e-12 (FP64).
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -111,6 +113,59 @@ def test_fused_beam_inputs_per_step_identical(vgb_mod, torch, oracle_mod, flags_
         assert np.array_equal(x4, x3)
     with pytest.raises(vgb_mod.VGBError):
         vgb_mod.pfb_variant(6)
+
+
+def finepfb():
+    """The reference's FINEPFB analysis filter (tests/golden/ref_filters.npz)."""
+    return np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_filters.npz"))["finepfb"]
+
+
+def test_split_wola_equals_int32(vgb_mod, torch, oracle_mod):
+    """With the reference's FINEPFB filter one FP32 sum is not exact but the
+    even/odd split is: on full-range voltages (uniform int8, so sums pass
+    2^24) the split path gives the int32 path's Stokes, beam voltages and
+    incoherent sums bit for bit in every front-end shape, and the PFB-only
+    kernel's complex-double output too. One forced FP32 sum differs (the
+    comparison can see a rounding). With FPGA rounding a split request takes
+    the int32 sums."""
+    h = finepfb()
+    assert vgb_mod.filter_wola_flags(h) == vgb_mod.WOLA_FP32_SPLIT
+    nant, ns = 18, 70
+    ninputs = 2 * nant
+    rng = np.random.default_rng(77)
+    htr = rng.integers(-128, 128, size=(2, ninputs, 64000, 2), dtype=np.int8)
+    J, phi = tables(nant)
+    W = weights_on_device(J, phi)
+    full = vgb_mod.PFB_FULL_PRECISION
+    ref = run_beam(vgb_mod, torch, htr, nant, 1, ns, h, full, W, 1 / 36)
+    for g in (4, 8, 3):
+        prev = vgb_mod.pfb_variant(g)
+        try:
+            got = run_beam(vgb_mod, torch, htr, nant, 1, ns, h, full | vgb_mod.WOLA_FP32_SPLIT, W, 1 / 36)
+        finally:
+            vgb_mod.pfb_variant(prev)
+        for x, y in zip(got, ref):
+            assert np.array_equal(x, y), g
+    one = run_beam(vgb_mod, torch, htr, nant, 1, ns, h, full | vgb_mod.WOLA_FP32, W, 1 / 36)
+    assert not np.array_equal(one[1], ref[1])
+    # PFB only, complex double: per-input fine channels
+    i_idx = SY.legacy_input_order(nant)
+    d = dev(htr.reshape(-1).view(np.uint8))
+    v = vgb_mod.reference_buffer_voltages(d, ninputs, 1)
+    outs = []
+    for extra in (0, vgb_mod.WOLA_FP32_SPLIT):
+        out = torch.empty(ns * K * ninputs * 16, dtype=torch.uint8, device="cuda")
+        vgb_mod.fpfb(v, 1, ns, dev(h), dev(i_idx), full | extra, out)
+        torch.cuda.synchronize()
+        outs.append(host(out))
+    assert np.array_equal(outs[0], outs[1])
+    # FPGA rounding: the split request is served by the int32 sums
+    smart = vgb_mod.PFB_SMART
+    a = run_beam(vgb_mod, torch, htr, nant, 1, ns, h, smart, W, 1 / 36)
+    b = run_beam(vgb_mod, torch, htr, nant, 1, ns, h, smart | vgb_mod.WOLA_FP32_SPLIT, W, 1 / 36)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    assert vgb_mod.check_device_status() == 0
 
 
 def test_fused_beam_stokes_i_only_and_batched(vgb_mod, torch, oracle_mod):
