@@ -540,17 +540,22 @@ def gb300_arm(args, rank, local_rank, world):
 
         # the host link's own rate on this machine: one second of voltages
         # pinned -> device with a single copy, beside the pipeline's numbers
-        dst = torch.empty(ncc * SECOND_BYTES, dtype=torch.int8, device="cuda")
-        dst.copy_(hin, non_blocking=True)
-        torch.cuda.synchronize()
-        l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        l0.record()
-        dst.copy_(hin, non_blocking=True)
-        l1.record()
-        l1.synchronize()
-        link_gbs = hin.numel() / (l0.elapsed_time(l1) / 1e3) / 1e9
-        del dst
-        torch.cuda.empty_cache()
+        # (taken before and after the timed steps: the link is shared with
+        # the machine's other GPUs)
+        def link_rate():
+            dst = torch.empty(ncc * SECOND_BYTES, dtype=torch.int8, device="cuda")
+            dst.copy_(hin, non_blocking=True)
+            torch.cuda.synchronize()
+            l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            l0.record()
+            dst.copy_(hin, non_blocking=True)
+            l1.record()
+            l1.synchronize()
+            del dst
+            torch.cuda.empty_cache()
+            return hin.numel() / (l0.elapsed_time(l1) / 1e3) / 1e9
+
+        link_gbs = link_rate()
         for _ in range(min(args.warmup, 3)):
             e2e_step()
         pipe.sync()
@@ -562,11 +567,12 @@ def gb300_arm(args, rank, local_rank, world):
         pipe.sync()
         barrier()
         e2e_s = max_over_ranks(time.perf_counter() - t0)
+        link_after = link_rate()
         e2e = {"value": e2e_steps * ncc_all / NCC / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": ncc * SECOND_BYTES,
                "d2h_bytes_per_step": psr_b + vdif_b + stat_b,
                "steps": e2e_steps, "ms_per_step": 1e3 * e2e_s / e2e_steps,
-               "h2d_link_gbs": link_gbs,
+               "h2d_link_gbs": link_gbs, "h2d_link_gbs_after": link_after,
                "link_bound": link_gbs * 1e9 / (ncc * SECOND_BYTES) * ncc_all / NCC,
                "path": "vgb_pipeline_run_host from pinned host memory, products (tied-array PSRFITS rows, "
                        "incoherent PSRFITS rows, VDIF frames, offsets, scales) back to pinned host buffers; "
