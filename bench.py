@@ -633,7 +633,7 @@ def gb300_arm(args, rank, local_rank, world):
             "run": {"step": "one data-second (24 coarse channels x 1 s)" +
                             (f"; rank r processes coarse channels shard(24, r, {world})" if world > 1 else ""),
                     "resident_seconds": args.resident,
-                    "pfb_inputs_per_step": vgb.pfb_variant_last(),
+                    "pfb_variant": vgb.pfb_variant_last(),
                     "cuda_graphs": "each second replayed from a captured CUDA graph (one per resident buffer "
                                    "and second parity), the per-second tracking tables inside it; stage_ms from "
                                    "a separate eager pass with events"},
@@ -1005,9 +1005,9 @@ def main():
     ap.add_argument("--mb-stream-iters", type=int, default=3, help="many-beam host-streaming calls timed (0: skip)")
     ap.add_argument("--no-pfb-only", dest="pfb_only", action="store_false",
                     help="skip the PFB-only (fine_pfb_offline) section")
-    ap.add_argument("--pfb-variant", type=int, default=0, choices=[0, 3, 4, 8],
-                    help="profiling: force the fused front end's variant (4 or 8 inputs per step, 3 the "
-                         "warp-specialised kernel; 0 = timed choice)")
+    ap.add_argument("--pfb-variant", type=int, default=0, choices=[0, 3, 4, 5, 8],
+                    help="profiling: force the fused front end's variant (4 or 8 inputs per step, 5 the 4-input "
+                         "shape at three CTAs per SM, 3 the warp-specialised kernel; 0 = timed choice)")
     ap.add_argument("--beam-sweep", action="store_true",
                     help="time 1..1024 beams per coarse channel-second on both beamformers and print their JSON")
     ap.add_argument("--traffic", type=float, default=None,

@@ -136,19 +136,21 @@ typedef struct vgb_voltages {
 int vgb_beamform_mwax(const vgb_voltages *v, int ncc, int nspectra, const int32_t *filter, int ntaps,
                       int nchan, unsigned pfb_flags, const void *W, int nant, float invw, int nstokes,
                       float *S, void *e, float *incoh, void *stream);
-/* The fused front end has three variants, all giving identical results:
+/* The fused front end has four variants, all giving identical results:
  * 4 inputs (two tiles) per step in 256-thread CTAs (two per SM); 8 inputs per
- * step in 512-thread CTAs (one per SM); and 3, warp-specialised: one 416-
- * thread CTA per SM whose front warps run the PFB of step i while its back
- * warps sum step i - 1, handing rows over through mbarriers instead of
- * block-wide barriers (measured slower: 26.0 against 21.5 ms per data-second
- * of the full band, so it runs only when forced). The first call for a shape
- * times variants 4 and 8 and keeps the faster (a call made while the stream
- * is being captured uses the known choice, else 4). Force one with 3, 4 or
- * 8, or 0 for the timed choice; returns the previous setting, -1 on a bad
- * value. */
+ * step in 512-thread CTAs (one per SM); 5, the 4-input shape at three CTAs
+ * per SM (each thread's beam sums kept in tensor memory between steps, taps
+ * read from shared memory, frames and weights single-buffered); and 3,
+ * warp-specialised: one 416-thread CTA per SM whose front warps run the PFB
+ * of step i while its back warps sum step i - 1, handing rows over through
+ * mbarriers instead of block-wide barriers (measured slower: 26.0 against
+ * 21.5 ms per data-second of the full band, so it runs only when forced).
+ * The first call for a shape times variants 4, 8 and 5 and keeps the fastest
+ * (a call made while the stream is being captured uses the known choice,
+ * else 4). Force one with 3, 4, 5 or 8, or 0 for the timed choice; returns
+ * the previous setting, -1 on a bad value. */
 int vgb_pfb_variant(int inputs_per_step);
-/* Variant of the last fused front-end launch (3, 4 or 8; 0 before the first). */
+/* Variant of the last fused front-end launch (3, 4, 5 or 8; 0 before the first). */
 int vgb_pfb_variant_last(void);
 
 /*

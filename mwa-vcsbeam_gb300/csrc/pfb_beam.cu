@@ -216,14 +216,39 @@ __device__ __forceinline__ float fpga_round(float X)
 //   kWolaInt32  int32 sums, any filter.
 constexpr int kWolaFp32 = 0, kWolaSplit = 1, kWolaInt32 = 2;
 
+// The taps of samples n0, n0 + 1 in the form the WOLA multiplies by: int32
+// pairs, or FP32 pairs carrying the output scale 2^-14 / K when there is no
+// FPGA rounding (a power of two: every product and partial sum is the exact
+// one scaled, so the result is identical and the final multiply goes).
+template <int kW> struct WolaTap {
+    using type = float2;
+};
+template <> struct WolaTap<kWolaInt32> {
+    using type = int2;
+};
+
+template <int kW, bool kFpga>
+__device__ __forceinline__ void make_taps(const int (&hc)[2][kP], typename WolaTap<kW>::type (&t)[kP])
+{
+#pragma unroll
+    for (int p = 0; p < kP; p++) {
+        if constexpr (kW == kWolaInt32) {
+            t[p] = make_int2(hc[0][p], hc[1][p]);
+        } else {
+            const float tsc = kFpga ? 1.0f : 1.0f / (16384.0f * kK);
+            t[p] = make_float2((float)hc[0][p] * tsc, (float)hc[1][p] * tsc);
+        }
+    }
+}
+
 // stage_in: the input's kWin staged frames [w][kK]; rows: its kT output rows.
 template <int kW, bool kFpga>
 __device__ __forceinline__ void wola_rows(const char2 *stage_in, float2 (*rows)[kFftRow], int n0,
-                                          const int (&hc)[2][kP])
+                                          const typename WolaTap<kW>::type (&t)[kP])
 {
     static_assert(kW != kWolaSplit || !kFpga, "the split sum is for the unrounded mode");
     const uint32_t *x = reinterpret_cast<const uint32_t *>(stage_in + n0);
-    if (kW == kWolaInt32) {
+    if constexpr (kW == kWolaInt32) {
         int ar[kT][2], ai[kT][2];
 #pragma unroll
         for (int m = 0; m < kT; m++) ar[m][0] = ar[m][1] = ai[m][0] = ai[m][1] = 0;
@@ -237,8 +262,9 @@ __device__ __forceinline__ void wola_rows(const char2 *stage_in, float2 (*rows)[
                 if (m >= 0 && m < kT) {
 #pragma unroll
                     for (int q = 0; q < 2; q++) {
-                        ar[m][q] += hc[q][p] * xr[q];
-                        ai[m][q] += hc[q][p] * xi[q];
+                        const int h = q ? t[p].y : t[p].x;
+                        ar[m][q] += h * xr[q];
+                        ai[m][q] += h * xi[q];
                     }
                 }
             }
@@ -258,17 +284,11 @@ __device__ __forceinline__ void wola_rows(const char2 *stage_in, float2 (*rows)[
             }
             *reinterpret_cast<float4 *>(&rows[m][n0]) = b;
         }
-    } else if (kW == kWolaSplit) {
+    } else if constexpr (kW == kWolaSplit) {
         // Two passes of kT / 2 spectra each keep the even and odd sums within
         // the FP32 path's registers; each pass reads the kT / 2 + kP - 1
-        // frames its spectra need. The output scale rides on the taps, as in
-        // the single-sum path (a power of two: every product and partial sum
-        // is the exact one scaled).
+        // frames its spectra need.
         constexpr int kH = kT / 2;
-        const float tsc = 1.0f / (16384.0f * kK);
-        float2 h2[kP];
-#pragma unroll
-        for (int p = 0; p < kP; p++) h2[p] = make_float2((float)hc[0][p] * tsc, (float)hc[1][p] * tsc);
 #pragma unroll
         for (int half = 0; half < 2; half++) {
             const int mb = half * kH;
@@ -284,11 +304,11 @@ __device__ __forceinline__ void wola_rows(const char2 *stage_in, float2 (*rows)[
                     const int m = w - p - mb;
                     if (m >= 0 && m < kH) {
                         if (p & 1) {
-                            od_r[m] = __ffma2_rn(h2[p], xr, od_r[m]);
-                            od_i[m] = __ffma2_rn(h2[p], xi, od_i[m]);
+                            od_r[m] = __ffma2_rn(t[p], xr, od_r[m]);
+                            od_i[m] = __ffma2_rn(t[p], xi, od_i[m]);
                         } else {
-                            er[m] = __ffma2_rn(h2[p], xr, er[m]);
-                            ei[m] = __ffma2_rn(h2[p], xi, ei[m]);
+                            er[m] = __ffma2_rn(t[p], xr, er[m]);
+                            ei[m] = __ffma2_rn(t[p], xi, ei[m]);
                         }
                     }
                 }
@@ -300,13 +320,6 @@ __device__ __forceinline__ void wola_rows(const char2 *stage_in, float2 (*rows)[
             }
         }
     } else {
-        // Without FPGA rounding the output scale 2^-14 / K (a power of two)
-        // rides on the taps: every product and partial sum is the exact one
-        // scaled, so the result is identical and the final multiply goes.
-        const float tsc = kFpga ? 1.0f : 1.0f / (16384.0f * kK);
-        float2 h2[kP];
-#pragma unroll
-        for (int p = 0; p < kP; p++) h2[p] = make_float2((float)hc[0][p] * tsc, (float)hc[1][p] * tsc);
         float2 ar[kT], ai[kT];
 #pragma unroll
         for (int m = 0; m < kT; m++) ar[m] = ai[m] = make_float2(0.f, 0.f);
@@ -318,8 +331,8 @@ __device__ __forceinline__ void wola_rows(const char2 *stage_in, float2 (*rows)[
             for (int p = 0; p < kP; p++) {
                 const int m = w - p;
                 if (m >= 0 && m < kT) {
-                    ar[m] = __ffma2_rn(h2[p], xr, ar[m]);
-                    ai[m] = __ffma2_rn(h2[p], xi, ai[m]);
+                    ar[m] = __ffma2_rn(t[p], xr, ar[m]);
+                    ai[m] = __ffma2_rn(t[p], xi, ai[m]);
                 }
             }
         }
@@ -337,9 +350,10 @@ __device__ __forceinline__ void wola_rows(const char2 *stage_in, float2 (*rows)[
 }
 
 template <int kW, bool kFpga, int G>
-__device__ __forceinline__ void wola_step(FrontSmemT<G> &sm, int s, int li, int n0, const int (&hc)[2][kP])
+__device__ __forceinline__ void wola_step(FrontSmemT<G> &sm, int s, int li, int n0,
+                                          const typename WolaTap<kW>::type (&t)[kP])
 {
-    wola_rows<kW, kFpga>(sm.stage[s][li][0], &sm.buf[li * kT], n0, hc);
+    wola_rows<kW, kFpga>(sm.stage[s][li][0], &sm.buf[li * kT], n0, t);
 }
 
 // vcsbeam.h.in:453-456: (int)round(x) clipped to [-8, 7].
@@ -541,9 +555,13 @@ __global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1)
 
     if (tid == 0) prefetch_tmap(&wmap);
     init_front(sm, tid);
-    int hc[2][kP];
+    typename WolaTap<kW>::type tp[kP];
     const int li = tid >> 6, n0 = 2 * (tid & 63);
-    load_taps(a.filter, n0, hc);
+    {
+        int hc[2][kP];
+        load_taps(a.filter, n0, hc);
+        make_taps<kW, kFpga>(hc, tp);
+    }
     __syncthreads();
     produce_spread(sm, a.vv, cc, 0, m0, a.nspectra, &wmap, a.status);
 
@@ -562,7 +580,7 @@ __global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1)
         }
         // everyone has finished step it-1, so its buffers may be refilled
         if (it + 1 < nsteps) produce_spread(sm, a.vv, cc, it + 1, m0, a.nspectra, &wmap, a.status);
-        wola_step<kW, kFpga>(sm, it & 1, li, n0, hc);
+        wola_step<kW, kFpga>(sm, it & 1, li, n0, tp);
         input_barrier(li);
         fft_step<kDemote, kFpga>(sm, tid);
         __syncthreads();
@@ -584,6 +602,202 @@ __global__ void __launch_bounds__(64 * G, G == 4 ? 2 : 1)
 #pragma unroll
     for (int mi = 0; mi < kMi; mi++) beam_store(a, cc, m0 + mh + kMh * mi, kp, acc[mi], kmn, kmx);
     beam_store_extremes(a, cc, kp, kmn, kmx);
+}
+
+// ---------------------------------------------------------------------------
+// Beamformer kernel with three CTAs per SM (variant 5).
+// ---------------------------------------------------------------------------
+// beam_kernel<..., 4> uses 126-128 registers and 95 KB of shared memory per
+// 256-thread CTA, so two CTAs (16 warps) share an SM, and its WOLA, FFT and
+// barrier latencies show as idle issue slots. This shape fits three (24
+// warps) with the same arithmetic in the same order (identical results):
+//   * each thread's 36 beam sums stay in tensor memory between steps
+//     (tcgen05.ld at the start of its beam phase, tcgen05.st at its end; one
+//     128-column allocation per CTA, warps w and w + 4 sharing a lane
+//     quarter at columns 0 and 64), so no register is held across steps;
+//   * the taps come from shared memory each step (12 loads per thread);
+//   * frames and weights are single-buffered: step it + 1's frames are copied
+//     as soon as every thread has finished step it's WOLA (the block barrier
+//     after the FFT) and land during its beam sums; step it's weights are
+//     copied after step it's first block barrier (every thread has finished
+//     step it - 1's sums) and land during its WOLA and FFT.
+// 72 KB of shared memory, at most 80 registers per thread.
+template <class Tap> struct TmSmem {
+    char2 stage[kG][kWin][kK];             // TMA destination: frames
+    float4 wst[2][kG / 2][kK];             // TMA destination: weights [row][tile][k']
+    float2 buf[kG * kT][kFftRow];          // WOLA output -> FFT (in place) -> voltages
+    float2 tw[128];                        // W128 twiddles
+    Tap taps[kP][kK / 2];                  // per (tap, sample pair n0 / 2)
+    uint64_t bar_f, bar_w;
+    uint32_t tmem;
+};
+static_assert(offsetof(TmSmem<float2>, wst) % 128 == 0 && offsetof(TmSmem<float2>, tw) % 16 == 0,
+              "TMA / vector alignment");
+constexpr uint32_t kTmCols = 128;          // TMEM columns per CTA (three CTAs: 384 of 512)
+
+// Frames of step `it` into the single stage: lane 0 of warp li (li < kG)
+// copies input it * kG + li, lane 0 of warp 0 posts the byte count first
+// (completing its own shortfall when frames fell outside the buffers, as
+// produce_spread does).
+template <class Tap>
+__device__ __forceinline__ void tm_frames(TmSmem<Tap> &sm, const VoltView &vv, int cc, int it, int m0, int nspectra,
+                                          unsigned *status)
+{
+    if ((threadIdx.x & 31) != 0) return;
+    const int warp = threadIdx.x >> 5;
+    if (warp >= kG) return;
+    const int w_end = min(m0 + kWin, nspectra + kP - 1);
+    const uint32_t per_input = (w_end - m0) * kFrameBytes;
+    if (warp == 0) {
+        uint32_t total = 0;
+        for (int li = 0; li < kG; li++)
+            if (it * kG + li < vv.ninputs) total += per_input;
+        mbar_arrive_expect_tx(&sm.bar_f, total);
+    }
+    const int pos = it * kG + warp;
+    if (pos < vv.ninputs) {
+        const uint32_t issued = issue_frames(vv, cc, pos, m0, w_end, sm.stage[warp][0], &sm.bar_f, status);
+        if (issued != per_input)
+            asm volatile("mbarrier.complete_tx.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&sm.bar_f)),
+                         "r"(per_input - issued)
+                         : "memory");
+    }
+}
+
+// The two Jones rows of step `it`'s tiles, by lane 0 of warp kG.
+template <class Tap> __device__ __forceinline__ void tm_weights(TmSmem<Tap> &sm, const CUtensorMap *wmap, int cc, int it)
+{
+    if (threadIdx.x != 32 * kG) return;
+    constexpr uint32_t kWBytes = (kG / 2) * kK * 16;
+    mbar_arrive_expect_tx(&sm.bar_w, 2 * kWBytes);
+    tma_load_5d(sm.wst[0][0], wmap, 0, 0, 0, (kG / 2) * it, cc, &sm.bar_w);
+    tma_load_5d(sm.wst[1][0], wmap, 0, 1, 0, (kG / 2) * it, cc, &sm.bar_w);
+}
+
+template <int kW, bool kFpga, bool kDemote>
+__global__ void __launch_bounds__(kThreads, 3)
+    beam_tm_kernel(const BeamArgs a, const __grid_constant__ CUtensorMap wmap)
+{
+    using Tap = typename WolaTap<kW>::type;
+    constexpr int kTiles = kG / 2;       // tiles per step
+    constexpr int kMh = kG / 2;          // threads per k' (spectra m = mh + kMh mi)
+    constexpr int kMi = kT / kMh;        // spectra per thread
+    static_assert(kMi * 9 == 36, "36 beam sums per thread");
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    TmSmem<Tap> &sm = *reinterpret_cast<TmSmem<Tap> *>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int cc = blockIdx.y;
+    const int m0 = blockIdx.x * kT;
+    const int nsteps = (a.vv.ninputs + kG - 1) / kG;
+    const int li = tid >> 6, n0 = 2 * (tid & 63);
+
+    if (tid == 0) prefetch_tmap(&wmap);
+    init_twiddles(sm.tw, tid);
+    if (tid < kK / 2) {
+        int hc[2][kP];
+        load_taps(a.filter, n0, hc);
+        Tap t[kP];
+        make_taps<kW, kFpga>(hc, t);
+#pragma unroll
+        for (int p = 0; p < kP; p++) sm.taps[p][tid] = t[p];
+    }
+    if (tid == 0) {
+        mbar_init(&sm.bar_f, 1);
+        mbar_init(&sm.bar_w, 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(&sm.tmem, kTmCols);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    // this thread's 36 sums: lane 32 (warp % 4) + lane, columns 64 (warp / 4) ..
+    const uint32_t tacc = sm.tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(64 * (warp >> 2));
+    if (nsteps > 0) {
+        tm_frames(sm, a.vv, cc, 0, m0, a.nspectra, a.status);
+        tm_weights(sm, &wmap, cc, 0);
+    }
+
+    const int kp = tid & (kK - 1), mh = tid >> 7;
+    bool wbad = false;                   // a weights wait gave up (leave at the next step's barrier)
+    int it = 0;
+    for (; it < nsteps; it++) {
+        // step it's frames have landed and every thread has finished step it - 1
+        const bool got = mbar_wait_bounded(&sm.bar_f, it & 1, 1u << 22);
+        if (__syncthreads_or(!got || wbad)) break;
+        if (it > 0) tm_weights(sm, &wmap, cc, it);
+        {
+            Tap t[kP];
+#pragma unroll
+            for (int p = 0; p < kP; p++) t[p] = sm.taps[p][tid & (kK / 2 - 1)];
+            wola_rows<kW, kFpga>(sm.stage[li][0], &sm.buf[li * kT], n0, t);
+        }
+        input_barrier(li);
+        fft_rows<kDemote, kFpga>(sm.buf, sm.tw, tid);
+        __syncthreads();
+        // every WOLA read of the stage is done: the next step's frames may land
+        if (it + 1 < nsteps) tm_frames(sm, a.vv, cc, it + 1, m0, a.nspectra, a.status);
+        if (!mbar_wait_bounded(&sm.bar_w, it & 1, 1u << 22)) {
+            wbad = true;
+            atomicOr(a.status, kErrWaitTimeout);
+        }
+        __syncwarp(); // the tensor-memory accesses are warp-collective
+        float acc[kMi * 9];
+        if (it == 0) {
+#pragma unroll
+            for (int q = 0; q < kMi * 9; q++) acc[q] = 0.f;
+        } else {
+            tmem_wait_st();
+            tmem_ld36(tacc, acc);
+        }
+#pragma unroll
+        for (int aa = 0; aa < kTiles; aa++) {
+            const int ant = it * kTiles + aa;
+            if (ant >= a.nant) break;
+            const float4 wa = sm.wst[0][aa][kp];
+            const float4 wb = sm.wst[1][aa][kp];
+#pragma unroll
+            for (int mi = 0; mi < kMi; mi++) {
+                const int m = mh + kMh * mi;
+                beam_accumulate(acc + 9 * mi, wa, wb, sm.buf[(2 * aa) * kT + m][kp], sm.buf[(2 * aa + 1) * kT + m][kp]);
+            }
+        }
+        tmem_st36(tacc, acc);
+    }
+
+    if (it < nsteps) {
+        // left early: the copies in flight (step it's frames, step it - 1's
+        // weights) get a bounded chance to land before the CTA exits
+        if (tid == 0) {
+            atomicOr(a.status, kErrWaitTimeout);
+            mbar_wait_bounded(&sm.bar_f, it & 1, 1u << 20);
+            if (it > 0) mbar_wait_bounded(&sm.bar_w, (it - 1) & 1, 1u << 20);
+        }
+    } else {
+        // a weights copy whose wait gave up in the last step may still land
+        if (tid == 0 && nsteps > 0) mbar_wait_bounded(&sm.bar_w, (nsteps - 1) & 1, 1u << 20);
+        __syncwarp();
+        float acc[kMi * 9];
+        if (nsteps == 0) {
+#pragma unroll
+            for (int q = 0; q < kMi * 9; q++) acc[q] = 0.f;
+        } else {
+            tmem_wait_st();
+            tmem_ld36(tacc, acc);
+        }
+        uint32_t kmn[4] = {~0u, ~0u, ~0u, ~0u}, kmx[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+        for (int mi = 0; mi < kMi; mi++) beam_store(a, cc, m0 + mh + kMh * mi, kp, acc + 9 * mi, kmn, kmx);
+        beam_store_extremes(a, cc, kp, kmn, kmx);
+    }
+    __syncwarp();
+    tmem_wait_st();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(sm.tmem, kTmCols);
 }
 
 // ---------------------------------------------------------------------------
@@ -716,15 +930,19 @@ __global__ void __launch_bounds__(kWsThreads, 1)
     }
     if (tid < kWsFront) {
         // ---- front: WOLA + FFT of input li ----
-        int hc[2][kP];
+        typename WolaTap<kW>::type tp[kP];
         const int li = tid >> 6, n0 = 2 * (tid & 63);
-        load_taps(a.filter, n0, hc);
+        {
+            int hc[2][kP];
+            load_taps(a.filter, n0, hc);
+            make_taps<kW, kFpga>(hc, tp);
+        }
         for (int it = 0; it < nsteps; it++) {
             const int s = it & 1, k = it >> 1;
             bool ok = ws_wait(abort, &sm.ffull[s], k & 1, a.status);
             if (ok && k > 0) ok = ws_wait(abort, &sm.rempty[s], (k - 1) & 1, a.status);
             if (pair_any(li, !ok)) break;
-            wola_rows<kW, kFpga>(sm.stage[s][li][0], &sm.buf[s][li * kT], n0, hc);
+            wola_rows<kW, kFpga>(sm.stage[s][li][0], &sm.buf[s][li * kT], n0, tp);
             __syncwarp();
             if (lane == 0) mbar_arrive(&sm.fempty[s]);
             input_barrier(li);
@@ -798,9 +1016,13 @@ __global__ void __launch_bounds__(kThreads, 2) pack_kernel(const PackArgs a)
         if (io >= 0 && io < I) inv[io] = i;
     }
     init_front(sm, tid);
-    int hc[2][kP];
+    typename WolaTap<kW>::type tp[kP];
     const int li = tid >> 6, n0 = 2 * (tid & 63);
-    load_taps(a.filter, n0, hc);
+    {
+        int hc[2][kP];
+        load_taps(a.filter, n0, hc);
+        make_taps<kW, kFpga>(hc, tp);
+    }
     __syncthreads();
     // i_idx must be a permutation of the inputs: a column nobody writes means
     // it is not (out of range or repeated)
@@ -826,7 +1048,7 @@ __global__ void __launch_bounds__(kThreads, 2) pack_kernel(const PackArgs a)
             return;
         }
         if (tid < 32 && it + 1 < nsteps) produce(sm, a.vv, cc, it + 1, m0, a.nspectra, nullptr, a.status, inv);
-        wola_step<kW, kFpga>(sm, it & 1, li, n0, hc);
+        wola_step<kW, kFpga>(sm, it & 1, li, n0, tp);
         input_barrier(li);
         fft_step<kDemote, kFpga>(sm, tid);
         __syncthreads();
@@ -920,17 +1142,28 @@ static int dispatch(const Args &a, dim3 grid, int wola, bool fpga, bool demote, 
 }
 
 // Process-wide switches, read and written from any host thread.
-static std::atomic<int> g_pfb_variant{0}; // 0: autotuned; else forced inputs per step (4 or 8)
+static std::atomic<int> g_pfb_variant{0}; // 0: autotuned; else the forced variant (3, 4, 5 or 8)
 static std::atomic<int> g_pfb_last{0};    // inputs per step of the last fused launch
 
 template <int A, bool B, bool C> struct BeamSel {
     static int run_g(const BeamArgs &a, dim3 grid, cudaStream_t st, int g)
     {
         CUtensorMap wmap;
-        int rc = make_tmap_beam_weights(&wmap, a.W, a.nant, (int)grid.y, a.W_cc, g == 3 ? kG / 2 : g / 2);
+        int rc = make_tmap_beam_weights(&wmap, a.W, a.nant, (int)grid.y, a.W_cc, (g == 3 || g == 5) ? kG / 2 : g / 2);
         if (rc) return rc;
         g_pfb_last = g;
-        if (g == 3) {
+        if (g == 5) {
+            auto kern = beam_tm_kernel<A, B, C>;
+            constexpr int kSmem = (int)sizeof(TmSmem<typename WolaTap<A>::type>);
+            if ((rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem),
+                                 "cudaFuncSetAttribute(tm smem)")))
+                return rc;
+            // three CTAs' shared memory per SM
+            if ((rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
+                                 "cudaFuncSetAttribute(tm carveout)")))
+                return rc;
+            kern<<<grid, kThreads, kSmem, st>>>(a, wmap);
+        } else if (g == 3) {
             auto kern = beam_ws_kernel<A, B, C>;
             if ((rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                       (int)sizeof(WsSmem)),
@@ -970,7 +1203,7 @@ template <int A, bool B, bool C> struct BeamSel {
         if (!rc) rc = check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
         float best = 0.f;
         int pick = 4;
-        for (int g : {4, 8}) { // variant 3 measured slower on every shape tried; forced only
+        for (int g : {4, 8, 5}) { // variant 3 measured slower on every shape tried; forced only
             if (rc) break;
             rc = run_g(a, grid, st, g);
             if (!rc) rc = check_cuda(cudaEventRecord(e0, st), "cudaEventRecord");
@@ -1012,7 +1245,7 @@ int pfb_variant_last() { return g_pfb_last; }
 
 int pfb_variant(int g)
 {
-    if (g != 0 && g != 3 && g != 4 && g != 8) return -1;
+    if (g != 0 && g != 3 && g != 4 && g != 5 && g != 8) return -1;
     return g_pfb_variant.exchange(g);
 }
 

@@ -237,7 +237,7 @@ int vgb_pfb_variant_last(void) { return pfb_variant_last(); }
 int vgb_pfb_variant(int inputs_per_step)
 {
     const int prev = pfb_variant(inputs_per_step);
-    if (prev < 0) set_error(VGB_ERR_INVALID, "pfb_variant: 0 (timed choice), 4 or 8");
+    if (prev < 0) set_error(VGB_ERR_INVALID, "pfb_variant: 0 (timed choice), 3, 4, 5 or 8");
     return prev;
 }
 

@@ -303,8 +303,9 @@ def gemm_variant(v: int) -> int:
 
 
 def pfb_variant(g: int) -> int:
-    """Force the fused front end's variant (4 or 8 inputs per step, 3 the
-    warp-specialised kernel; 0 = timed choice)."""
+    """Force the fused front end's variant (4 or 8 inputs per step, 5 the
+    4-input shape at three CTAs per SM, 3 the warp-specialised kernel; 0 =
+    timed choice)."""
     prev = lib().vgb_pfb_variant(g)
     if prev < 0:
         raise VGBError(lib().vgb_last_error().decode())
@@ -312,7 +313,7 @@ def pfb_variant(g: int) -> int:
 
 
 def pfb_variant_last() -> int:
-    """Variant of the last fused front-end launch (4, 8 or 3; 0 before any)."""
+    """Variant of the last fused front-end launch (4, 8, 5 or 3; 0 before any)."""
     return lib().vgb_pfb_variant_last()
 
 

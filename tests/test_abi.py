@@ -68,7 +68,7 @@ def test_argument_errors_are_status_codes(vgb_mod):
     info = vgb_mod.SubfileInfo()
     assert lib.vgb_subfile_info_read(b"/nonexistent/x.sub", ctypes.byref(info)) == 1
     assert lib.vgb_legacy_read_second(b"/nonexistent/x.dat", 16, 0, 1) == 1
-    assert lib.vgb_pfb_variant(5) == -1
+    assert lib.vgb_pfb_variant(6) == -1
 
 
 def test_filter_exactness_rule(vgb_mod):

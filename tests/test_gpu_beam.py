@@ -88,9 +88,10 @@ def test_fused_beam_matches_oracle(vgb_mod, torch, oracle_mod, mode):
 
 @pytest.mark.parametrize("flags_name", ["smart", "full"])
 def test_fused_beam_inputs_per_step_identical(vgb_mod, torch, oracle_mod, flags_name):
-    """The front end's three shapes (4 inputs per step in 256-thread CTAs, 8 in
-    512-thread CTAs, and the warp-specialised 416-thread CTAs of variant 3)
-    give identical Stokes, beam voltages and incoherent sums; an odd tile
+    """The front end's four shapes (4 inputs per step in 256-thread CTAs, 8 in
+    512-thread CTAs, 4 at three CTAs per SM with the sums in tensor memory
+    (variant 5), and the warp-specialised 416-thread CTAs of variant 3) give
+    identical Stokes, beam voltages and incoherent sums; an odd tile
     count leaves the last step partly filled, and 70 spectra leave the last
     CTA partly filled."""
     nant, ns = 18, 70
@@ -101,15 +102,16 @@ def test_fused_beam_inputs_per_step_identical(vgb_mod, torch, oracle_mod, flags_
     W = weights_on_device(J, phi)
     flags = (vgb_mod.PFB_SMART if flags_name == "smart" else vgb_mod.PFB_FULL_PRECISION) | vgb_mod.WOLA_FP32
     out = {}
-    for g in (4, 8, 3):
+    for g in (4, 8, 5, 3):
         prev = vgb_mod.pfb_variant(g)
         try:
             out[g] = run_beam(vgb_mod, torch, htr, nant, 1, ns, filt, flags, W, 1 / 36)
         finally:
             vgb_mod.pfb_variant(prev)
         assert vgb_mod.check_device_status() == 0
-    for x4, x8, x3 in zip(out[4], out[8], out[3]):
+    for x4, x8, x5, x3 in zip(out[4], out[8], out[5], out[3]):
         assert np.array_equal(x4, x8)
+        assert np.array_equal(x4, x5)
         assert np.array_equal(x4, x3)
     with pytest.raises(vgb_mod.VGBError):
         vgb_mod.pfb_variant(6)
@@ -138,7 +140,7 @@ def test_split_wola_equals_int32(vgb_mod, torch, oracle_mod):
     W = weights_on_device(J, phi)
     full = vgb_mod.PFB_FULL_PRECISION
     ref = run_beam(vgb_mod, torch, htr, nant, 1, ns, h, full, W, 1 / 36)
-    for g in (4, 8, 3):
+    for g in (4, 8, 5, 3):
         prev = vgb_mod.pfb_variant(g)
         try:
             got = run_beam(vgb_mod, torch, htr, nant, 1, ns, h, full | vgb_mod.WOLA_FP32_SPLIT, W, 1 / 36)
