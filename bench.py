@@ -562,17 +562,24 @@ def gb300_arm(args, rank, local_rank, world):
         barrier()
         t0 = time.perf_counter()
         e2e_steps = max(1, min(args.steps, args.e2e_steps))
+        done = []                           # each second's completion on the pipeline's stream
         for _ in range(e2e_steps):
             e2e_step()
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record(stream)
+            done.append(ev)
         pipe.sync()
         barrier()
         e2e_s = max_over_ranks(time.perf_counter() - t0)
+        periods = np.array([done[i].elapsed_time(done[i + 1]) for i in range(len(done) - 1)])
         link_after = link_rate()
         e2e = {"value": e2e_steps * ncc_all / NCC / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": ncc * SECOND_BYTES,
                "d2h_bytes_per_step": psr_b + vdif_b + stat_b,
                "steps": e2e_steps, "ms_per_step": 1e3 * e2e_s / e2e_steps,
                "h2d_link_gbs": link_gbs, "h2d_link_gbs_after": link_after,
+               "step_period_ms": ({"median": float(np.median(periods)), "p90": float(np.percentile(periods, 90)),
+                                   "max": float(periods.max())} if periods.size else None),
                "link_bound": link_gbs * 1e9 / (ncc * SECOND_BYTES) * ncc_all / NCC,
                "path": "vgb_pipeline_run_host from pinned host memory, products (tied-array PSRFITS rows, "
                        "incoherent PSRFITS rows, VDIF frames, offsets, scales) back to pinned host buffers; "
