@@ -191,6 +191,62 @@ def test_fused_beam_stokes_i_only_and_batched(vgb_mod, torch, oracle_mod):
     assert rel_err(S[1, :, 0], Sref[0, :, 0]) < 1e-5
 
 
+@pytest.mark.parametrize("nant", [1, 256])
+def test_fused_beam_edge_sizes(vgb_mod, torch, oracle_mod, nant):
+    """The smallest and the largest arrays: one tile (half of the one step
+    empty) and 256 tiles (512 inputs, MWA Phase III). Every front-end shape
+    gives the same bytes, and they match the oracle's PFB + beamformer within
+    1e-5 (norm-wise)."""
+    ninputs, ns = 2 * nant, 24
+    htr = oracle_mod.mwax_buffer(61 + nant, 2, ninputs)
+    filt = SY.analysis_filter_int16()
+    J, phi = tables(nant)
+    W = weights_on_device(J, phi)
+    invw = 1.0 / ninputs
+    flags = vgb_mod.PFB_FULL_PRECISION | vgb_mod.WOLA_FP32
+    out = {}
+    for g in (4, 8, 5, 3):
+        prev = vgb_mod.pfb_variant(g)
+        try:
+            out[g] = run_beam(vgb_mod, torch, htr, nant, 1, ns, filt, flags, W, invw)
+        finally:
+            vgb_mod.pfb_variant(prev)
+    for g in (8, 5, 3):
+        for x, y in zip(out[g], out[4]):
+            assert np.array_equal(x, y), g
+    i_idx = SY.legacy_input_order(nant)
+    polQ, polP = pol_lists(i_idx)
+    v = oracle_mod.fpfb(htr, ninputs, ns, filt, K, 12, i_idx, flags & 0xFFFF)
+    Sref, eref = oracle_mod.beamform(v, J, phi, polQ, polP, invw)
+    S, e, _ = out[4]
+    assert rel_err(e[0], eref[0]) < 1e-5
+    if nant > 1:        # one tile's Stokes cancel to rounding (the test below)
+        for st in range(4):
+            assert rel_err(S[0, :, st], Sref[0, :, st]) < 1e-5, st
+
+
+def test_fused_beam_empty_and_bad_shapes(vgb_mod, torch, oracle_mod):
+    """No spectra: success, nothing written. No coarse channels, or an input
+    count that is not two per tile: a status code, nothing launched."""
+    nant = 4
+    htr = oracle_mod.mwax_buffer(3, 2, 2 * nant)
+    d = dev(htr.reshape(-1).view(np.uint8))
+    v = vgb_mod.reference_buffer_voltages(d, 2 * nant, 1)
+    J, phi = tables(nant)
+    W = weights_on_device(J, phi)
+    filt = dev(SY.analysis_filter_int16())
+    S = torch.full((16 * 4 * K,), 7.0, dtype=torch.float32, device="cuda")
+    vgb_mod.beamform_mwax(v, 1, 0, filt, vgb_mod.PFB_FULL_PRECISION, W, nant, 0.125, 4, S)
+    torch.cuda.synchronize()
+    assert vgb_mod.check_device_status() == 0
+    assert bool((S == 7.0).all())
+    with pytest.raises(vgb_mod.VGBError, match="ncc"):
+        vgb_mod.beamform_mwax(v, 0, 16, filt, vgb_mod.PFB_FULL_PRECISION, W, nant, 0.125, 4, S)
+    with pytest.raises(vgb_mod.VGBError, match="2\\*nant"):
+        vgb_mod.beamform_mwax(v, 1, 16, filt, vgb_mod.PFB_FULL_PRECISION, W, nant + 1, 0.125, 4, S)
+    assert bool((S == 7.0).all())
+
+
 def test_single_tile_autocorrelation_cancels(vgb_mod, torch, oracle_mod):
     """With one tile, |sum e|^2 - sum |e|^2 = 0: all Stokes vanish (to FP32
     rounding) while the beam voltages do not."""
