@@ -120,7 +120,10 @@ __device__ __forceinline__ void inverse_jones(const double2 *d, const double2 *b
         for (int i = 0; i < 4; i++) o[i] = make_double2(0.0, 0.0);
         return;
     }
-    for (int i = 0; i < 4; i++) m[i] = make_double2(m[i].x / F, m[i].y / F);
+    // one FP64 division instead of eight (FP64 is this GPU's slow pipe;
+    // the products differ from the quotients by at most an ulp)
+    const double rF = 1.0 / F;
+    for (int i = 0; i < 4; i++) m[i] = make_double2(m[i].x * rF, m[i].y * rF);
     const double2 det = zsub(zmul(m[0], m[3]), zmul(m[1], m[2]));
     const double scale = 1.0 / (det.x * det.x + det.y * det.y);
     const double2 inv = make_double2(scale * det.x, -scale * det.y);
