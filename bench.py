@@ -48,6 +48,8 @@ NI = 2 * NANT
 NSPEC = NBLK * 500
 SECOND_BYTES = NBLK * NI * 64000 * 2           # one coarse channel, one second
 BEAM_KERNEL_DRAM_BYTES_PER_CC = (1.322368e9 + 86.6944e6) / 2
+# the same for the three-CTAs-per-SM shape (variant 5): 1.323002 GB read + 86.5 MB written
+BEAM_TM_KERNEL_DRAM_BYTES_PER_CC = (1.323002e9 + 86.53568e6) / 2
 # Algorithmic FP32 flops of the fused PFB + beamformer per (RF input, fine
 # spectrum): the 12-tap weighted overlap-add of 128 complex samples
 # (12 x 2 x 2 x 128 = 6,144), a 128-point complex FFT counted as 5 N log2 N
@@ -599,7 +601,9 @@ def gb300_arm(args, rank, local_rank, world):
     # launch (1.3224 GB read + 86.7 MB written) scaled by the channels
     # processed, since each channel's voltages are read once and its products
     # written once
-    traffic = args.traffic if args.traffic is not None else ncc * BEAM_KERNEL_DRAM_BYTES_PER_CC
+    variant = vgb.pfb_variant_last()
+    per_cc = BEAM_TM_KERNEL_DRAM_BYTES_PER_CC if variant == 5 else BEAM_KERNEL_DRAM_BYTES_PER_CC
+    traffic = args.traffic if args.traffic is not None else ncc * per_cc
     achieved = alg_bytes / (stage[0] / 1e3) / 1e9
     # the compute side: FP32 flops of the launch against this GPU's measured
     # FP32 FMA throughput (scalar FFMA and packed FFMA2, the better of both)
@@ -616,15 +620,23 @@ def gb300_arm(args, rank, local_rank, world):
                "achieved": fp32_achieved, "unit": "TFLOP/s",
                "peak_ffma": fp32_ffma, "peak_ffma2": fp32_ffma2, "peak_source": "measured (vgb_fp32_peak)",
                "frac": (fp32_achieved / fp32_peak) if fp32_peak else None}
-    roofline = {"kernel": "beam_kernel (fused PFB + tied-array/incoherent beam + Stokes)", "bound": "hbm",
+    if variant == 5:
+        kname = "beam_tm_kernel (fused PFB + tied-array/incoherent beam + Stokes; three CTAs per SM)"
+        limiter = ("not HBM: the FMA pipe and the shared-memory pipe, each ~60 % busy, issue 65 % (ncu of a "
+                   "2-channel launch: issue 65.3 %, FMA pipe 59.6 %, shared-memory wavefronts 62.4 % of peak, "
+                   "math-pipe throttle the second stall reason; DRAM 1.41 GB in 1.875 ms)")
+    else:
+        kname = "beam_kernel (fused PFB + tied-array/incoherent beam + Stokes)"
+        limiter = ("not HBM: instruction issue, the FMA pipe and the shared-memory pipe, each ~60 % busy "
+                   "(ncu of a 2-channel launch: issue 61.0 %, FMA pipe 58.8 %, shared-memory wavefronts "
+                   "59.3 % of peak; DRAM 9.4 %)")
+    roofline = {"kernel": kname, "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                 "traffic": traffic, "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a "
                 "2-channel launch, scaled to the channels of this launch" if args.traffic is None else "--traffic",
                 "alg_bytes_per_launch": alg_bytes,
-                "limiter": "not HBM: instruction issue, the FMA pipe and the shared-memory pipe, each ~60 % busy "
-                           "(ncu of a 2-channel launch: issue 61.0 %, FMA pipe 58.8 %, shared-memory wavefronts "
-                           "59.3 % of peak; DRAM 9.4 %)",
+                "limiter": limiter, "pfb_variant": variant,
                 "stage_ms": {"pfb_beam": stage[0], "renormalise": stage[1], "ipfb_vdif": stage[2],
                              "history": stage[3], "tracking_tables": stage[4]},
                 "compute": compute}
