@@ -761,6 +761,7 @@ def multibeam_section(torch, vgb, SY, iters: int, cases=None, modes=None, nfine=
             mb.run(v, out=psr, offsets=off, scales=scl, stream=st)
             launches += mb.launches()
             stages = mb.stage_ms()
+            pair = mb.last_pair()
             mb.close()
             if vgb.check_device_status() != 0:
                 raise RuntimeError("device status raised in the many-beam bench")
@@ -771,7 +772,8 @@ def multibeam_section(torch, vgb, SY, iters: int, cases=None, modes=None, nfine=
             if prec != 3:
                 planes = 2 if prec == 0 else 1
                 mma_tf = alg * planes * 256 / 250 / (beam_ms / 1e3)
-                entry["roofline"] = {"kernel": "mb_beam_kernel", "bound": "tensor",
+                entry["roofline"] = {"kernel": f"mb_beam_pair_kernel (cta_group::2 over the two SMs of a TPC, "
+                                               f"{pair} pairs)" if pair else "mb_beam_kernel", "bound": "tensor",
                                      "achieved": alg / (beam_ms / 1e3), "peak": peak_tf, "unit": "TFLOP/s",
                                      "frac": alg / (beam_ms / 1e3) / peak_tf,
                                      "mma_issued_tflops": mma_tf, "mma_frac": mma_tf / peak_tf,
@@ -1021,6 +1023,8 @@ def main():
                     "and print their JSON; no bench line")
     ap.add_argument("--mb-modes", default=None, help="profiling: comma-separated precision modes")
     ap.add_argument("--mb-nfine", type=int, default=K, help="profiling: fine channels per case")
+    ap.add_argument("--mb-beam-variant", type=int, default=0, choices=[0, 1, 2],
+                    help="many-beam GEMM kernel: 0 automatic, 1 single CTA, 2 CTA pairs")
     ap.add_argument("--mb-stream-iters", type=int, default=3, help="many-beam host-streaming calls timed (0: skip)")
     ap.add_argument("--no-pfb-only", dest="pfb_only", action="store_false",
                     help="skip the PFB-only (fine_pfb_offline) section")
@@ -1050,6 +1054,7 @@ def main():
         import vgb
 
         vgb.lib()
+        vgb.multibeam_beam_variant(args.mb_beam_variant)
         sec, nl = multibeam_section(torch, vgb, SY, args.mb_iters, cases=args.mb_only.split(","),
                                     modes=args.mb_modes.split(",") if args.mb_modes else None, nfine=args.mb_nfine,
                                     stream_iters=args.mb_stream_iters)

@@ -555,6 +555,19 @@ int vgb_multibeam_run_host(vgb_multibeam *mb, const void *v_host, uint8_t *out_h
                            float *scl_host, void *stream);
 /* Kernels the last vgb_multibeam_run launched. */
 int vgb_multibeam_launches(const vgb_multibeam *mb);
+/* The beam GEMM's kernel, for all multibeam objects (results are identical):
+ * 0 (default) automatic: where the beam tiles of 32 beams pair up, an
+ * object's first run (outside stream capture) times the CTA-pair kernel
+ * (cta_group::2: the two SMs of a TPC share one 256-row MMA and each stages
+ * half of the voltage tile) against the single-CTA kernel on its first coarse
+ * channel, two launches each, waits for them, and keeps the faster (a first
+ * run inside a capture takes the pair kernel); otherwise the single-CTA
+ * kernel. 1 the single-CTA kernel; 2 the pair kernel or an error. Returns the
+ * previous setting (-1 on a bad value). */
+int vgb_multibeam_beam_variant(int v);
+/* CTA pairs (2-CTA clusters) the last beam GEMM ran on; 0 if it ran the
+ * single-CTA kernel. */
+int vgb_multibeam_last_pair(const vgb_multibeam *mb);
 /* Stage timing with CUDA events (off by default): ms[0..4] = weights,
  * voltage conversion, autocorrelation GEMM, beam GEMM, renormalise of the
  * last run, summed over coarse channels (waits for the run to finish). */

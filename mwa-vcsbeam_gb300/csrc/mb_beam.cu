@@ -42,6 +42,8 @@
 // the wrap of the phase turns dt * f (geometry.c:40-101) are FP64; the
 // per-(beam, tile, channel) product and the sine/cosine of the wrapped phase
 // are FP32 (relative error ~1e-7, below the 2^-17 of the split weights).
+#include <atomic>
+
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -576,6 +578,98 @@ struct MbBeamArgs {
     unsigned *status;
 };
 
+// Epilogue of one accumulator tile (beam tile m, sample tile n, fine channel
+// c) by one thread of warps 2-5: TMEM lane `row` of the 256 columns at
+// `tacc` (lane quarter and buffer included). Lanes 4b..4b+3 hold beam b's
+// Xr, Xi, Yr, Yi; XX, YY, XY are formed across them, integrated over 10
+// samples, the autocorrelation term subtracted (form_beam.cpp:300-371) and
+// Stokes written [chan][beam][stokes][t], with each row's extremes folded into
+// order-preserving integer atomics for the 8-bit stage. `wait` blocks until
+// the accumulator is complete (false: it gave up, nothing is written);
+// `release` hands the TMEM buffer back once every load of it has finished.
+template <int kNst, class Wait, class Release>
+__device__ __forceinline__ bool mb_epilogue_tile(const MbBeamArgs &g, uint32_t tacc, int m, int n, int c, int row,
+                                                 Wait &&wait, Release &&release)
+{
+    const int lane = threadIdx.x & 31;
+    const int l = lane & 3;
+    const int bl = row >> 2;
+    const int p = m * kMbBeamsPerTile + bl;
+    const int t0 = n * kMbNint;
+    const int nv = min(kMbNint, g.nint - t0);
+    const int st = kNst == 4 ? l : 0;
+    const bool writer = p < g.B && (kNst == 4 || l == 0);
+    const long long rrow = (long long)c * g.Mq + (long long)p * kNst + st;
+    float rv[kMbNint];
+    float qs = 0.f;
+    if (writer) qs = g.qscale[rrow];
+#pragma unroll
+    for (int i = 0; i < kMbNint; i++) rv[i] = (writer && i < nv) ? g.R[rrow * g.nint_p + t0 + i] : 0.f;
+    float *srow = g.S + (((long long)c * g.B + p) * kNst + st) * g.nint + t0;
+    float smin = __int_as_float(0x7f800000), smax = -__int_as_float(0x7f800000);
+
+    if (!wait()) {
+        if (lane == 0) atomicOr(g.status, kErrWaitTimeout);
+        return false;
+    }
+    tc_fence_after();
+    float sq = 0.f, pb = 0.f, pc = 0.f;
+#pragma unroll
+    for (int j = 0; j < kMbN / 32; j++) {
+        float v[32];
+        tmem_ld32(tacc + 32 * j, v);
+#pragma unroll
+        for (int col = 0; col < 32; col++) {
+            const int gcol = 32 * j + col;
+            if (gcol < kMbUsed) {
+                const float x = v[col];
+                sq = fmaf(x, x, sq);
+                if (kNst == 4) {
+                    const float xb = __shfl_xor_sync(0xffffffffu, x, 2);
+                    const float xc = __shfl_xor_sync(0xffffffffu, x, 3);
+                    pb = fmaf(x, xb, pb);
+                    pc = fmaf(x, xc, pc);
+                }
+                if (gcol % kMbInt == kMbInt - 1) {
+                    const int ti = gcol / kMbInt;
+                    float val;
+                    if (kNst == 4) {
+                        // lanes of a beam: 0 Xr, 1 Xi, 2 Yr, 3 Yi
+                        const float t1 = sq + __shfl_xor_sync(0xffffffffu, sq, 1);
+                        const float t1o = __shfl_xor_sync(0xffffffffu, t1, 2);
+                        const float xx = l < 2 ? t1 : t1o, yy = l < 2 ? t1o : t1;
+                        const float re = pb + __shfl_xor_sync(0xffffffffu, pb, 1);
+                        const float d = __shfl_xor_sync(0xffffffffu, pc, 1) - pc;
+                        const float im = (l == 0 || l == 3) ? d : -d;
+                        val = l == 0 ? xx + yy : l == 1 ? xx - yy : l == 2 ? 2.f * re : -2.f * im;
+                    } else {
+                        float t1 = sq + __shfl_xor_sync(0xffffffffu, sq, 1);
+                        t1 += __shfl_xor_sync(0xffffffffu, t1, 2);
+                        val = t1;
+                    }
+                    if (writer && ti < nv) {
+                        const float sv = g.invw * (val - qs * rv[ti]);
+                        srow[ti] = sv;
+                        smin = fminf(smin, sv);
+                        smax = fmaxf(smax, sv);
+                        if (ti == 0 && t0 == 0) g.stats.nan0[((long long)c * g.B + p) * kNst + st] = sv != sv;
+                    }
+                    sq = pb = pc = 0.f;
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncwarp();
+    release();
+    if (writer) {
+        const long long r = ((long long)c * g.B + p) * kNst + st;
+        atomicMin(&g.stats.mn[r], fkey(smin));
+        atomicMax(&g.stats.mx[r], fkey(smax));
+    }
+    return true;
+}
+
 template <int kPlanes, bool kF16, int kNst>
 __global__ void __launch_bounds__(kMbThreads, 1)
     mb_beam_kernel(const __grid_constant__ CUtensorMap tw, const __grid_constant__ CUtensorMap tv, const MbBeamArgs g)
@@ -685,88 +779,19 @@ __global__ void __launch_bounds__(kMbThreads, 1)
     } else {
         // ---- epilogue: warps 2-5, TMEM lane quarter = warp % 4 ----
         const int q4 = warp & 3;
-        const int row = 32 * q4 + lane;
-        const int l = lane & 3;
-        const int bl = row >> 2;
         uint32_t tc = 0;
         for (long long tile = blockIdx.x; tile < g.total; tile += gridDim.x, tc++) {
             const int buf = tc & 1;
             const int m = (int)(tile % g.mtiles);
             const int n = (int)((tile / g.mtiles) % g.ntn);
             const int c = (int)(tile / per_tile);
-            const int p = m * kMbBeamsPerTile + bl;
-            const int t0 = n * kMbNint;
-            const int nv = min(kMbNint, g.nint - t0);
-            const int st = kNst == 4 ? l : 0;
-            const bool writer = p < g.B && (kNst == 4 || l == 0);
-            const long long rrow = (long long)c * g.Mq + (long long)p * kNst + st;
-            float rv[kMbNint];
-            float qs = 0.f;
-            if (writer) qs = g.qscale[rrow];
-#pragma unroll
-            for (int i = 0; i < kMbNint; i++) rv[i] = (writer && i < nv) ? g.R[rrow * g.nint_p + t0 + i] : 0.f;
-            float *srow = g.S + (((long long)c * g.B + p) * kNst + st) * g.nint + t0;
-            float smin = __int_as_float(0x7f800000), smax = -__int_as_float(0x7f800000);
-
-            if (!mbar_wait_bounded(&sm.tfull[buf], (tc >> 1) & 1, kMbPolls)) {
-                if (lane == 0) atomicOr(g.status, kErrWaitTimeout);
-                break;
-            }
-            tc_fence_after();
-            float sq = 0.f, pb = 0.f, pc = 0.f;
-#pragma unroll
-            for (int j = 0; j < kMbN / 32; j++) {
-                float v[32];
-                tmem_ld32(tmem + ((uint32_t)(32 * q4) << 16) + buf * kMbN + 32 * j, v);
-#pragma unroll
-                for (int col = 0; col < 32; col++) {
-                    const int gcol = 32 * j + col;
-                    if (gcol < kMbUsed) {
-                        const float x = v[col];
-                        sq = fmaf(x, x, sq);
-                        if (kNst == 4) {
-                            const float xb = __shfl_xor_sync(0xffffffffu, x, 2);
-                            const float xc = __shfl_xor_sync(0xffffffffu, x, 3);
-                            pb = fmaf(x, xb, pb);
-                            pc = fmaf(x, xc, pc);
-                        }
-                        if (gcol % kMbInt == kMbInt - 1) {
-                            const int ti = gcol / kMbInt;
-                            float val;
-                            if (kNst == 4) {
-                                // lanes of a beam: 0 Xr, 1 Xi, 2 Yr, 3 Yi
-                                const float t1 = sq + __shfl_xor_sync(0xffffffffu, sq, 1);
-                                const float t1o = __shfl_xor_sync(0xffffffffu, t1, 2);
-                                const float xx = l < 2 ? t1 : t1o, yy = l < 2 ? t1o : t1;
-                                const float re = pb + __shfl_xor_sync(0xffffffffu, pb, 1);
-                                const float d = __shfl_xor_sync(0xffffffffu, pc, 1) - pc;
-                                const float im = (l == 0 || l == 3) ? d : -d;
-                                val = l == 0 ? xx + yy : l == 1 ? xx - yy : l == 2 ? 2.f * re : -2.f * im;
-                            } else {
-                                float t1 = sq + __shfl_xor_sync(0xffffffffu, sq, 1);
-                                t1 += __shfl_xor_sync(0xffffffffu, t1, 2);
-                                val = t1;
-                            }
-                            if (writer && ti < nv) {
-                                const float sv = g.invw * (val - qs * rv[ti]);
-                                srow[ti] = sv;
-                                smin = fminf(smin, sv);
-                                smax = fmaxf(smax, sv);
-                                if (ti == 0 && t0 == 0) g.stats.nan0[((long long)c * g.B + p) * kNst + st] = sv != sv;
-                            }
-                            sq = pb = pc = 0.f;
-                        }
-                    }
-                }
-            }
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&sm.tempty[buf]);
-            if (writer) {
-                const long long r = ((long long)c * g.B + p) * kNst + st;
-                atomicMin(&g.stats.mn[r], fkey(smin));
-                atomicMax(&g.stats.mx[r], fkey(smax));
-            }
+            const bool ok = mb_epilogue_tile<kNst>(
+                g, tmem + ((uint32_t)(32 * q4) << 16) + buf * kMbN, m, n, c, 32 * q4 + lane,
+                [&] { return mbar_wait_bounded(&sm.tfull[buf], (tc >> 1) & 1, kMbPolls); },
+                [&] {
+                    if (lane == 0) mbar_arrive(&sm.tempty[buf]);
+                });
+            if (!ok) break;
         }
     }
     __syncwarp();
@@ -774,6 +799,187 @@ __global__ void __launch_bounds__(kMbThreads, 1)
     __syncthreads();
     tc_fence_after();
     if (warp == 0) tmem_dealloc(tmem, 512);
+}
+
+// ---------------------------------------------------------------------------
+// The beam GEMM over CTA pairs (cta_group::2)
+// ---------------------------------------------------------------------------
+// mb_beam_kernel's 128 x 256 tile needs 48 KB of operands per 64-wide K step
+// from L2 for 2 M MACs (single plane): at the tensor pipe's rate that stream
+// is the limit of the single-plane modes (tensor pipe ~70 % active). Here the
+// two CTAs of a cluster (the two SMs of a TPC) own beam tiles 2i and 2i + 1 of
+// the same 256-sample tile: each stages its own 128 weight rows and HALF of
+// the voltage tile (128 samples), and one thread of the even CTA issues
+// 256 x 256 x 16 MMAs that read both CTAs' shared memory, so each SM takes in
+// 32 KB per K step instead of 48 KB for the same MMA work. Each CTA's tensor
+// memory holds its own 128 beam rows x 256 samples, and the epilogue is
+// mb_beam_kernel's (identical arithmetic, same outputs).
+//   warp 0 lane 0 (both CTAs): the TMA producer. Both CTAs' copies complete
+//     on the even CTA's `full` barriers, whose expected byte count the even
+//     CTA posts for the pair; each waits on its own `empty` barrier, which the
+//     MMA commit reaches in both CTAs.
+//   warp 1 lane 0 (even CTA): MMA issuer; each accumulator buffer is handed
+//     to both CTAs' epilogues (`tfull`, multicast commit) and comes back when
+//     all eight epilogue warps of the pair have arrived on the even CTA's
+//     `tempty`.
+//   warps 2-5 (both CTAs): epilogue of the CTA's own beam tile.
+// Every wait is bounded; the CTAs meet at a cluster barrier before either
+// releases tensor memory or exits, so neither leaves while the other may
+// still signal its barriers.
+template <int kPlanes> struct Mb2Ring {
+    static constexpr int kTileA = 128 * 128;         // 128 weight rows x 64 K, 16-bit
+    static constexpr int kTileB = 128 * 128;         // half the voltage tile: 128 samples x 64 K
+    static constexpr int kStage = kPlanes * kTileA + kTileB;
+    static constexpr int kStages = kPlanes == 2 ? 4 : 6;
+};
+
+template <int kPlanes> struct Mb2Smem {
+    uint8_t ring[Mb2Ring<kPlanes>::kStages][Mb2Ring<kPlanes>::kStage];
+    uint64_t full[Mb2Ring<kPlanes>::kStages], empty[Mb2Ring<kPlanes>::kStages];
+    uint64_t tfull[2], tempty[2], drain;
+    uint32_t tmem;
+};
+
+template <int kPlanes, bool kF16, int kNst>
+__global__ void __launch_bounds__(kMbThreads, 1)
+    mb_beam_pair_kernel(const __grid_constant__ CUtensorMap tw, const __grid_constant__ CUtensorMap tv2,
+                        const MbBeamArgs g)
+{
+    using Ring = Mb2Ring<kPlanes>;
+    constexpr int kStages = Ring::kStages;
+    extern __shared__ uint8_t mb_raw[];
+    Mb2Smem<kPlanes> &sm =
+        *reinterpret_cast<Mb2Smem<kPlanes> *>((reinterpret_cast<uintptr_t>(mb_raw) + 1023) & ~uintptr_t(1023));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t rank = cluster_rank();
+    const long long pair = blockIdx.x >> 1, npairs = gridDim.x >> 1;
+    const int mtp = g.mtiles >> 1;                 // beam-tile pairs
+    const long long per_c = (long long)g.ntn * mtp;
+    const long long total = per_c * g.nfine;
+
+    if (threadIdx.x == 0) {
+        prefetch_tmap(&tw);
+        prefetch_tmap(&tv2);
+        for (int s = 0; s < kStages; s++) {
+            mbar_init(&sm.full[s], 1);
+            mbar_init(&sm.empty[s], 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&sm.tfull[b], 1);
+            mbar_init(&sm.tempty[b], 8);          // four epilogue warps in each CTA
+        }
+        mbar_init(&sm.drain, 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    if (warp == 0) {
+        tmem_alloc_pair(&sm.tmem, 512);
+        tmem_relinquish_pair();
+    }
+    tc_fence_before();
+    // both CTAs' barriers are initialised before either signals the other's
+    cluster_sync();
+    tc_fence_after();
+    const uint32_t tmem = sm.tmem;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---- TMA producer (both CTAs) ----
+            uint32_t it = 0;
+            bool ok = true;
+            for (long long pt = pair; pt < total && ok; pt += npairs) {
+                const int mp = (int)(pt % mtp);
+                const int n = (int)((pt / mtp) % g.ntn);
+                const int c = (int)(pt / per_c);
+                const int arow = c * g.Mrows + (2 * mp + (int)rank) * 128;
+                const int brow = c * g.ns + n * kMbUsed + (int)rank * 128;
+                for (int kc = 0; kc < g.nk; kc++, it++) {
+                    const int s = it % kStages;
+                    const uint32_t r = it / kStages;
+                    if (r > 0 && !mbar_wait_cluster(&sm.empty[s], (r - 1) & 1, kMbPolls)) {
+                        atomicOr(g.status, kErrWaitTimeout);
+                        ok = false;
+                        break;
+                    }
+                    uint8_t *st = sm.ring[s];
+                    const uint32_t full0 = mapa_shared(smem_u32(&sm.full[s]), 0);
+                    if (rank == 0) mbar_arrive_expect_tx(&sm.full[s], 2 * Ring::kStage);
+                    tma_load_2d_pair(st, &tw, kc * 64, arow, full0);
+                    if (kPlanes == 2)
+                        tma_load_2d_pair(st + Ring::kTileA, &tw, kc * 64, arow + g.nfine * g.Mrows, full0);
+                    tma_load_2d_pair(st + kPlanes * Ring::kTileA, &tv2, kc * 64, brow, full0);
+                }
+            }
+            // the even CTA: every copy of the pair has landed before the
+            // cluster barrier below lets either CTA leave
+            if (rank == 0)
+                for (uint32_t k = (it > kStages ? it - kStages : 0); k < it; k++)
+                    mbar_wait_cluster(&sm.full[k % kStages], (k / kStages) & 1, kMbPolls);
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && rank == 0) {
+            // ---- MMA issuer (even CTA) ----
+            const uint32_t idesc = idesc_pair_f32(kMbN, kF16);
+            uint32_t it = 0, tc = 0;
+            bool ok = true;
+            for (long long pt = pair; pt < total && ok; pt += npairs, tc++) {
+                const int buf = tc & 1;
+                const uint32_t u = tc >> 1;
+                if (u > 0 && !mbar_wait_cluster(&sm.tempty[buf], (u - 1) & 1, kMbPolls)) {
+                    atomicOr(g.status, kErrWaitTimeout);
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d = tmem + buf * kMbN;
+                for (int kc = 0; kc < g.nk; kc++, it++) {
+                    const int s = it % kStages;
+                    if (!mbar_wait_cluster(&sm.full[s], (it / kStages) & 1, kMbPolls)) {
+                        atomicOr(g.status, kErrWaitTimeout);
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t sa = smem_u32(sm.ring[s]);
+                    const uint64_t a0 = sdesc_sw128(sa);
+                    const uint64_t a1 = sdesc_sw128(sa + Ring::kTileA);
+                    const uint64_t bd = sdesc_sw128(sa + kPlanes * Ring::kTileA);
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        tc_mma_pair(d, sdesc_advance_k(a0, k), sdesc_advance_k(bd, k), idesc, (kc | k) != 0);
+                        if (kPlanes == 2) tc_mma_pair(d, sdesc_advance_k(a1, k), sdesc_advance_k(bd, k), idesc, 1);
+                    }
+                    tc_commit_pair_both(&sm.empty[s]);
+                }
+                if (ok) tc_commit_pair_both(&sm.tfull[buf]);
+            }
+            // all MMAs this thread issued have completed before teardown
+            tc_commit_pair_own(&sm.drain);
+            mbar_wait_cluster(&sm.drain, 0, kMbPolls);
+        }
+    } else {
+        // ---- epilogue: warps 2-5 of both CTAs, TMEM lane quarter = warp % 4 ----
+        const int q4 = warp & 3;
+        const uint32_t tempty0 = mapa_shared(smem_u32(&sm.tempty[0]), 0), tempty1 = mapa_shared(smem_u32(&sm.tempty[1]), 0);
+        uint32_t tc = 0;
+        for (long long pt = pair; pt < total; pt += npairs, tc++) {
+            const int buf = tc & 1;
+            const int mp = (int)(pt % mtp);
+            const int n = (int)((pt / mtp) % g.ntn);
+            const int c = (int)(pt / per_c);
+            const bool ok = mb_epilogue_tile<kNst>(
+                g, tmem + ((uint32_t)(32 * q4) << 16) + buf * kMbN, 2 * mp + (int)rank, n, c, 32 * q4 + lane,
+                [&] { return mbar_wait_cluster(&sm.tfull[buf], (tc >> 1) & 1, kMbPolls); },
+                [&] {
+                    if (lane == 0) mbar_arrive_cluster(buf ? tempty1 : tempty0);
+                });
+            if (!ok) break;
+        }
+    }
+    __syncwarp();
+    tc_fence_before();
+    cluster_sync();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc_pair(tmem, 512);
 }
 
 
@@ -1077,6 +1283,10 @@ struct vgb_multibeam {
     uint32_t *d_stats = nullptr; // min keys, max keys, first-is-NaN: 3 x [nfine][B][nst]
     bool simt = false;
     CUtensorMap tmW, tmV;
+    CUtensorMap tmV2;            // voltages in 128-sample boxes: the pair kernel's half tiles
+    int pair_clusters = -1;      // co-resident 2-CTA clusters of the pair kernel (-1: not yet asked)
+    int beam_pick = 0;           // automatic choice: 0 undecided, 1 single-CTA kernel, 2 pair kernel
+    int last_pair = 0;           // CTA pairs of the last beam GEMM (0: the single-CTA kernel ran)
     bool have_geometry = false, have_jones = false;
     int nsm = 0;
     int last_launches = 0; // kernels the last run launched
@@ -1123,7 +1333,56 @@ void mb_free(vgb_multibeam *mb)
         if (p) cudaFree(p);
 }
 
-template <int kPlanes, bool kF16, int kNst> int mb_launch_beam(vgb_multibeam *mb, const MbBeamArgs &a, cudaStream_t st)
+// Beam GEMM kernel: 0 = the pair kernel where the beam tiles pair up and a
+// 2-CTA cluster fits, else the single-CTA kernel; 1 = always the single-CTA
+// kernel; 2 = the pair kernel wherever the beam tiles pair up.
+std::atomic<int> g_mb_beam_variant{0};
+
+// The pair kernel over as many co-resident 2-CTA clusters as the tiles need
+// (at most the occupancy query's count). Returns 1 (nothing launched) when no
+// cluster of that shape fits on the device.
+template <int kPlanes, bool kF16, int kNst>
+int mb_launch_beam_pair(vgb_multibeam *mb, const MbBeamArgs &a, cudaStream_t st)
+{
+    auto kern = mb_beam_pair_kernel<kPlanes, kF16, kNst>;
+    // 16 KB beyond the ring: the last stage's half voltage tile is followed by
+    // memory of this CTA whatever extent the MMA reads from it
+    const int smem = (int)sizeof(Mb2Smem<kPlanes>) + 1024 + 16384;
+    int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                        "cudaFuncSetAttribute(mb_beam_pair_kernel)");
+    if (rc) return rc;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(kMbThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (mb->pair_clusters < 0) {
+        int n = 0;
+        cfg.gridDim = dim3(2 * (unsigned)mb->nsm);
+        if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            n = 0;
+        }
+        mb->pair_clusters = n;
+    }
+    if (mb->pair_clusters <= 0) return 1;
+    const long long pairs = a.total / 2;
+    const long long clusters = pairs < mb->pair_clusters ? pairs : mb->pair_clusters;
+    cfg.gridDim = dim3(2 * (unsigned)clusters);
+    rc = check_cuda(cudaLaunchKernelEx(&cfg, kern, mb->tmW, mb->tmV2, a), "cudaLaunchKernelEx(mb_beam_pair_kernel)");
+    if (!rc) rc = check_launch("mb_beam_pair_kernel");
+    if (!rc) mb->last_pair = (int)clusters;
+    return rc;
+}
+
+template <int kPlanes, bool kF16, int kNst>
+int mb_launch_beam_single(vgb_multibeam *mb, const MbBeamArgs &a, cudaStream_t st)
 {
     auto kern = mb_beam_kernel<kPlanes, kF16, kNst>;
     const int smem = (int)sizeof(MbSmem<kPlanes>) + 1024;
@@ -1132,7 +1391,64 @@ template <int kPlanes, bool kF16, int kNst> int mb_launch_beam(vgb_multibeam *mb
     if (rc) return rc;
     const long long grid = a.total < mb->nsm ? a.total : mb->nsm;
     kern<<<(unsigned)grid, kMbThreads, smem, st>>>(mb->tmW, mb->tmV, a);
+    mb->last_pair = 0;
     return check_launch("mb_beam_kernel");
+}
+
+// The automatic choice for this object, made on its first beam GEMM outside
+// stream capture: both kernels run twice on this coarse channel (each run
+// writes the same Stokes and the same idempotent row extremes) and the faster
+// is kept. The host waits for those four launches once.
+template <int kPlanes, bool kF16, int kNst>
+int mb_pick_beam(vgb_multibeam *mb, const MbBeamArgs &a, cudaStream_t st)
+{
+    cudaEvent_t ev[3] = {};
+    int rc = VGB_SUCCESS;
+    for (int i = 0; i < 3 && !rc; i++) rc = check_cuda(cudaEventCreate(&ev[i]), "cudaEventCreate");
+    float t_single = 0.f, t_pair = 0.f;
+    bool fits = true;
+    if (!rc) rc = check_cuda(cudaEventRecord(ev[0], st), "cudaEventRecord");
+    for (int i = 0; i < 2 && !rc; i++) rc = mb_launch_beam_single<kPlanes, kF16, kNst>(mb, a, st);
+    if (!rc) rc = check_cuda(cudaEventRecord(ev[1], st), "cudaEventRecord");
+    for (int i = 0; i < 2 && !rc && fits; i++) {
+        const int r = mb_launch_beam_pair<kPlanes, kF16, kNst>(mb, a, st);
+        if (r == 1) fits = false;
+        else rc = r;
+    }
+    if (!rc) rc = check_cuda(cudaEventRecord(ev[2], st), "cudaEventRecord");
+    if (!rc) rc = check_cuda(cudaEventSynchronize(ev[2]), "cudaEventSynchronize");
+    if (!rc) rc = check_cuda(cudaEventElapsedTime(&t_single, ev[0], ev[1]), "cudaEventElapsedTime");
+    if (!rc) rc = check_cuda(cudaEventElapsedTime(&t_pair, ev[1], ev[2]), "cudaEventElapsedTime");
+    for (cudaEvent_t e : ev)
+        if (e) cudaEventDestroy(e);
+    if (!rc) mb->beam_pick = fits && t_pair < t_single ? 2 : 1;
+    return rc;
+}
+
+template <int kPlanes, bool kF16, int kNst> int mb_launch_beam(vgb_multibeam *mb, const MbBeamArgs &a, cudaStream_t st)
+{
+    const int v = g_mb_beam_variant.load();
+    const bool pairs_ok = mb->mtiles % 2 == 0;
+    if (v == 2 && !pairs_ok)
+        return set_error(VGB_ERR_UNSUPPORTED, "multibeam: the pair kernel needs an even number of beam tiles");
+    if (v == 0 && pairs_ok && mb->beam_pick == 0) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+            cudaGetLastError();
+            cs = cudaStreamCaptureStatusActive;
+        }
+        if (cs == cudaStreamCaptureStatusNone) {
+            const int rc = mb_pick_beam<kPlanes, kF16, kNst>(mb, a, st);
+            if (rc) return rc;
+        }
+    }
+    // undecided (first run inside a capture): the pair kernel
+    if (v == 2 || (v == 0 && pairs_ok && mb->beam_pick != 1)) {
+        const int r = mb_launch_beam_pair<kPlanes, kF16, kNst>(mb, a, st);
+        if (r != 1) return r;
+        if (v == 2) return set_error(VGB_ERR_UNSUPPORTED, "multibeam: no 2-CTA cluster of the pair kernel fits");
+    }
+    return mb_launch_beam_single<kPlanes, kF16, kNst>(mb, a, st);
 }
 
 } // namespace
@@ -1212,6 +1528,9 @@ extern "C" int vgb_multibeam_create(const vgb_multibeam_config *cfg, vgb_multibe
                             128, mb->fp16);
     if (!rc)
         rc = make_tmap_bf16(&mb->tmV, mb->d_V, (uint64_t)nf * c.nsamples, mb->KA, (uint64_t)mb->KA * 2, kMbN,
+                            mb->fp16);
+    if (!rc)
+        rc = make_tmap_bf16(&mb->tmV2, mb->d_V, (uint64_t)nf * c.nsamples, mb->KA, (uint64_t)mb->KA * 2, kMbN / 2,
                             mb->fp16);
     if (rc) {
         mb_free(mb);
@@ -1603,3 +1922,11 @@ extern "C" int vgb_multibeam_launches(const vgb_multibeam *mb)
     // per coarse channel: weights, convert, R GEMM, beam GEMM (+ renormalise)
     return mb ? mb->last_launches : 0;
 }
+
+extern "C" int vgb_multibeam_beam_variant(int v)
+{
+    if (v < 0 || v > 2) return set_error(VGB_ERR_INVALID, "multibeam_beam_variant: 0, 1 or 2"), -1;
+    return g_mb_beam_variant.exchange(v);
+}
+
+extern "C" int vgb_multibeam_last_pair(const vgb_multibeam *mb) { return mb ? mb->last_pair : 0; }

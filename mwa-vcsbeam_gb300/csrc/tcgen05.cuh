@@ -57,6 +57,13 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t N, bool negate_a 
            | ((128u >> 4) << 24);       // M >> 4
 }
 
+// The same for an MMA issued over a CTA pair (cta_group::2): M = 256, rows
+// 0-127 from the issuing CTA's shared memory and 128-255 from its peer's.
+__host__ __device__ constexpr uint32_t idesc_pair_f32(uint32_t N, bool fp16 = false)
+{
+    return (idesc_bf16_f32(N, false, fp16) & ~(0x1Fu << 24)) | ((256u >> 4) << 24);
+}
+
 // Shared-memory matrix descriptor for a SWIZZLE_128B K-major tile whose
 // 1024-byte aligned start is `saddr` (shared-space byte address).
 __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr)
@@ -199,6 +206,116 @@ __device__ __forceinline__ void tma_load_5d(void *dst, const CUtensorMap *map, i
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap *map)
 {
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// CTA pairs (cta_group::2): the two CTAs of a 2-CTA cluster, which the
+// hardware places on the two SMs of one TPC. One thread of the even CTA
+// issues MMAs with M = 256 whose A rows and B columns are split between the
+// two CTAs' shared memory (same offsets in both) and whose accumulator rows
+// are split between their tensor memories (rows 0-127 in the even CTA, 128-255
+// in the odd one, same columns). Every tcgen05 instruction of such a kernel
+// names cta_group::2; the allocation is made collectively by one warp of each
+// CTA.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t cluster_rank()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// Shared::cluster address of the object at shared-space address `saddr` of
+// this CTA, in the CTA of cluster rank `rank`.
+__device__ __forceinline__ uint32_t mapa_shared(uint32_t saddr, uint32_t rank)
+{
+    uint32_t d;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d) : "r"(saddr), "r"(rank));
+    return d;
+}
+
+// All threads of both CTAs; orders earlier shared-memory writes (barrier
+// initialisation included) before the peer's later accesses.
+__device__ __forceinline__ void cluster_sync()
+{
+    asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc_pair(uint32_t *dst_smem, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
+                 "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish_pair()
+{
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc_pair(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void tc_mma_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// Arrive on the mbarrier at the same offset as `bar` in both CTAs of the pair
+// once the pair MMAs issued before it have completed.
+__device__ __forceinline__ void tc_commit_pair_both(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::
+                     "r"(smem_u32(bar)),
+                 "h"((uint16_t)0x3)
+                 : "memory");
+}
+// The same on this CTA's own `bar` only.
+__device__ __forceinline__ void tc_commit_pair_own(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// 2-D tiled load into this CTA's shared memory whose completion is counted on
+// the mbarrier at shared::cluster address `bar_cl` (this CTA's or its peer's).
+__device__ __forceinline__ void tma_load_2d_pair(void *dst, const CUtensorMap *map, int x, int y, uint32_t bar_cl)
+{
+    asm volatile("cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, "
+                 "{%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+                 "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar_cl)
+                 : "memory");
+}
+
+// Arrive (release at cluster scope) on the mbarrier at shared::cluster address
+// `bar_cl`.
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cl)
+{
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cl) : "memory");
+}
+
+// Bounded wait with acquire at cluster scope (the phase may have been
+// completed by the peer CTA's arrivals or copies).
+__device__ __forceinline__ bool mbar_wait_cluster(uint64_t *bar, uint32_t phase, uint32_t max_polls)
+{
+    const uint32_t addr = smem_u32(bar);
+    for (uint32_t i = 0; i < max_polls; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n"
+            " mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
 }
 
 // Host: build a 2-D tensor map over a row-major bf16 matrix [rows][cols]

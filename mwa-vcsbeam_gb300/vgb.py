@@ -178,6 +178,8 @@ _SIGS = {
     "vgb_multibeam_run": (I, [V, V, V, V, V, V, V]),
     "vgb_multibeam_run_host": (I, [V, V, V, V, V, V]),
     "vgb_multibeam_launches": (I, [V]),
+    "vgb_multibeam_beam_variant": (I, [I]),
+    "vgb_multibeam_last_pair": (I, [V]),
     "vgb_multibeam_enable_timing": (I, [V, I]),
     "vgb_multibeam_stage_ms": (I, [V, V, I]),
     "vgb_gemm_batched": (I, [V, V, V, I, I, I, I, I, V]),
@@ -292,6 +294,15 @@ def beamform_mwax_psrfits_noalloc(v: Voltages, ncc, nspectra, filt, flags, W, na
 def gemm_bf16(A, B, C, M, N, K, stream=None):
     """C[M][N] = A[M][K] @ B[N][K]^T on the tensor cores (bf16 in, FP32 out)."""
     check(lib().vgb_gemm_bf16(ptr(A), ptr(B), ptr(C), M, N, K, stream_ptr(stream)))
+
+
+def multibeam_beam_variant(v: int) -> int:
+    """Force the many-beam GEMM kernel (0 automatic, 1 single CTA, 2 CTA
+    pairs); returns the previous setting."""
+    prev = lib().vgb_multibeam_beam_variant(v)
+    if prev < 0:
+        raise VGBError(lib().vgb_last_error().decode())
+    return prev
 
 
 def gemm_variant(v: int) -> int:
@@ -687,6 +698,10 @@ class Multibeam:
 
     def launches(self) -> int:
         return lib().vgb_multibeam_launches(self.h)
+
+    def last_pair(self) -> int:
+        """CTA pairs the last run's beam GEMM ran on (0: the single-CTA kernel)."""
+        return lib().vgb_multibeam_last_pair(self.h)
 
     def enable_timing(self, on=True):
         check(lib().vgb_multibeam_enable_timing(self.h, int(bool(on))))

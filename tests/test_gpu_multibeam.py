@@ -326,3 +326,68 @@ def test_mwax_smart_pfb_into_multibeam(vgb_mod, torch, oracle_mod):
     mb.close()
     errs = stokes_err(host(S).reshape(K, npnt, 4, ns // NINT), oracle_stokes(O, case, 4, invw))
     assert max(errs) < 1e-3, errs
+
+
+def _run_variant(vgb, torch, case, nant, npnt, nfine, ns, nstokes, precision, variant, int8=False):
+    prev = vgb.multibeam_beam_variant(variant)
+    try:
+        mb = vgb.Multibeam(1, nfine, nant, npnt, ns, nstokes=nstokes, precision=precision,
+                           input=vgb.MB_INT8 if int8 else vgb.MB_INT4)
+        mb.set_geometry(dev(case["unit"]), dev(case["east"]), dev(case["north"]), dev(case["height"]),
+                        dev(case["cable"]))
+        mb.set_jones(dev(case["D"]), dev(case["B"]), dev(case["freqs"]), dev(case["polQ"]), dev(case["polP"]))
+        nint = ns // NINT
+        S = torch.full((nfine * npnt * nstokes * nint,), float("nan"), dtype=torch.float32, device="cuda")
+        out = torch.empty(npnt * nint * nstokes * nfine, dtype=torch.uint8, device="cuda")
+        off = torch.empty(npnt * nstokes * nfine, dtype=torch.float32, device="cuda")
+        scl = torch.empty_like(off)
+        mb.run(dev(case["v_dev"]), S=S, out=out, offsets=off, scales=scl)
+        torch.cuda.synchronize()
+        assert vgb.check_device_status() == 0
+        res = dict(S=host(S), out=host(out), off=host(off), scl=host(scl), pair=mb.last_pair())
+        mb.close()
+        return res
+    finally:
+        vgb.multibeam_beam_variant(prev)
+
+
+@pytest.mark.parametrize("precision,nstokes,int8", [(0, 4, False), (2, 4, False), (1, 4, False), (0, 1, True),
+                                                    (2, 1, True)])
+def test_multibeam_pair_kernel_equals_single(vgb_mod, torch, oracle_mod, precision, nstokes, int8):
+    """The beam GEMM over CTA pairs (cta_group::2: two SMs share each 256-row
+    MMA, each staging half of the voltage tile) gives the single-CTA kernel's
+    Stokes and PSRFITS bytes bit for bit: four beam tiles (two pairs), a
+    sample count that leaves the last sample tile partly used, three fine
+    channels; and, checked against the FP64 oracle, within the mode's
+    tolerance."""
+    nant, npnt, nfine, ns = 32, 128, 3, 770
+    case = make_case(oracle_mod, nant, npnt, nfine, ns, seed=61, int8=int8)
+    single = _run_variant(vgb_mod, torch, case, nant, npnt, nfine, ns, nstokes, precision, 1, int8)
+    pair = _run_variant(vgb_mod, torch, case, nant, npnt, nfine, ns, nstokes, precision, 2, int8)
+    assert not single["pair"] and pair["pair"]
+    assert not np.isnan(pair["S"]).any()
+    for k in ("S", "out", "off", "scl"):
+        assert np.array_equal(single[k], pair[k]), k
+    ref = oracle_stokes(oracle_mod, case, nstokes, 1.0 / (2 * nant))
+    errs = stokes_err(pair["S"].reshape(nfine, npnt, nstokes, ns // NINT), ref)
+    tol = {0: 1e-3, 2: 4e-3, 1: 3e-2}[precision]
+    assert max(errs) < tol, errs
+
+
+def test_multibeam_pair_kernel_selection(vgb_mod, torch, oracle_mod):
+    """The automatic choice times both kernels where the 32-beam tiles pair up
+    (whichever it keeps, the bytes are the single-CTA kernel's) and takes the
+    single-CTA kernel otherwise (three tiles); forcing the pair kernel on three
+    tiles is an error, not a different result."""
+    nant, nfine, ns = 16, 2, 250
+    even = make_case(oracle_mod, nant, 64, nfine, ns, seed=62)
+    odd = make_case(oracle_mod, nant, 70, nfine, ns, seed=63)
+    auto = _run_variant(vgb_mod, torch, even, nant, 64, nfine, ns, 4, 0, 0)
+    single = _run_variant(vgb_mod, torch, even, nant, 64, nfine, ns, 4, 0, 1)
+    for k in ("S", "out", "off", "scl"):
+        assert np.array_equal(auto[k], single[k]), k
+    assert not _run_variant(vgb_mod, torch, odd, nant, 70, nfine, ns, 4, 0, 0)["pair"]
+    with pytest.raises(vgb_mod.VGBError, match="even number of beam tiles"):
+        _run_variant(vgb_mod, torch, odd, nant, 70, nfine, ns, 4, 0, 2)
+    with pytest.raises(vgb_mod.VGBError):
+        vgb_mod.multibeam_beam_variant(3)
