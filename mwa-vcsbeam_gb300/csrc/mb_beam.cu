@@ -57,7 +57,9 @@ constexpr int kMbInt = 10;     // samples per integration (1 ms at 10 kHz)
 constexpr int kMbUsed = 250;   // samples of a tile that are used: 25 integrations
 constexpr int kMbNint = kMbUsed / kMbInt;
 constexpr int kMbBeamsPerTile = 32;  // 128 rows / 4
-constexpr int kMbThreads = 192;      // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr int kMbEpq = 3;            // epilogue warps per TMEM lane quarter
+constexpr int kMbEpiWarps = 4 * kMbEpq;
+constexpr int kMbThreads = 64 + 32 * kMbEpiWarps; // warp 0 TMA, warp 1 MMA, warps 2.. epilogue
 constexpr uint32_t kMbPolls = 1u << 26;
 
 // Per-row statistics for the 8-bit stage, gathered by the beam epilogues: the
@@ -579,18 +581,22 @@ struct MbBeamArgs {
 };
 
 // Epilogue of one accumulator tile (beam tile m, sample tile n, fine channel
-// c) by one thread of warps 2-5: TMEM lane `row` of the 256 columns at
-// `tacc` (lane quarter and buffer included). Lanes 4b..4b+3 hold beam b's
-// Xr, Xi, Yr, Yi; XX, YY, XY are formed across them, integrated over 10
-// samples, the autocorrelation term subtracted (form_beam.cpp:300-371) and
-// Stokes written [chan][beam][stokes][t], with each row's extremes folded into
+// c) by one thread of an epilogue warp: TMEM lane `row` of the tile at `tacc`
+// (lane quarter and buffer included), integrations [kI0, kI1) of the tile's
+// 25 (columns 10 kI0 .. 10 kI1 - 1; the kMbEpq warps of a lane quarter take
+// one range each, so every Stokes value is still formed by one thread from
+// its 10 columns). Lanes 4b..4b+3 hold beam b's Xr, Xi, Yr, Yi; XX, YY, XY
+// are formed across them, integrated over 10 samples, the autocorrelation
+// term subtracted (form_beam.cpp:300-371) and Stokes written
+// [chan][beam][stokes][t], with each row's extremes folded into
 // order-preserving integer atomics for the 8-bit stage. `wait` blocks until
 // the accumulator is complete (false: it gave up, nothing is written);
 // `release` hands the TMEM buffer back once every load of it has finished.
-template <int kNst, class Wait, class Release>
+template <int kNst, int kI0, int kI1, class Wait, class Release>
 __device__ __forceinline__ bool mb_epilogue_tile(const MbBeamArgs &g, uint32_t tacc, int m, int n, int c, int row,
                                                  Wait &&wait, Release &&release)
 {
+    constexpr int kC0 = kMbInt * kI0, kC1 = kMbInt * kI1;   // columns of this range
     const int lane = threadIdx.x & 31;
     const int l = lane & 3;
     const int bl = row >> 2;
@@ -600,11 +606,11 @@ __device__ __forceinline__ bool mb_epilogue_tile(const MbBeamArgs &g, uint32_t t
     const int st = kNst == 4 ? l : 0;
     const bool writer = p < g.B && (kNst == 4 || l == 0);
     const long long rrow = (long long)c * g.Mq + (long long)p * kNst + st;
-    float rv[kMbNint];
+    float rv[kI1 - kI0];
     float qs = 0.f;
     if (writer) qs = g.qscale[rrow];
 #pragma unroll
-    for (int i = 0; i < kMbNint; i++) rv[i] = (writer && i < nv) ? g.R[rrow * g.nint_p + t0 + i] : 0.f;
+    for (int i = kI0; i < kI1; i++) rv[i - kI0] = (writer && i < nv) ? g.R[rrow * g.nint_p + t0 + i] : 0.f;
     float *srow = g.S + (((long long)c * g.B + p) * kNst + st) * g.nint + t0;
     float smin = __int_as_float(0x7f800000), smax = -__int_as_float(0x7f800000);
 
@@ -615,13 +621,13 @@ __device__ __forceinline__ bool mb_epilogue_tile(const MbBeamArgs &g, uint32_t t
     tc_fence_after();
     float sq = 0.f, pb = 0.f, pc = 0.f;
 #pragma unroll
-    for (int j = 0; j < kMbN / 32; j++) {
+    for (int j = kC0 / 32; j <= (kC1 - 1) / 32; j++) {
         float v[32];
         tmem_ld32(tacc + 32 * j, v);
 #pragma unroll
         for (int col = 0; col < 32; col++) {
             const int gcol = 32 * j + col;
-            if (gcol < kMbUsed) {
+            if (gcol >= kC0 && gcol < kC1) {
                 const float x = v[col];
                 sq = fmaf(x, x, sq);
                 if (kNst == 4) {
@@ -648,11 +654,12 @@ __device__ __forceinline__ bool mb_epilogue_tile(const MbBeamArgs &g, uint32_t t
                         val = t1;
                     }
                     if (writer && ti < nv) {
-                        const float sv = g.invw * (val - qs * rv[ti]);
+                        const float sv = g.invw * (val - qs * rv[ti - kI0]);
                         srow[ti] = sv;
                         smin = fminf(smin, sv);
                         smax = fmaxf(smax, sv);
-                        if (ti == 0 && t0 == 0) g.stats.nan0[((long long)c * g.B + p) * kNst + st] = sv != sv;
+                        if (kI0 == 0 && ti == 0 && t0 == 0)
+                            g.stats.nan0[((long long)c * g.B + p) * kNst + st] = sv != sv;
                     }
                     sq = pb = pc = 0.f;
                 }
@@ -662,12 +669,26 @@ __device__ __forceinline__ bool mb_epilogue_tile(const MbBeamArgs &g, uint32_t t
     tc_fence_before();
     __syncwarp();
     release();
-    if (writer) {
+    if (writer && kI0 < nv) {
         const long long r = ((long long)c * g.B + p) * kNst + st;
         atomicMin(&g.stats.mn[r], fkey(smin));
         atomicMax(&g.stats.mx[r], fkey(smax));
     }
     return true;
+}
+
+// Epilogue warp e (0 .. kMbEpiWarps - 1) of a CTA: lane quarter = its warp
+// index % 4 (the TMEM lanes a warp may read), integrations part e / 4 of the
+// tile's 25 split into kMbEpq ranges.
+template <int kNst, class Wait, class Release>
+__device__ __forceinline__ bool mb_epilogue_part(int part, const MbBeamArgs &g, uint32_t tacc, int m, int n, int c,
+                                                 int row, Wait &&wait, Release &&release)
+{
+    static_assert(kMbEpq == 3, "three integration ranges");
+    constexpr int a = kMbNint / 3, b = 2 * kMbNint / 3;   // 8, 16 of 25
+    if (part == 0) return mb_epilogue_tile<kNst, 0, a>(g, tacc, m, n, c, row, wait, release);
+    if (part == 1) return mb_epilogue_tile<kNst, a, b>(g, tacc, m, n, c, row, wait, release);
+    return mb_epilogue_tile<kNst, b, kMbNint>(g, tacc, m, n, c, row, wait, release);
 }
 
 template <int kPlanes, bool kF16, int kNst>
@@ -690,7 +711,7 @@ __global__ void __launch_bounds__(kMbThreads, 1)
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(&sm.tfull[b], 1);
-            mbar_init(&sm.tempty[b], 4);
+            mbar_init(&sm.tempty[b], kMbEpiWarps);
         }
         mbar_init(&sm.drain, 1);
         fence_mbar_init();
@@ -777,15 +798,15 @@ __global__ void __launch_bounds__(kMbThreads, 1)
             mbar_wait_bounded(&sm.drain, 0, kMbPolls);
         }
     } else {
-        // ---- epilogue: warps 2-5, TMEM lane quarter = warp % 4 ----
-        const int q4 = warp & 3;
+        // ---- epilogue: warps 2.., TMEM lane quarter = warp % 4, integration range (warp - 2) / 4 ----
+        const int q4 = warp & 3, part = (warp - 2) >> 2;
         uint32_t tc = 0;
         for (long long tile = blockIdx.x; tile < g.total; tile += gridDim.x, tc++) {
             const int buf = tc & 1;
             const int m = (int)(tile % g.mtiles);
             const int n = (int)((tile / g.mtiles) % g.ntn);
             const int c = (int)(tile / per_tile);
-            const bool ok = mb_epilogue_tile<kNst>(
+            const bool ok = mb_epilogue_part<kNst>(part, 
                 g, tmem + ((uint32_t)(32 * q4) << 16) + buf * kMbN, m, n, c, 32 * q4 + lane,
                 [&] { return mbar_wait_bounded(&sm.tfull[buf], (tc >> 1) & 1, kMbPolls); },
                 [&] {
@@ -820,9 +841,9 @@ __global__ void __launch_bounds__(kMbThreads, 1)
 //     MMA commit reaches in both CTAs.
 //   warp 1 lane 0 (even CTA): MMA issuer; each accumulator buffer is handed
 //     to both CTAs' epilogues (`tfull`, multicast commit) and comes back when
-//     all eight epilogue warps of the pair have arrived on the even CTA's
-//     `tempty`.
-//   warps 2-5 (both CTAs): epilogue of the CTA's own beam tile.
+//     every epilogue warp of the pair has arrived on the even CTA's `tempty`.
+//   warps 2.. (both CTAs): epilogue of the CTA's own beam tile (mb_beam_kernel's
+//     split: three warps per TMEM lane quarter, one integration range each).
 // Every wait is bounded; the CTAs meet at a cluster barrier before either
 // releases tensor memory or exits, so neither leaves while the other may
 // still signal its barriers.
@@ -866,7 +887,7 @@ __global__ void __launch_bounds__(kMbThreads, 1)
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(&sm.tfull[b], 1);
-            mbar_init(&sm.tempty[b], 8);          // four epilogue warps in each CTA
+            mbar_init(&sm.tempty[b], 2 * kMbEpiWarps); // every epilogue warp of both CTAs
         }
         mbar_init(&sm.drain, 1);
         fence_mbar_init();
@@ -957,8 +978,8 @@ __global__ void __launch_bounds__(kMbThreads, 1)
             mbar_wait_cluster(&sm.drain, 0, kMbPolls);
         }
     } else {
-        // ---- epilogue: warps 2-5 of both CTAs, TMEM lane quarter = warp % 4 ----
-        const int q4 = warp & 3;
+        // ---- epilogue: warps 2.. of both CTAs, TMEM lane quarter = warp % 4, range (warp - 2) / 4 ----
+        const int q4 = warp & 3, part = (warp - 2) >> 2;
         const uint32_t tempty0 = mapa_shared(smem_u32(&sm.tempty[0]), 0), tempty1 = mapa_shared(smem_u32(&sm.tempty[1]), 0);
         uint32_t tc = 0;
         for (long long pt = pair; pt < total; pt += npairs, tc++) {
@@ -966,7 +987,7 @@ __global__ void __launch_bounds__(kMbThreads, 1)
             const int mp = (int)(pt % mtp);
             const int n = (int)((pt / mtp) % g.ntn);
             const int c = (int)(pt / per_c);
-            const bool ok = mb_epilogue_tile<kNst>(
+            const bool ok = mb_epilogue_part<kNst>(part, 
                 g, tmem + ((uint32_t)(32 * q4) << 16) + buf * kMbN, 2 * mp + (int)rank, n, c, 32 * q4 + lane,
                 [&] { return mbar_wait_cluster(&sm.tfull[buf], (tc >> 1) & 1, kMbPolls); },
                 [&] {
