@@ -1366,9 +1366,7 @@ template <int kPlanes, bool kF16, int kNst>
 int mb_launch_beam_pair(vgb_multibeam *mb, const MbBeamArgs &a, cudaStream_t st)
 {
     auto kern = mb_beam_pair_kernel<kPlanes, kF16, kNst>;
-    // 16 KB beyond the ring: the last stage's half voltage tile is followed by
-    // memory of this CTA whatever extent the MMA reads from it
-    const int smem = (int)sizeof(Mb2Smem<kPlanes>) + 1024 + 16384;
+    const int smem = (int)sizeof(Mb2Smem<kPlanes>) + 1024;
     int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
                         "cudaFuncSetAttribute(mb_beam_pair_kernel)");
     if (rc) return rc;
