@@ -8,7 +8,9 @@ checked through properties that do not depend on size:
   oracle chain (reference tables, per-sample beamformer summed over each
   integration) within 1e-4 of each Stokes parameter's largest magnitude;
 * beams are independent: permuting the pointings (and their primary-beam
-  matrices) permutes every product, bit for bit.
+  matrices) permutes every product, bit for bit;
+* the beam GEMM over CTA pairs (cta_group::2) and the single-CTA kernel give
+  the same products, bit for bit.
 """
 import numpy as np
 import pytest
@@ -69,7 +71,16 @@ def test_multibeam_full_size(vgb_mod, torch, oracle_mod):
         return (host(S).reshape(NF, NB, 4, NT), host(out).reshape(NB, NT, 4, NF), host(off).reshape(NB, 4, NF),
                 host(scl).reshape(NB, 4, NF))
 
-    S1, u1, off1, sc1 = run(unit, B)
+    prev = vgb.multibeam_beam_variant(1)
+    try:
+        S1, u1, off1, sc1 = run(unit, B)
+        vgb.multibeam_beam_variant(2)
+        Sp, up, offp, scp = run(unit, B)
+    finally:
+        vgb.multibeam_beam_variant(prev)
+    assert np.array_equal(Sp, S1) and np.array_equal(up, u1)
+    assert np.array_equal(offp, off1) and np.array_equal(scp, sc1)
+    del Sp, up
 
     # PSRFITS bytes from the device's own Stokes, in [beam][t][stokes][chan]
     off, sc, u8 = O.renormalise(np.ascontiguousarray(S1.transpose(1, 3, 2, 0)))
