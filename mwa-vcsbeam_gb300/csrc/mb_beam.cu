@@ -917,7 +917,7 @@ __global__ void __launch_bounds__(kMbThreads, 1)
                 for (int kc = 0; kc < g.nk; kc++, it++) {
                     const int s = it % kStages;
                     const uint32_t r = it / kStages;
-                    if (r > 0 && !mbar_wait_cluster(&sm.empty[s], (r - 1) & 1, kMbPolls)) {
+                    if (r > 0 && !mbar_wait_bounded(&sm.empty[s], (r - 1) & 1, kMbPolls)) {
                         atomicOr(g.status, kErrWaitTimeout);
                         ok = false;
                         break;
@@ -935,7 +935,7 @@ __global__ void __launch_bounds__(kMbThreads, 1)
             // cluster barrier below lets either CTA leave
             if (rank == 0)
                 for (uint32_t k = (it > kStages ? it - kStages : 0); k < it; k++)
-                    mbar_wait_cluster(&sm.full[k % kStages], (k / kStages) & 1, kMbPolls);
+                    mbar_wait_bounded(&sm.full[k % kStages], (k / kStages) & 1, kMbPolls);
         }
     } else if (warp == 1) {
         if (lane == 0 && rank == 0) {
@@ -946,7 +946,7 @@ __global__ void __launch_bounds__(kMbThreads, 1)
             for (long long pt = pair; pt < total && ok; pt += npairs, tc++) {
                 const int buf = tc & 1;
                 const uint32_t u = tc >> 1;
-                if (u > 0 && !mbar_wait_cluster(&sm.tempty[buf], (u - 1) & 1, kMbPolls)) {
+                if (u > 0 && !mbar_wait_bounded(&sm.tempty[buf], (u - 1) & 1, kMbPolls)) {
                     atomicOr(g.status, kErrWaitTimeout);
                     break;
                 }
@@ -954,7 +954,7 @@ __global__ void __launch_bounds__(kMbThreads, 1)
                 const uint32_t d = tmem + buf * kMbN;
                 for (int kc = 0; kc < g.nk; kc++, it++) {
                     const int s = it % kStages;
-                    if (!mbar_wait_cluster(&sm.full[s], (it / kStages) & 1, kMbPolls)) {
+                    if (!mbar_wait_bounded(&sm.full[s], (it / kStages) & 1, kMbPolls)) {
                         atomicOr(g.status, kErrWaitTimeout);
                         ok = false;
                         break;
@@ -975,7 +975,7 @@ __global__ void __launch_bounds__(kMbThreads, 1)
             }
             // all MMAs this thread issued have completed before teardown
             tc_commit_pair_own(&sm.drain);
-            mbar_wait_cluster(&sm.drain, 0, kMbPolls);
+            mbar_wait_bounded(&sm.drain, 0, kMbPolls);
         }
     } else {
         // ---- epilogue: warps 2.. of both CTAs, TMEM lane quarter = warp % 4, range (warp - 2) / 4 ----
@@ -989,7 +989,7 @@ __global__ void __launch_bounds__(kMbThreads, 1)
             const int c = (int)(pt / per_c);
             const bool ok = mb_epilogue_part<kNst>(part, 
                 g, tmem + ((uint32_t)(32 * q4) << 16) + buf * kMbN, 2 * mp + (int)rank, n, c, 32 * q4 + lane,
-                [&] { return mbar_wait_cluster(&sm.tfull[buf], (tc >> 1) & 1, kMbPolls); },
+                [&] { return mbar_wait_bounded(&sm.tfull[buf], (tc >> 1) & 1, kMbPolls); },
                 [&] {
                     if (lane == 0) mbar_arrive_cluster(buf ? tempty1 : tempty0);
                 });

@@ -292,30 +292,13 @@ __device__ __forceinline__ void tma_load_2d_pair(void *dst, const CUtensorMap *m
                  : "memory");
 }
 
-// Arrive (release at cluster scope) on the mbarrier at shared::cluster address
-// `bar_cl`.
+// Arrive on the mbarrier at shared::cluster address `bar_cl` (this CTA's or
+// its peer's). What it hands over is tensor memory, whose reads the caller
+// has completed (tcgen05.wait::ld) and ordered (tcgen05.fence::before_
+// thread_sync) before it, so no cluster-wide memory fence is needed.
 __device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cl)
 {
-    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cl) : "memory");
-}
-
-// Bounded wait with acquire at cluster scope (the phase may have been
-// completed by the peer CTA's arrivals or copies).
-__device__ __forceinline__ bool mbar_wait_cluster(uint64_t *bar, uint32_t phase, uint32_t max_polls)
-{
-    const uint32_t addr = smem_u32(bar);
-    for (uint32_t i = 0; i < max_polls; i++) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n"
-            " mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
-            " selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(addr), "r"(phase)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
+    asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(bar_cl) : "memory");
 }
 
 // Host: build a 2-D tensor map over a row-major bf16 matrix [rows][cols]
