@@ -619,7 +619,12 @@ def gb300_arm(args, rank, local_rank, world):
                "alg_flops_per_input_spectrum": {"wola": 6144, "fft_5nlog2n": 4480, "beam_back_end": 3840},
                "achieved": fp32_achieved, "unit": "TFLOP/s",
                "peak_ffma": fp32_ffma, "peak_ffma2": fp32_ffma2, "peak_source": "measured (vgb_fp32_peak)",
-               "frac": (fp32_achieved / fp32_peak) if fp32_peak else None}
+               "frac": (fp32_achieved / fp32_peak) if fp32_peak else None,
+               # 14,464 flops per 256 voltage bytes: the HBM fraction this kernel
+               # would reach running at the FP32 peak (its ceiling on the hbm roofline)
+               "flops_per_byte": alg_flops / alg_bytes,
+               "hbm_frac_at_fp32_peak": (alg_bytes / (alg_flops / (fp32_peak * 1e12)) / 1e9 / peak)
+               if fp32_peak else None}
     if variant == 5:
         kname = "beam_tm_kernel (fused PFB + tied-array/incoherent beam + Stokes; three CTAs per SM)"
         limiter = ("not HBM: the FMA pipe and the shared-memory pipe, each ~60 % busy, issue 65 % (ncu of a "
