@@ -806,8 +806,8 @@ __global__ void __launch_bounds__(kMbThreads, 1)
             const int m = (int)(tile % g.mtiles);
             const int n = (int)((tile / g.mtiles) % g.ntn);
             const int c = (int)(tile / per_tile);
-            const bool ok = mb_epilogue_part<kNst>(part, 
-                g, tmem + ((uint32_t)(32 * q4) << 16) + buf * kMbN, m, n, c, 32 * q4 + lane,
+            const bool ok = mb_epilogue_part<kNst>(
+                part, g, tmem + ((uint32_t)(32 * q4) << 16) + buf * kMbN, m, n, c, 32 * q4 + lane,
                 [&] { return mbar_wait_bounded(&sm.tfull[buf], (tc >> 1) & 1, kMbPolls); },
                 [&] {
                     if (lane == 0) mbar_arrive(&sm.tempty[buf]);
@@ -825,9 +825,8 @@ __global__ void __launch_bounds__(kMbThreads, 1)
 // ---------------------------------------------------------------------------
 // The beam GEMM over CTA pairs (cta_group::2)
 // ---------------------------------------------------------------------------
-// mb_beam_kernel's 128 x 256 tile needs 48 KB of operands per 64-wide K step
-// from L2 for 2 M MACs (single plane): at the tensor pipe's rate that stream
-// is the limit of the single-plane modes (tensor pipe ~70 % active). Here the
+// mb_beam_kernel's 128 x 256 tile takes in 48 KB of operands per 64-wide K
+// step from L2 for 2 M MACs (single plane), 64 KB in the split mode. Here the
 // two CTAs of a cluster (the two SMs of a TPC) own beam tiles 2i and 2i + 1 of
 // the same 256-sample tile: each stages its own 128 weight rows and HALF of
 // the voltage tile (128 samples), and one thread of the even CTA issues
@@ -987,8 +986,8 @@ __global__ void __launch_bounds__(kMbThreads, 1)
             const int mp = (int)(pt % mtp);
             const int n = (int)((pt / mtp) % g.ntn);
             const int c = (int)(pt / per_c);
-            const bool ok = mb_epilogue_part<kNst>(part, 
-                g, tmem + ((uint32_t)(32 * q4) << 16) + buf * kMbN, 2 * mp + (int)rank, n, c, 32 * q4 + lane,
+            const bool ok = mb_epilogue_part<kNst>(
+                part, g, tmem + ((uint32_t)(32 * q4) << 16) + buf * kMbN, 2 * mp + (int)rank, n, c, 32 * q4 + lane,
                 [&] { return mbar_wait_bounded(&sm.tfull[buf], (tc >> 1) & 1, kMbPolls); },
                 [&] {
                     if (lane == 0) mbar_arrive_cluster(buf ? tempty1 : tempty0);
