@@ -391,3 +391,30 @@ def test_multibeam_pair_kernel_selection(vgb_mod, torch, oracle_mod):
         _run_variant(vgb_mod, torch, odd, nant, 70, nfine, ns, 4, 0, 2)
     with pytest.raises(vgb_mod.VGBError):
         vgb_mod.multibeam_beam_variant(3)
+
+
+@pytest.mark.parametrize("nant,npnt,nfine,ns,nstokes,int8", [
+    (16, 64, 1, 250, 4, False),     # one beam-tile pair, one sample tile, one 64-wide K step
+    (16, 40, 3, 10, 4, False),      # one integration: a sample tile with 10 of 256 columns used
+    (64, 256, 2, 2500, 1, True),    # 8-bit, Stokes I, 4 pairs x 10 sample tiles x 2 channels
+    (32, 64, 96, 260, 4, False),    # 1 pair x 2 sample tiles x 96 channels = 192 pair tiles
+    (32, 96, 4, 260, 4, False),     # three beam tiles: odd, so the automatic choice is one CTA
+])
+def test_multibeam_pair_kernel_edges(vgb_mod, torch, oracle_mod, nant, npnt, nfine, ns, nstokes, int8):
+    """The CTA-pair beam GEMM at the edges of its tiling equals the single-CTA
+    kernel bit for bit (where the beam tiles pair up), including runs with
+    more beam-tile pairs than co-resident clusters (80 and 192 pair tiles on
+    at most 76 clusters)."""
+    case = make_case(oracle_mod, nant, npnt, nfine, ns, seed=71, int8=int8)
+    single = _run_variant(vgb_mod, torch, case, nant, npnt, nfine, ns, nstokes, 0, 1, int8)
+    bp = (npnt + 31) // 32
+    if bp % 2:
+        auto = _run_variant(vgb_mod, torch, case, nant, npnt, nfine, ns, nstokes, 0, 0, int8)
+        assert not auto["pair"]
+        other = auto
+    else:
+        other = _run_variant(vgb_mod, torch, case, nant, npnt, nfine, ns, nstokes, 0, 2, int8)
+        assert other["pair"] > 0
+    for k in ("S", "out", "off", "scl"):
+        assert np.array_equal(single[k], other[k]), k
+    assert not np.isnan(single["S"]).any()
