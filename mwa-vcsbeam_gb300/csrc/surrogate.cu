@@ -486,6 +486,7 @@ struct vgb_surrogate {
     unsigned *cell_err = nullptr, *max_err = nullptr, *nfallback = nullptr;
     float tol = 1e-3f;
     bool validated = false;
+    std::vector<int> cells_ok;           // per delay set: sky cells within the tolerance (host copy)
     long long step = 0;
     float *Jsur = nullptr;
     double2 *Bsur = nullptr;
@@ -974,6 +975,12 @@ extern "C" int vgb_surrogate_validate(vgb_surrogate *s, long long nval, float to
     for (size_t i = 0; i < ncell; i++)
         if (h[i] == 0u) h[i] = 0x7f800000u;
     rc = check_cuda(cudaMemcpy(s->cell_err, h.data(), ncell * sizeof(unsigned), cudaMemcpyHostToDevice), "cudaMemcpy");
+    s->cells_ok.assign(s->nsets, 0);
+    for (size_t i = 0; i < ncell; i++) {
+        float f;
+        std::memcpy(&f, &h[i], sizeof(f));
+        if (f <= tol) s->cells_ok[i / (kSurNaz * kSurNza)]++;
+    }
     if (max_err) std::memcpy(max_err, &mx, sizeof(float));
     if (frac_cells_ok) *frac_cells_ok = (float)ok / (float)ncell;
     s->tol = tol;
@@ -996,15 +1003,40 @@ extern "C" int vgb_surrogate_beam(vgb_surrogate *s, const double *az, const doub
     // the network runs only for the delay sets some tile uses (as vmCalcB
     // evaluates once per distinct configuration)
     std::vector<int> ts(ntile), list, slot(s->nsets, -1);
+    std::vector<double> zah(npointing);
     int rc = check_cuda(cudaMemcpyAsync(ts.data(), tile_set, sizeof(int) * ntile, cudaMemcpyDeviceToHost, caller),
                         "cudaMemcpyAsync(tile_set)");
+    if (!rc)
+        rc = check_cuda(cudaMemcpyAsync(zah.data(), za, sizeof(double) * npointing, cudaMemcpyDeviceToHost, caller),
+                        "cudaMemcpyAsync(za)");
     if (!rc) rc = check_cuda(cudaStreamSynchronize(caller), "cudaStreamSynchronize");
     if (rc) return rc;
-    for (int t = 0; t < ntile; t++)
-        if (ts[t] >= 0 && ts[t] < s->nsets && slot[ts[t]] < 0) {
-            slot[ts[t]] = (int)list.size();
-            list.push_back(ts[t]);
+    bool every_tile_trained = true;
+    for (int t = 0; t < ntile; t++) {
+        if (ts[t] >= 0 && ts[t] < s->nsets) {
+            if (slot[ts[t]] < 0) {
+                slot[ts[t]] = (int)list.size();
+                list.push_back(ts[t]);
+            }
+        } else {
+            every_tile_trained = false;
         }
+    }
+    // Work whose answers would all be discarded is skipped (the products are
+    // the same): the network when no sky cell of the sets in use is within
+    // the tolerance (every entry falls back), the plain model when every cell
+    // is, every tile's set was trained and every pointing is within the
+    // trained zenith angles (no entry falls back).
+    bool any_cell_ok = false, all_cells_ok = every_tile_trained;
+    for (int k : list) {
+        any_cell_ok |= s->cells_ok[k] > 0;
+        all_cells_ok &= s->cells_ok[k] == kSurNaz * kSurNza;
+    }
+    for (double z : zah) all_cells_ok &= z <= kSurZaMax;
+    if (!any_cell_ok) {
+        list.clear();
+        for (int &k : slot) k = -1;
+    }
     const int nslots = (int)list.size();
     const long long rows = (long long)nfreq * npointing * nslots;
     std::vector<int> map(2 * s->nsets, 0);
@@ -1059,7 +1091,7 @@ extern "C" int vgb_surrogate_beam(vgb_surrogate *s, const double *az, const doub
     }
     // fallback answers: the plain model for every entry (once per distinct
     // delay set, copied to tiles), then the network's answers overwrite it
-    if (!rc) {
+    if (!rc && !all_cells_ok) {
         PbArgs pb{az, za, npointing, freq_hz, nfreq, delays, ntile, latitude, pa_correction, static_cast<double2 *>(B)};
         rc = launch_beam_model(pb, s->st);
     }

@@ -102,9 +102,11 @@ def test_what_the_trained_network_gains(vgb_mod):
         and no gain;
       * at a loose 0.1 tolerance the network answers queries, each within
         twice the validated tolerance of the plain model;
-      * the surrogate path is slower than the plain model either way (the
-        analytic stand-in is a 16-term sum; the network would pay only
-        against a model as costly as the FEE one).
+      * where the network answers, the surrogate path is slower than the
+        plain model (the analytic stand-in is a 16-term sum; the network
+        would pay only against a model as costly as the FEE one); where no
+        sky cell qualifies it skips the network, so it costs less than
+        where the network runs.
     The measured numbers are printed."""
     torch = torch_cuda()
     nsets, nfreq = 16, 24
@@ -145,5 +147,5 @@ def test_what_the_trained_network_gains(vgb_mod):
     strict, loose = out[1e-3], out[0.1]
     assert strict["cells_within"] == 0.0 and strict["fallback_fraction"] == 1.0 and strict["max_B_error"] == 0.0
     assert loose["fallback_fraction"] < 1.0 and loose["max_B_error"] <= 2 * 0.1
-    assert strict["surrogate_ms"] > ms_plain and loose["surrogate_ms"] > ms_plain
+    assert loose["surrogate_ms"] > ms_plain and strict["surrogate_ms"] < loose["surrogate_ms"]
     s.close()
