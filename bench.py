@@ -789,10 +789,13 @@ def multibeam_section(torch, vgb, SY, iters: int, cases=None, modes=None, nfine=
                                      "mma_issued_tflops": mma_tf, "mma_frac": mma_tf / peak_tf,
                                      "peak_source": "measured" if "bf16_tflops" in peaks else "fallback"}
             case["modes"][mode] = entry
-        # end to end: 4 coarse channel-seconds per call from pinned host memory
+        # end to end: 8 coarse channel-seconds per call from pinned host memory
+        # (the caller's stream completes once a call's products are on the
+        # host, so the next call's compute waits for the previous call's last
+        # download: a batch of 8 spreads that over 8 channel-seconds)
         # through vgb_multibeam_run_host (uploads, compute and downloads overlap)
         if name == "C4" and stream_iters > 0:
-            ncs = 4
+            ncs = 8
             for mode, prec in MB_MODES:
                 if prec == 3 or (modes and mode not in modes):
                     continue
