@@ -186,6 +186,25 @@ __device__ __forceinline__ void c4_to_f(uint32_t w, float2 &re, float2 &im)
               bias);
 }
 
+// The same four values by the integer-to-float conversion of each signed
+// byte (exact). The conversion pipe issues 16 per clock per SM but otherwise
+// idles here, while the FMA pipe, which the form above loads with one
+// operation per value, is this kernel's busiest: without FPGA rounding this
+// form is the faster (full band 21.40 -> 21.12 ms per data-second). With it
+// the rounding and 4-bit demotion keep the conversion pipe busy and the form
+// above is the faster (24.5 against 25.4 ms).
+__device__ __forceinline__ void c4_to_f_cvt(uint32_t w, float2 &re, float2 &im)
+{
+    re = make_float2((float)(signed char)(w & 0xFFu), (float)(signed char)((w >> 16) & 0xFFu));
+    im = make_float2((float)(signed char)((w >> 8) & 0xFFu), (float)(signed char)(w >> 24));
+}
+
+template <bool kFpga> __device__ __forceinline__ void widen4(uint32_t w, float2 &re, float2 &im)
+{
+    if constexpr (kFpga) c4_to_f(w, re, im);
+    else c4_to_f_cvt(w, re, im);
+}
+
 __device__ __forceinline__ void c4_to_i(uint32_t w, int (&re)[2], int (&im)[2])
 {
     re[0] = (int)(signed char)(w & 0xFFu);
@@ -298,7 +317,7 @@ __device__ __forceinline__ void wola_rows(const char2 *stage_in, float2 (*rows)[
 #pragma unroll
             for (int w = mb; w < mb + kH + kP - 1; w++) {
                 float2 xr, xi;
-                c4_to_f(x[w * (kK / 2)], xr, xi);
+                widen4<kFpga>(x[w * (kK / 2)], xr, xi);
 #pragma unroll
                 for (int p = 0; p < kP; p++) {
                     const int m = w - p - mb;
@@ -326,7 +345,7 @@ __device__ __forceinline__ void wola_rows(const char2 *stage_in, float2 (*rows)[
 #pragma unroll
         for (int w = 0; w < kWin; w++) {
             float2 xr, xi;
-            c4_to_f(x[w * (kK / 2)], xr, xi);
+            widen4<kFpga>(x[w * (kK / 2)], xr, xi);
 #pragma unroll
             for (int p = 0; p < kP; p++) {
                 const int m = w - p;
