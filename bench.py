@@ -48,8 +48,8 @@ NI = 2 * NANT
 NSPEC = NBLK * 500
 SECOND_BYTES = NBLK * NI * 64000 * 2           # one coarse channel, one second
 BEAM_KERNEL_DRAM_BYTES_PER_CC = (1.322368e9 + 86.6944e6) / 2
-# the same for the three-CTAs-per-SM shape (variant 5): 1.323002 GB read + 86.5 MB written
-BEAM_TM_KERNEL_DRAM_BYTES_PER_CC = (1.323002e9 + 86.53568e6) / 2
+# the same for the three-CTAs-per-SM shape (variant 5): 1.321426 GB read + 85.7 MB written
+BEAM_TM_KERNEL_DRAM_BYTES_PER_CC = (1.321426e9 + 85.663232e6) / 2
 # Algorithmic FP32 flops of the fused PFB + beamformer per (RF input, fine
 # spectrum): the 12-tap weighted overlap-add of 128 complex samples
 # (12 x 2 x 2 x 128 = 6,144), a 128-point complex FFT counted as 5 N log2 N
@@ -627,9 +627,9 @@ def gb300_arm(args, rank, local_rank, world):
                if fp32_peak else None}
     if variant == 5:
         kname = "beam_tm_kernel (fused PFB + tied-array/incoherent beam + Stokes; three CTAs per SM)"
-        limiter = ("not HBM: the FMA pipe and the shared-memory pipe, each ~60 % busy, issue 65 % (ncu of a "
-                   "2-channel launch: issue 65.3 %, FMA pipe 59.6 %, shared-memory wavefronts 62.4 % of peak, "
-                   "math-pipe throttle the second stall reason; DRAM 1.41 GB in 1.875 ms)")
+        limiter = ("not HBM: the FMA pipe and the shared-memory pipe, each ~60 % busy (ncu of a 2-channel "
+                   "launch: issue 62.7 %, FMA pipe 56.0 %, shared-memory wavefronts 63 % of peak, conversions "
+                   "on the XU pipe 17.3 %, math-pipe throttle the second stall reason; DRAM 1.41 GB in 1.854 ms)")
     else:
         kname = "beam_kernel (fused PFB + tied-array/incoherent beam + Stokes)"
         limiter = ("not HBM: instruction issue, the FMA pipe and the shared-memory pipe, each ~60 % busy "
