@@ -487,7 +487,10 @@ int vgb_surrogate_validate(vgb_surrogate *s, long long nval, float tol, float *m
  * with plain-model fallback; nfallback (host, nullable) receives the number
  * of (frequency, pointing, tile) entries the plain model answered. The
  * network runs once per (frequency, pointing) for each delay set some tile
- * uses; tile_set is read back to the host on `stream` (the call waits for it). */
+ * uses; tile_set and za are read back to the host on `stream` (the call waits
+ * for them) to skip work whose answers would be discarded. When no sky cell
+ * of any trained set passed the last validation's tolerance, the call is the
+ * plain model on `stream` (nothing read back, nothing waited for). */
 int vgb_surrogate_beam(vgb_surrogate *s, const double *az, const double *za, int npointing, const double *freq_hz,
                        int nfreq, const int *tile_set, const uint32_t *delays, int ntile, double latitude,
                        int pa_correction, void *B, unsigned *nfallback, void *stream);

@@ -1000,6 +1000,17 @@ extern "C" int vgb_surrogate_beam(vgb_surrogate *s, const double *az, const doub
     if ((reinterpret_cast<uintptr_t>(delays) | reinterpret_cast<uintptr_t>(B)) & 15)
         return set_error(VGB_ERR_INVALID, "surrogate_beam: delays and B must be 16-byte aligned");
     cudaStream_t caller = static_cast<cudaStream_t>(stream);
+    // No sky cell of any trained set within the tolerance: every query falls
+    // back, so the answer is the plain model's, on the caller's stream, with
+    // no reads of the tile sets to the host.
+    bool none_ok = true;
+    for (int k : s->cells_ok) none_ok &= k == 0;
+    if (none_ok) {
+        PbArgs pb{az, za, npointing, freq_hz, nfreq, delays, ntile, latitude, pa_correction, static_cast<double2 *>(B)};
+        const int rc0 = launch_beam_model(pb, caller);
+        if (!rc0 && nfallback) *nfallback = (unsigned)((long long)nfreq * npointing * ntile);
+        return rc0;
+    }
     // the network runs only for the delay sets some tile uses (as vmCalcB
     // evaluates once per distinct configuration)
     std::vector<int> ts(ntile), list, slot(s->nsets, -1);
