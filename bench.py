@@ -824,7 +824,8 @@ def multibeam_section(torch, vgb, SY, iters: int, cases=None, modes=None, nfine=
                     "value": ccs / dt / NCC, "unit": UNIT, "ms_per_cc_s": 1e3 * dt / ccs,
                     "h2d_bytes_per_cc_s": nbytes, "d2h_bytes_per_cc_s": int(oh.numel() + 8 * offh.numel()) // ncs,
                     "path": f"vgb_multibeam_run_host, {ncs} coarse channel-seconds per call from pinned host memory, "
-                            f"{stream_iters} calls timed (wall clock), products back to pinned host memory"}
+                            f"{stream_iters} calls timed (wall clock; {ccs / NCC:g} data-seconds of the full band), "
+                            "products back to pinned host memory"}
                 del vh, oh, offh, sclh
         m = case["modes"]
         # each tensor mode against the plain FP32 CUDA-core path on the same
@@ -1061,7 +1062,9 @@ def main():
     ap.add_argument("--mb-nfine", type=int, default=K, help="profiling: fine channels per case")
     ap.add_argument("--mb-beam-variant", type=int, default=0, choices=[0, 1, 2],
                     help="many-beam GEMM kernel: 0 automatic, 1 single CTA, 2 CTA pairs")
-    ap.add_argument("--mb-stream-iters", type=int, default=3, help="many-beam host-streaming calls timed (0: skip)")
+    ap.add_argument("--mb-stream-iters", type=int, default=30,
+                    help="many-beam host-streaming calls timed, 8 coarse channel-seconds each (30: 10 data-seconds "
+                         "of the full band; 0: skip)")
     ap.add_argument("--no-pfb-only", dest="pfb_only", action="store_false",
                     help="skip the PFB-only (fine_pfb_offline) section")
     ap.add_argument("--pfb-variant", type=int, default=0, choices=[0, 3, 4, 5, 8],
