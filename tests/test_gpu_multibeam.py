@@ -209,38 +209,45 @@ def test_multibeam_psrfits_repeat_runs(vgb_mod, torch, oracle_mod):
     mb.close()
 
 
-def test_multibeam_run_host_streams(vgb_mod, torch, oracle_mod):
+@pytest.mark.parametrize("npnt,variant", [(32, 0), (64, 2)])
+def test_multibeam_run_host_streams(vgb_mod, torch, oracle_mod, npnt, variant):
     """Three coarse channels from pinned host memory through the two device
-    slots: the bytes equal vgb_multibeam_run's on device-resident input."""
-    nant, npnt, nfine, ns, ncc = 16, 32, 32, 200, 3
-    vgb = vgb_mod
-    cases = [make_case(oracle_mod, nant, npnt, nfine, ns, seed=30 + k) for k in range(ncc)]
-    c0 = cases[0]
-    mb = vgb.Multibeam(ncc, nfine, nant, npnt, ns, nstokes=4)
-    mb.set_geometry(dev(c0["unit"]), dev(c0["east"]), dev(c0["north"]), dev(c0["height"]), dev(c0["cable"]))
-    D = np.ascontiguousarray(np.stack([c["D"] for c in cases]))
-    B = np.ascontiguousarray(np.stack([c["B"] for c in cases]))
-    F = np.ascontiguousarray(np.concatenate([c["freqs"] for c in cases]))
-    mb.set_jones(dev(D), dev(B), dev(F), dev(c0["polQ"]), dev(c0["polP"]))
-    v = np.ascontiguousarray(np.stack([c["v_dev"] for c in cases]))
-    nint = ns // NINT
-    nout, nstat = ncc * npnt * nint * 4 * nfine, ncc * npnt * 4 * nfine
-    out_d = torch.empty(nout, dtype=torch.uint8, device="cuda")
-    off_d = torch.empty(nstat, dtype=torch.float32, device="cuda")
-    scl_d = torch.empty_like(off_d)
-    mb.run(dev(v), out=out_d, offsets=off_d, scales=scl_d)
-    v_h = torch.from_numpy(v.reshape(-1).copy()).pin_memory()
-    out_h = torch.zeros(nout, dtype=torch.uint8).pin_memory()
-    off_h = torch.zeros(nstat, dtype=torch.float32).pin_memory()
-    scl_h = torch.zeros(nstat, dtype=torch.float32).pin_memory()
-    st = torch.cuda.current_stream()
-    mb.run_host(v_h, out_h, off_h, scl_h, stream=st)
-    st.synchronize()
-    assert vgb.check_device_status() == 0
-    assert torch.equal(out_h, out_d.cpu())
-    assert torch.equal(off_h, off_d.cpu()) and torch.equal(scl_h, scl_d.cpu())
-    assert mb.launches() == 5 * ncc
-    mb.close()
+    slots: the bytes equal vgb_multibeam_run's on device-resident input (one
+    beam tile, single-CTA GEMM; and two, over CTA pairs)."""
+    nant, nfine, ns, ncc = 16, 32, 200, 3
+    prev = vgb_mod.multibeam_beam_variant(variant)
+    try:
+        vgb = vgb_mod
+        cases = [make_case(oracle_mod, nant, npnt, nfine, ns, seed=30 + k) for k in range(ncc)]
+        c0 = cases[0]
+        mb = vgb.Multibeam(ncc, nfine, nant, npnt, ns, nstokes=4)
+        mb.set_geometry(dev(c0["unit"]), dev(c0["east"]), dev(c0["north"]), dev(c0["height"]), dev(c0["cable"]))
+        D = np.ascontiguousarray(np.stack([c["D"] for c in cases]))
+        B = np.ascontiguousarray(np.stack([c["B"] for c in cases]))
+        F = np.ascontiguousarray(np.concatenate([c["freqs"] for c in cases]))
+        mb.set_jones(dev(D), dev(B), dev(F), dev(c0["polQ"]), dev(c0["polP"]))
+        v = np.ascontiguousarray(np.stack([c["v_dev"] for c in cases]))
+        nint = ns // NINT
+        nout, nstat = ncc * npnt * nint * 4 * nfine, ncc * npnt * 4 * nfine
+        out_d = torch.empty(nout, dtype=torch.uint8, device="cuda")
+        off_d = torch.empty(nstat, dtype=torch.float32, device="cuda")
+        scl_d = torch.empty_like(off_d)
+        mb.run(dev(v), out=out_d, offsets=off_d, scales=scl_d)
+        v_h = torch.from_numpy(v.reshape(-1).copy()).pin_memory()
+        out_h = torch.zeros(nout, dtype=torch.uint8).pin_memory()
+        off_h = torch.zeros(nstat, dtype=torch.float32).pin_memory()
+        scl_h = torch.zeros(nstat, dtype=torch.float32).pin_memory()
+        st = torch.cuda.current_stream()
+        mb.run_host(v_h, out_h, off_h, scl_h, stream=st)
+        st.synchronize()
+        assert vgb.check_device_status() == 0
+        assert torch.equal(out_h, out_d.cpu())
+        assert torch.equal(off_h, off_d.cpu()) and torch.equal(scl_h, scl_d.cpu())
+        assert mb.launches() == 5 * ncc
+        assert (mb.last_pair() > 0) == (variant == 2)
+        mb.close()
+    finally:
+        vgb_mod.multibeam_beam_variant(prev)
 
 
 def test_multibeam_all_tiles_flagged(vgb_mod, torch, oracle_mod):

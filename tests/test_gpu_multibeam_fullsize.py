@@ -106,3 +106,60 @@ def test_multibeam_full_size(vgb_mod, torch, oracle_mod):
     assert np.array_equal(u2, u1[perm])
     assert np.array_equal(off2, off1[perm]) and np.array_equal(sc2, sc1[perm])
     torch.cuda.empty_cache()
+
+
+def test_multibeam_c3_full_size(vgb_mod, torch, oracle_mod):
+    """The 256-beam case at its full size (128 tiles x 2 pols of 8-bit
+    voltages, 256 beams, 128 fine channels x 1 s, Stokes I at 1 ms): the
+    CTA-pair and single-CTA beam GEMMs give the same split-BF16 products bit
+    for bit; the PSRFITS bytes, offsets and scales are the oracle's
+    renormalise of the device's Stokes; FP16 weights stay within 1e-3 and
+    split BF16 within 1e-5 of FP32 weights on the CUDA cores, all on the same
+    voltages and tables."""
+    O, vgb = oracle_mod, vgb_mod
+    nant, nb, nf, ns = 128, 256, 128, 10000
+    nt = ns // NINT
+    D = SY.calibration_jones(nant, nf, seed=13)
+    B = np.ascontiguousarray(SY.identity_beam(nb, nant) +
+                             0.05 * (1 + 1j) * O.gauss(17, nb * nant * 4).reshape(nb, nant, 2, 2))
+    east, north, height, cable = SY.tile_layout(nant, seed=15)
+    az, za = SY.grid_pointings(16, 0.02)
+    unit = np.ascontiguousarray(SY.unit_vectors(az, za))
+    freqs = SY.fine_chan_freqs_hz(SY.coarse_chan_start_hz(3))[:nf].astype(np.float64)
+    polQ, polP = pol_lists(np.arange(2 * nant))
+    g = torch.Generator(device="cuda").manual_seed(19)
+    v = torch.randn(ns * nf * 2 * nant * 2, device="cuda", generator=g).mul_(16).round_().clamp_(-127, 127)
+    v = v.to(torch.int8).view(torch.uint8)
+    invw = 1.0 / (2 * nant)
+
+    def run(precision, variant):
+        prev = vgb.multibeam_beam_variant(variant)
+        try:
+            mb = vgb.Multibeam(1, nf, nant, nb, ns, nstokes=1, precision=precision, input=vgb.MB_INT8, invw=invw)
+            mb.set_geometry(dev(unit), dev(east), dev(north), dev(height), dev(cable))
+            mb.set_jones(dev(D), dev(B), dev(freqs), dev(polQ), dev(polP))
+            S = torch.empty(nf * nb * nt, dtype=torch.float32, device="cuda")
+            out = torch.empty(nb * nt * nf, dtype=torch.uint8, device="cuda")
+            off = torch.empty(nb * nf, dtype=torch.float32, device="cuda")
+            scl = torch.empty_like(off)
+            mb.run(v, S=S, out=out, offsets=off, scales=scl)
+            torch.cuda.synchronize()
+            assert vgb.check_device_status() == 0
+            pair = mb.last_pair()
+            mb.close()
+            return S, host(out).reshape(nb, nt, 1, nf), host(off).reshape(nb, 1, nf), host(scl).reshape(nb, 1, nf), pair
+        finally:
+            vgb.multibeam_beam_variant(prev)
+
+    S1, u1, o1, c1, p1 = run(vgb.MB_SPLIT_BF16, 1)
+    S2, u2, o2, c2, p2 = run(vgb.MB_SPLIT_BF16, 2)
+    assert p1 == 0 and p2 > 0
+    assert torch.equal(S1, S2) and np.array_equal(u1, u2) and np.array_equal(o1, o2) and np.array_equal(c1, c2)
+    off, sc, u8 = O.renormalise(np.ascontiguousarray(host(S1).reshape(nf, nb, 1, nt).transpose(1, 3, 2, 0)))
+    assert np.array_equal(u1, u8) and np.array_equal(o1, off) and np.array_equal(c1, sc)
+    S32 = run(vgb.MB_FP32, 0)[0]
+    S16 = run(vgb.MB_FP16, 0)[0]
+    scale = S32.abs().max().item()
+    assert (S1 - S32).abs().max().item() / scale < 1e-5
+    assert (S16 - S32).abs().max().item() / scale < 1e-3
+    torch.cuda.empty_cache()
